@@ -1,0 +1,186 @@
+"""Generate the golden vectors in this folder from the reference itself.
+
+Run in a checkout that has the reference next to it (the default location is
+``/root/reference``; override with ``PYRO_REFERENCE_ROOT``)::
+
+    python tests/golden/make_golden.py
+
+For each mechanism below it
+
+1. builds the mechanism with :mod:`pyrometheus_gb300.synthetic` and stores
+   its Cantera-YAML text (so the tests rebuild exactly the same mechanism);
+2. renders the reference's ``PythonCodeGenerator`` class for it
+   (``oracle/refgen.py``: the reference's generator with stand-ins for its
+   uninstalled Cantera/pymbolic/mako dependencies);
+3. evaluates the reference's generated methods with numpy on seeded states
+   and stores inputs and outputs;
+4. evaluates the same generated class on torch CPU float64 tensors and
+   differentiates the constant-pressure reactor source with
+   ``torch.func.jacfwd`` -- the stand-in for the reference's
+   ``jax.jacfwd`` over its generated class (``test/test.py:335-347``,
+   ``flamelets/equations.py:124-129``, ``examples/free_flame/reactors.py:125``).
+
+The outputs are small ``.npz`` files; this script is the only thing that
+writes them.
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import refgen  # noqa: E402
+from pyrometheus_gb300 import synthetic  # noqa: E402
+from pyrometheus_gb300.mechanism import gas_constant  # noqa: E402
+from pyrometheus_gb300.yaml_mech import dump_mechanism  # noqa: E402
+
+
+def quirks_mechanism():
+    """Small mechanism exercising irreversible reactions, explicit reaction
+    orders and a zero default efficiency."""
+    sol = synthetic.make_mechanism(synthetic.SPECIES_9, 18, 3, 2, 1, seed=7,
+                                   irreversible_fraction=0.35,
+                                   name="quirks9")
+    rng = np.random.default_rng(70)
+    n_orders = 0
+    for r in sol.reactions():
+        if not r.reversible and n_orders < 3:
+            r.orders = {sp: float(np.round(rng.uniform(0.3, 1.7), 2))
+                        for sp in r.reactants}
+            n_orders += 1
+    tb = [r for r in sol.reactions()
+          if r.reaction_type == "three-body-Arrhenius"]
+    tb[0].third_body.default_efficiency = 0.0
+    return sol
+
+
+def edge_states(sol, n, seed):
+    t, p, y = synthetic.sample_states(sol, n, seed=seed)
+    # the strict T > Tmid branch (chem_expr.py:54) at exactly Tmid,
+    # the ends of the range, and exact zeros in the composition
+    t[0], t[1], t[2] = 1000.0, 300.0, 3000.0
+    y[:, 3] = 0.0
+    y[sol.species_index("N2"), 3] = 1.0
+    zero = [k for k in range(sol.n_species) if k % 3 == 1]
+    y[zero, 4] = 0.0
+    y[:, 4] /= y[:, 4].sum()
+    return t, p, y
+
+
+class _TorchNS:
+    """``pyro_np`` namespace mapping the generated code's calls to torch."""
+
+    def __init__(self):
+        import torch
+        self.torch = torch
+        self.linalg = torch.linalg
+
+    def __getattr__(self, name):
+        return getattr(self.torch, name)
+
+
+def torch_reference(cls):
+    import torch
+
+    class TorchThermo(cls):
+        def _pyro_make_array(self, res_list):
+            ts = [x if isinstance(x, torch.Tensor) else torch.tensor(
+                float(x), dtype=torch.float64) for x in res_list]
+            ts = torch.broadcast_tensors(*ts)
+            return torch.stack(ts)
+
+        def _pyro_norm(self, argument, normord):
+            return torch.linalg.norm(argument, normord)
+
+    return TorchThermo(_TorchNS())
+
+
+def reactor_jacobian(cls, p, t, y):
+    """``jacfwd`` of ``[dT/dt, dY/dt]`` (adiabatic, constant p) w.r.t.
+    ``(T, Y)`` through the reference's generated methods."""
+    import torch
+    from torch.func import jacfwd, vmap
+    th = torch_reference(cls)
+    mw = torch.tensor(th.molecular_weights, dtype=torch.float64)
+
+    def source(x, pres):
+        temp, mass = x[0], x[1:]
+        rho = th.get_density(pres, temp, mass)
+        w = th.get_net_production_rates(rho, temp, mass)
+        h_rt = th.get_species_enthalpies_rt(temp)
+        cp = th.get_mixture_specific_heat_cp_mass(temp, mass)
+        tdot = -(th.gas_constant * temp * (h_rt * w).sum()) / (rho * cp)
+        return torch.cat([tdot[None], mw * w / rho])
+
+    x = torch.tensor(np.concatenate([t[None, :], y], axis=0).T)
+    pres = torch.tensor(p)
+    jac = vmap(jacfwd(source), in_dims=(0, 0))(x, pres)
+    val = vmap(source, in_dims=(0, 0))(x, pres)
+    return jac.numpy(), val.numpy().T
+
+
+def golden(sol, n, seed, n_jac, fname):
+    cls = refgen.reference_class(sol)
+    ref = cls()
+    t, p, y = edge_states(sol, n, seed)
+    mmw = ref.get_mixture_molecular_weight(y)
+    rho = p * mmw / (gas_constant * t)
+    c = np.array(list(ref.get_concentrations(rho, y)))
+
+    def arr(x):
+        return np.array([np.broadcast_to(np.asarray(v, dtype=np.float64),
+                                         (n,)) for v in x])
+
+    out = dict(
+        T=t, P=p, Y=y, rho=rho, conc=c,
+        mmw=np.asarray(mmw),
+        pressure=np.asarray(ref.get_pressure(rho, t, y)),
+        cp_r=arr(ref.get_species_specific_heats_r(t)),
+        h_rt=arr(ref.get_species_enthalpies_rt(t)),
+        s_r=arr(ref.get_species_entropies_r(t)),
+        g_rt=arr(ref.get_species_gibbs_rt(t)),
+        dcp_r=arr(ref.get_species_specific_heats_r_derivative(t)),
+        dh_rt=arr(ref.get_species_enthalpies_rt_derivative(t)),
+        ds_r=arr(ref.get_species_entropies_rt_derivative(t)),
+        cp_mass=np.asarray(ref.get_mixture_specific_heat_cp_mass(t, y)),
+        cv_mass=np.asarray(ref.get_mixture_specific_heat_cv_mass(t, y)),
+        h_mass=np.asarray(ref.get_mixture_enthalpy_mass(t, y)),
+        e_mass=np.asarray(ref.get_mixture_internal_energy_mass(t, y)),
+        log_k_eq=arr(ref.get_equilibrium_constants(t)),
+        k_fwd=arr(ref.get_fwd_rate_coefficients(t, c)),
+        r_net=arr(ref.get_net_rates_of_progress(t, c)),
+        r_fwd=arr(ref.get_fwd_rates_of_progress(t, c)),
+        r_rev=arr(ref.get_rev_rates_of_progress(t, c)),
+        wdot=arr(ref.get_net_production_rates(rho, t, y)),
+        cdot=arr(ref.get_creation_rates(rho, t, y)),
+        ddot=arr(ref.get_destruction_rates(rho, t, y)),
+    )
+    e = out["e_mass"]
+    h = out["h_mass"]
+    out["T_from_e"] = np.asarray(ref.get_temperature(e, 1500.0, y, True))
+    out["T_from_h"] = np.asarray(ref.get_temperature(h, 1500.0, y, False))
+    jac, src = reactor_jacobian(cls, p[:n_jac], t[:n_jac], y[:, :n_jac])
+    out["jac"] = jac
+    out["reactor_source"] = src
+    out["mech_yaml"] = np.array(dump_mechanism(sol))
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+    print(f"wrote {fname}: S={sol.n_species} R={sol.n_reactions} N={n} "
+          f"jac={n_jac}")
+
+
+def main():
+    if not refgen.reference_available():
+        raise SystemExit("reference checkout not found")
+    golden(synthetic.config1_mechanism(), 256, 11, 24, "synthetic9.npz")
+    golden(synthetic.config2_mechanism(), 48, 12, 6, "synthetic53.npz")
+    golden(quirks_mechanism(), 128, 13, 12, "quirks9.npz")
+
+
+if __name__ == "__main__":
+    main()

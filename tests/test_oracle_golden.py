@@ -1,0 +1,118 @@
+"""The CPU oracle against golden vectors produced by the reference's own
+generator (``tests/golden/make_golden.py``), plus the identities the
+reference's tests check (``test/test.py:125-297``)."""
+
+import numpy as np
+import pytest
+
+from conftest import load_golden, rel_err
+from oracle.thermo_oracle import Thermochemistry as Oracle
+from pyrometheus_gb300 import synthetic
+from pyrometheus_gb300.yaml_mech import dump_mechanism
+
+# The reference's own acceptance thresholds (test/test.py): thermo 1e-13,
+# rate coefficients 1e-13 relative, falloff 4e-14, temperature 1e-10 K.
+# The oracle restates the same formulas, so it is held to 1e-13 everywhere.
+TOL = 1e-13
+
+
+def test_synthetic_mechanisms_are_reproducible():
+    for name, make in (("synthetic9", synthetic.config1_mechanism),
+                       ("synthetic53", synthetic.config2_mechanism)):
+        sol, _ = load_golden(name)
+        assert dump_mechanism(make()) == dump_mechanism(sol)
+
+
+def test_thermo(golden):
+    sol, g = golden
+    o = Oracle(sol)
+    t = g["T"]
+    assert rel_err(o.get_species_specific_heats_r(t), g["cp_r"]) < TOL
+    assert rel_err(o.get_species_enthalpies_rt(t), g["h_rt"]) < TOL
+    assert rel_err(o.get_species_entropies_r(t), g["s_r"]) < TOL
+    assert rel_err(o.get_species_gibbs_rt(t), g["g_rt"]) < TOL
+    assert rel_err(o.get_species_specific_heats_r_derivative(t),
+                   g["dcp_r"]) < TOL
+    assert rel_err(o.get_species_enthalpies_rt_derivative(t),
+                   g["dh_rt"]) < TOL
+    assert rel_err(o.get_species_entropies_rt_derivative(t),
+                   g["ds_r"]) < TOL
+    y = g["Y"]
+    assert rel_err(o.get_mixture_molecular_weight(y), g["mmw"]) < TOL
+    assert rel_err(o.get_pressure(g["rho"], t, y), g["pressure"]) < TOL
+    for key, fn in (("cp_mass", o.get_mixture_specific_heat_cp_mass),
+                    ("cv_mass", o.get_mixture_specific_heat_cv_mass),
+                    ("h_mass", o.get_mixture_enthalpy_mass),
+                    ("e_mass", o.get_mixture_internal_energy_mass)):
+        assert rel_err(fn(t, y), g[key]) < TOL, key
+
+
+def test_equilibrium_constants(golden):
+    sol, g = golden
+    o = Oracle(sol)
+    lk = o.get_equilibrium_constants(g["T"])
+    # log Kc values pass through zero: compare absolutely at the scale of
+    # the Gibbs terms, and Kc itself relatively (test/test.py:157-171)
+    scale = np.abs(g["g_rt"]).max(axis=0)
+    assert np.all(np.abs(lk - g["log_k_eq"]) <= TOL * scale)
+    assert rel_err(np.exp(-lk), np.exp(-g["log_k_eq"])) < 1e-12
+
+
+def test_rate_coefficients_and_rates(golden):
+    sol, g = golden
+    o = Oracle(sol)
+    t, c, rho, y = g["T"], g["conc"], g["rho"], g["Y"]
+    assert rel_err(o.get_fwd_rate_coefficients(t, c), g["k_fwd"]) < TOL
+    assert rel_err(o.get_fwd_rates_of_progress(t, c), g["r_fwd"]) < TOL
+    assert rel_err(o.get_rev_rates_of_progress(t, c), g["r_rev"]) < TOL
+    s_r = np.abs(g["r_fwd"]) + np.abs(g["r_rev"])
+    assert rel_err(o.get_net_rates_of_progress(t, c), g["r_net"], s_r) < TOL
+    s = g["cdot"] + g["ddot"]
+    assert rel_err(o.get_net_production_rates(rho, t, y), g["wdot"], s) < TOL
+    cd, dd = o.get_creation_destruction_rates(rho, t, y)
+    assert rel_err(cd, g["cdot"]) < TOL
+    assert rel_err(dd, g["ddot"]) < TOL
+
+
+def test_temperature(golden):
+    sol, g = golden
+    o = Oracle(sol)
+    y = g["Y"]
+    te = o.get_temperature(g["e_mass"], 1500.0, y, do_energy=True)
+    th = o.get_temperature(g["h_mass"], 1500.0, y, do_energy=False)
+    assert np.abs(te - g["T_from_e"]).max() < 1e-10
+    assert np.abs(th - g["T_from_h"]).max() < 1e-10
+    # and both recover the state temperature (test/test.py:174-209)
+    assert np.abs(te - g["T"]).max() < 1e-10
+
+
+def test_reactor_source(golden):
+    sol, g = golden
+    o = Oracle(sol)
+    n = g["jac"].shape[0]
+    src = o.reactor_source(g["P"][:n], g["T"][:n], g["Y"][:, :n])
+    ref = g["reactor_source"]
+    assert np.abs(src - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_identities(golden):
+    sol, g = golden
+    o = Oracle(sol)
+    rho, t, y = g["rho"], g["T"], g["Y"]
+    w = o.get_net_production_rates(rho, t, y)
+    cd, dd = o.get_creation_destruction_rates(rho, t, y)
+    scale = (cd + dd).max(axis=0)
+    # net == creation - destruction (test/test.py:276)
+    assert np.all(np.abs(w - (cd - dd)).max(axis=0) <= 1e-13 * scale)
+    # element conservation: sum_k W_k w_k == 0 for balanced mechanisms
+    mass = (o.molecular_weights[:, None] * w).sum(axis=0)
+    mscale = (o.molecular_weights[:, None] * (cd + dd)).sum(axis=0)
+    assert np.all(np.abs(mass) <= 1e-13 * mscale)
+
+
+def test_newton_raises_like_reference():
+    sol, g = load_golden("synthetic9")
+    o = Oracle(sol)
+    with pytest.raises(RuntimeError,
+                       match="Temperature iteration failed to converge"):
+        o.get_temperature(np.array([np.nan]), 1500.0, g["Y"][:, :1], True)
