@@ -1,0 +1,411 @@
+#!/usr/bin/env python
+"""Benchmark of the per-state thermochemistry hot path on GB300.
+
+Workload (the configuration the headline metric is quoted on): a seeded
+synthetic 53-species / 325-reaction mechanism (30 three-body, 25 Troe,
+3 Lindemann), 4,194,304 states with T ~ U[300, 3000] K, p log-uniform in
+[1e4, 1e6] Pa, Y = 0.6 e_N2 + 0.4 Dirichlet(0.5).  One step = one pass over
+all states of density -> net production rates -> temperature Newton from
+the internal energy (T0 = 1500 K), FP64 -- the fused kernel behind
+``Thermochemistry.get_net_production_rates_and_temperature``.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Prints one JSON line (rank 0).  ``value``: states/s over all ranks with the
+inputs resident in HBM (the inputs, 1.9 GB, exceed the 129 MB L2, so no
+flush is needed between steps); ``e2e``: the same metric through the public
+API with pinned host inputs copied in and results copied out every step.
+``--impl reference`` times the CPU oracle port of the reference's generated
+numpy class on all host cores over a bounded sample.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+N_STATES = 4_194_304
+WORKLOAD = "synthetic53_325: density + net production rates + T(e) Newton"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--states", type=int, default=N_STATES)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0,
+                    help="target duration of the CPU baseline sample")
+    return ap.parse_args()
+
+
+# {{{ distributed plumbing
+
+def dist_info():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def init_dist(world):
+    if world <= 1:
+        return None
+    import torch.distributed as dist
+    os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+    dist.init_process_group("nccl")
+    return dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(dist, value, device):
+    if dist is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+# }}}
+
+
+# {{{ clocks
+
+class ClockSampler:
+    """Samples nvidia-smi during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,"
+              "clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index),
+                 f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, ValueError):
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [],
+                    "samples": 0}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.thread.join(timeout=5)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                smax.append(float(parts[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[3:7]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+# }}}
+
+
+# {{{ CPU baseline (oracle port of the reference's generated numpy class)
+
+def _oracle_chunk(args):
+    """Worker: one chunk of the workload through the CPU oracle; returns
+    seconds spent."""
+    n, seed = args
+    os.environ.setdefault("OMP_NUM_THREADS", "1")
+    import numpy as np  # noqa: F401
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    from pyrometheus_gb300 import synthetic
+    sol = synthetic.config2_mechanism()
+    orc = Oracle(sol)
+    t, p, y = synthetic.sample_states(sol, n, seed=seed)
+    e = orc.get_mixture_internal_energy_mass(t, y)
+    t0 = time.perf_counter()
+    rho = orc.get_density(p, t, y)
+    orc.get_net_production_rates(rho, t, y)
+    orc.get_temperature(e, 1500.0, y, do_energy=True)
+    return time.perf_counter() - t0
+
+
+def cpu_baseline(target_s: float, processes: int):
+    """States/s of the oracle port on *processes* host cores over a bounded
+    sample (chunks of 16,384 states, about *target_s* seconds of work)."""
+    chunk = 16384
+    one = _oracle_chunk((2048, 7))           # calibrate
+    per_state = one / 2048
+    total = max(chunk, int(target_s / per_state) // chunk * chunk)
+    jobs = [(chunk, 1000 + i) for i in range(total // chunk)]
+    if processes <= 1:
+        t0 = time.perf_counter()
+        for j in jobs:
+            _oracle_chunk(j)
+        dt = time.perf_counter() - t0
+    else:
+        import multiprocessing as mp
+        ctx = mp.get_context("spawn")
+        with ctx.Pool(processes) as pool:
+            pool.map(_oracle_chunk, [(256, 1)] * processes)   # warm
+            t0 = time.perf_counter()
+            pool.map(_oracle_chunk, jobs)
+            dt = time.perf_counter() - t0
+    states = len(jobs) * chunk
+    return {"value": states / dt, "unit": "states/s", "cores": processes,
+            "kind": "port",
+            "sample": f"{states} states of the workload in chunks of {chunk}"
+                      f" (oracle numpy restatement of the reference's "
+                      f"generated class, {processes} process(es))"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    cores = len(os.sched_getaffinity(0))
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
+    base = None
+    vals = []
+    for s in range(warmup + steps):
+        b = cpu_baseline(min(args.cpu_seconds, 8.0), cores)
+        if s >= warmup:
+            vals.append(b["value"])
+            base = b
+    v = statistics.median(vals)
+    base = dict(base, value=v)
+    out = {
+        "metric": "FP64 states/s (density + net production rates + "
+                  "temperature Newton)",
+        "value": v, "unit": "states/s", "n_gpus": 0, "steps": steps,
+        "warmup": warmup, "ms_per_step": None, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "states": args.states,
+                   "mechanism": "synthetic 53 species / 325 reactions"},
+        "impl": "reference",
+        "cpu_baseline": base,
+        "e2e": {"value": v, "unit": "states/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(out))
+
+# }}}
+
+
+def newton_iterations(sol, t, y, e, t0=1500.0, tol=1e-6):
+    """Mean per-state Newton iterations of the fused step on a sample
+    (the same update as the kernel)."""
+    import numpy as np
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    orc = Oracle(sol)
+    temp = np.full_like(t, t0)
+    done = np.zeros(t.shape, dtype=bool)
+    its = np.zeros(t.shape)
+    for _ in range(100):
+        cv = orc.get_mixture_specific_heat_cv_mass(temp, y)
+        ee = orc.get_mixture_internal_energy_mass(temp, y)
+        dt = (e - ee) / cv
+        temp = np.where(done, temp, temp + dt)
+        its += ~done
+        done |= np.abs(dt) < tol
+        if done.all():
+            break
+    return float(its.mean())
+
+
+def run_gb300(args):
+    import numpy as np
+    import torch
+
+    from pyrometheus_gb300 import get_thermochem_class, native, opcount
+    from pyrometheus_gb300 import synthetic
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    dist = init_dist(world)
+
+    sol = synthetic.config2_mechanism()
+    n = args.states
+    th = get_thermochem_class(sol)(device=dev)
+    t, p, y = synthetic.sample_states(sol, n, seed=2024 + rank)
+
+    # pinned host inputs (the e2e leg copies from these every step)
+    T_h = torch.from_numpy(t).pin_memory()
+    P_h = torch.from_numpy(p).pin_memory()
+    Y_h = torch.from_numpy(y).pin_memory()
+    T_d = T_h.to(dev)
+    P_d = P_h.to(dev)
+    Y_d = Y_h.to(dev)
+    E_d = th.get_mixture_internal_energy_mass(T_d, Y_d)
+    E_h = E_d.cpu().pin_memory()
+    torch.cuda.synchronize()
+
+    def step():
+        return th.get_net_production_rates_and_temperature(
+            P_d, T_d, Y_d, E_d, 1500.0, do_energy=True, check=False)
+
+    # warm-up (also checks convergence once)
+    for _ in range(max(args.warmup, 3)):
+        w, tn = step()
+    th.get_net_production_rates_and_temperature(P_d, T_d, Y_d, E_d, 1500.0)
+    torch.cuda.synchronize()
+
+    stream = torch.cuda.current_stream(dev)
+    clocks = ClockSampler(local)
+    barrier(dist)
+    torch.cuda.synchronize()
+    clocks.start()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        w, tn = step()
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier(dist)
+    clk = clocks.stop()
+    ms = ev0.elapsed_time(ev1)
+    ms = max_over_ranks(dist, ms, dev)
+    ms_per_step = ms / args.steps
+    value = n * world * args.steps / (ms * 1e-3)
+
+    # e2e: public API with pinned host buffers; copies in the timed region
+    W_h = torch.empty((sol.n_species, n), dtype=torch.float64).pin_memory()
+    To_h = torch.empty(n, dtype=torch.float64).pin_memory()
+    e2e_steps = max(1, min(args.steps, 5))
+
+    def e2e_step():
+        w_, t_ = th.get_net_production_rates_and_temperature(
+            P_h, T_h, Y_h, E_h, 1500.0, do_energy=True)
+        W_h.copy_(w_, non_blocking=True)
+        To_h.copy_(t_, non_blocking=True)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    barrier(dist)
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0, dev)
+    e2e_value = n * world * e2e_steps / e2e_s
+    h2d = (P_h.numel() + T_h.numel() + Y_h.numel() + E_h.numel()) * 8
+    d2h = (W_h.numel() + To_h.numel()) * 8
+
+    if rank != 0:
+        return
+
+    # roofline: FP64 pipe (the bound) and HBM (for context)
+    scratch = torch.empty(int(native.peaks_scratch_doubles()),
+                          dtype=torch.float64, device=dev)
+    dfma, exp_rate, log_rate = native.measure_fp64(scratch)
+    weights = opcount.libm_weights(dfma, exp_rate, log_rate)
+    idx = np.random.default_rng(0).choice(n, size=8192, replace=False)
+    iters = newton_iterations(sol, t[idx], y[:, idx],
+                              E_h.numpy()[idx])
+    counts = opcount.fused_step_counts(sol, iters)
+    flops_state = opcount.weighted_flops(counts, weights)
+    achieved = flops_state * n / (ms_per_step * 1e-3)
+    bps = opcount.bytes_per_state(sol)
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            hbm_peak = float(json.load(f)["hbm_gbs"])
+        hbm_src = "MEASURED_PEAKS.json"
+    except (OSError, KeyError, ValueError):
+        hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
+    hbm_achieved = bps * n / (ms_per_step * 1e-3) / 1e9
+
+    base = cpu_baseline(args.cpu_seconds, 1)
+    out = {
+        "metric": "FP64 states/s (density + net production rates + "
+                  "temperature Newton)",
+        "value": value, "unit": "states/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded states, seeded synthetic mechanism)",
+        "config": {"workload": WORKLOAD, "states_per_gpu": n,
+                   "mechanism": "synthetic 53 species / 325 reactions "
+                                "(30 three-body, 25 Troe, 3 Lindemann)",
+                   "l2": "inputs (1.9 GB) larger than L2; no flush",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": args.steps,
+        "e2e": {"value": e2e_value, "unit": "states/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "steps": e2e_steps},
+        "roofline": {
+            "bound": "fp64", "achieved": achieved / 1e12,
+            "peak": dfma / 1e12, "unit": "TFLOP/s",
+            "frac": achieved / dfma, "traffic": None,
+            "peak_source": "DFMA throughput measured live by bench.py "
+                           "(MEASURED_PEAKS.json has no FP64 figure)",
+            "flops_per_state": flops_state,
+            "flop_model": {"arith_flops": counts["flops"],
+                           "transcendentals": {k: counts[k] for k in
+                                               opcount.TRANSCENDENTALS},
+                           "flops_per_transcendental": weights,
+                           "newton_iterations": iters},
+        },
+        "hbm": {"bytes_per_state": bps, "achieved_gbs": hbm_achieved,
+                "peak_gbs": hbm_peak, "frac": hbm_achieved / hbm_peak,
+                "peak_source": hbm_src},
+        "cpu_baseline": base,
+        "clocks": clk,
+    }
+    print(json.dumps(out))
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gb300(args)
+
+
+if __name__ == "__main__":
+    main()
+
+# vim: foldmethod=marker

@@ -1,0 +1,136 @@
+/*
+ * pyrometheus_gb300 C ABI.
+ *
+ * A mechanism library (libpyro_<mechanism>_<hash>.so) is generated by the
+ * `cuda` code-generation target and exports the entry points below, one
+ * per method of the reference's generated Thermochemistry class
+ * (pyrometheus/codegen/python.py).  Every entry point:
+ *
+ *   - takes caller-owned device pointers, sizes and strides in elements,
+ *     and a cudaStream_t; it is asynchronous on that stream;
+ *   - allocates nothing;
+ *   - returns a PyroStatus (0 ok, 1 bad argument, 2 launch failure,
+ *     3 non-convergence, 4 unsupported option).
+ *
+ * Layouts (FP64): per-species and per-reaction arrays are species-major,
+ * x[k * ld + i] for state i (ld >= n).  A per-state scalar argument is a
+ * pointer plus an increment: inc = 1 for an array of n values, inc = 0 to
+ * broadcast one device value to every state (the reference's scalar
+ * arguments).
+ */
+#ifndef PYROMETHEUS_GB300_H
+#define PYROMETHEUS_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* cudaStream_t;
+
+enum PyroStatus {
+  PYRO_OK = 0,
+  PYRO_ERR_ARGUMENT = 1,
+  PYRO_ERR_LAUNCH = 2,
+  PYRO_ERR_NOT_CONVERGED = 3,
+  PYRO_ERR_UNSUPPORTED = 4
+};
+
+/* ---- mechanism library (generated per mechanism) ------------------------ */
+
+/* Sizes of the compiled mechanism (num_species, num_reactions, num_falloff:
+ * python.py:180-185), the kernels' block size and table footprint. */
+int pyro_mechanism_info(int* n_species, int* n_reactions, int* n_falloff,
+                        int* block_size, int* table_bytes);
+
+/* Species NASA-7 properties at T, out[S][ldo]; which:
+ *   0 cp/R          get_species_specific_heats_r            python.py:334
+ *   1 h/RT          get_species_enthalpies_rt               python.py:341
+ *   2 s/R           get_species_entropies_r                 python.py:348
+ *   3 g/RT          get_species_gibbs_rt                    python.py:355
+ *   4 d(cp/R)/dT    get_species_specific_heats_r_derivative python.py:313
+ *   5 d(h/RT)/dT    get_species_enthalpies_rt_derivative    python.py:320
+ *   6 d(s/R)/dT     get_species_entropies_rt_derivative     python.py:327 */
+int pyro_species_property(int which, const double* T, int64_t t_inc,
+                          double* out, int64_t ldo, int64_t n,
+                          cudaStream_t stream);
+
+/* Mixture properties, out[n]; which:
+ *   0 mixture molecular weight   get_mixture_molecular_weight  python.py:265
+ *   1 specific gas constant      get_specific_gas_constant     python.py:248
+ *   2 cp (mass)                  get_mixture_specific_heat_cp_mass :293
+ *   3 cv (mass)                  get_mixture_specific_heat_cv_mass :298
+ *   4 h (mass)                   get_mixture_enthalpy_mass         :303
+ *   5 e (mass)                   get_mixture_internal_energy_mass  :308
+ *   6 density, aux = pressure    get_density                   python.py:255
+ *   7 pressure, aux = density    get_pressure                  python.py:260
+ * T may be NULL for which 0-1, aux must be given for which 6-7. */
+int pyro_mixture_property(int which, const double* T, int64_t t_inc,
+                          const double* Y, int64_t ldy, const double* aux,
+                          int64_t aux_inc, double* out, int64_t n,
+                          cudaStream_t stream);
+
+/* out[S][ldo]; which 0: concentrations, aux = rho
+ * (get_concentrations, python.py:272); which 1: mole fractions, aux =
+ * mixture molecular weight (get_mole_fractions, python.py:279). */
+int pyro_species_scale(int which, const double* aux, int64_t aux_inc,
+                       const double* Y, int64_t ldy, double* out, int64_t ldo,
+                       int64_t n, cudaStream_t stream);
+
+/* Per-reaction quantities from T and concentrations, out[R][ldo]; mode:
+ *   0 log equilibrium constants  get_equilibrium_constants  python.py:360
+ *     (conc may be NULL)
+ *   1 forward rate coefficients  get_fwd_rate_coefficients  python.py:453
+ *     (falloff slots as get_falloff_rates writes them, python.py:399)
+ *   2 net rates of progress      get_net_rates_of_progress  python.py:475
+ *   3 forward rates of progress  get_fwd_rates_of_progress  python.py:497
+ *   4 reverse rates of progress  get_rev_rates_of_progress  python.py:506 */
+int pyro_reaction_quantity(int mode, const double* T, int64_t t_inc,
+                           const double* conc, int64_t ldc, double* out,
+                           int64_t ldo, int64_t n, cudaStream_t stream);
+
+/* Net molar production rates wdot[S][ldw] from (rho, T, Y):
+ * get_net_production_rates, python.py:486.  The hot path. */
+int pyro_net_production_rates(const double* rho, int64_t rho_inc,
+                              const double* T, int64_t t_inc,
+                              const double* Y, int64_t ldy, double* wdot,
+                              int64_t ldw, int64_t n, cudaStream_t stream);
+
+/* Creation and destruction rates (either output may be NULL):
+ * get_creation_destruction_rates, python.py:543 (and get_creation_rates
+ * :517, get_destruction_rates :530). */
+int pyro_creation_destruction_rates(const double* rho, int64_t rho_inc,
+                                    const double* T, int64_t t_inc,
+                                    const double* Y, int64_t ldy,
+                                    double* cdot, double* ddot, int64_t ldo,
+                                    int64_t n, cudaStream_t stream);
+
+/* Temperature from mass-specific internal energy (do_energy != 0) or
+ * enthalpy: get_temperature, python.py:375 (tol 1e-6, max_iter 500 there).
+ * Per-state Newton; states that do not reach |dT| < tol within max_iter are
+ * counted into *fail_count (device int, may be NULL; the caller zeroes it).
+ * The caller raises the reference's RuntimeError when it is non-zero. */
+int pyro_temperature(const double* target, int64_t target_inc,
+                     const double* t0, int64_t t0_inc, const double* Y,
+                     int64_t ldy, int do_energy, double tol, int max_iter,
+                     double* T_out, int* fail_count, int64_t n,
+                     cudaStream_t stream);
+
+/* One pass per state of get_density(p, T, Y) -> get_net_production_rates
+ * -> get_temperature(target, t0, Y, do_energy): the chain of the 0-D
+ * reactor right-hand side (examples/free_flame/reactors.py:115-123) and the
+ * flamelet source terms (flamelets/equations.py:313-359). */
+int pyro_fused_step(const double* p, int64_t p_inc, const double* T,
+                    int64_t t_inc, const double* Y, int64_t ldy,
+                    const double* target, int64_t target_inc,
+                    const double* t0, int64_t t0_inc, int do_energy,
+                    double tol, int max_iter, double* wdot, int64_t ldw,
+                    double* T_out, int* fail_count, int64_t n,
+                    cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* PYROMETHEUS_GB300_H */

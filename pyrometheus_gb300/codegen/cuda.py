@@ -1,0 +1,535 @@
+"""``-l cuda``: the GB300 (sm_103a) code-generation target.
+
+``CudaCodeGenerator.generate(name, sol)`` emits one self-contained CUDA
+translation unit for a mechanism.  It plays the role the Mako template of
+``pyrometheus/codegen/python.py:106-642`` plays for numpy: the same
+per-species/per-reaction formulas (``pyrometheus/chem_expr.py``), written as
+FP64 device code with one thread per thermochemical state.
+
+Design (GB300-first):
+
+* the mechanism is baked into straight-line code: NASA-7 coefficients,
+  Arrhenius parameters, efficiencies and stoichiometry are compile-time
+  constants that the compiler places in the constant bank (operands of the
+  FP64 instructions), so no table is fetched per state;
+* states are independent: a grid-stride loop assigns one state per thread;
+  inputs/outputs are species-major ``[S, N]`` arrays (unit stride along the
+  state axis), so a warp's loads and stores are 256-byte coalesced rows;
+* per-state working sets (concentrations, Gibbs energies) stay in registers
+  for small mechanisms and move to a per-thread slice of shared memory for
+  large ones; production-rate accumulators stay in registers;
+* the work is FP64-pipe bound (GB300 FP64 is ~1.2 TFLOP/s against
+  ~7 TB/s of HBM), so the generated code minimises FP64 instructions:
+  ``k_r = exp(ln k_f + ln K)`` reuses the forward exponent, third-body sums
+  use the total concentration plus per-species corrections, the temperature
+  Newton folds the mass-weighted NASA polynomials into one mixture
+  polynomial per range before iterating, and NASA ranges are chosen with
+  selects instead of divergent branches.
+
+The emitted C-ABI (``extern "C"``, plain pointers, sizes, strides and a
+``cudaStream_t``) is declared in ``include/pyrometheus_gb300.h``.
+"""
+
+from __future__ import annotations
+
+import hashlib
+import math
+import os
+import subprocess
+import sys
+import threading
+from dataclasses import dataclass
+from typing import Dict, List, Optional, Tuple
+
+import numpy as np
+
+from . import CodeGenerationOptions, CodeGenerator
+
+file_extension = "cu"
+
+GAS_CONSTANT = 8314.46261815324
+ONE_ATM = 101325.0
+IRREVERSIBLE_LOG_KEQ_SLOPE = -0.17364695002734
+
+CSRC = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(
+    __file__))), "csrc")
+
+
+@dataclass(frozen=True)
+class CudaGenerationOptions(CodeGenerationOptions):
+    """Options of the ``cuda`` target.
+
+    ``block_size``: threads per block of the per-state kernels (``None``:
+    as many as let two blocks' per-thread shared-memory columns fit on an
+    SM, at most 128);
+    ``blocks_per_sm``: grid cap, in blocks per SM, of the grid-stride loops.
+    """
+
+    block_size: Optional[int] = None
+    blocks_per_sm: int = 8
+
+
+# {{{ mechanism model
+
+def _hexd(x: float) -> str:
+    """Exact C literal for a double."""
+    x = float(x)
+    if math.isinf(x):
+        return "(1.0/0.0)" if x > 0 else "(-1.0/0.0)"
+    if x == 0.0:
+        return "0.0" if math.copysign(1.0, x) > 0 else "-0.0"
+    return float.hex(x)
+
+
+class _Rate:
+    """Arrhenius parameters in the generated form (``chem_expr.py:310-324``)."""
+
+    def __init__(self, rate):
+        self.A = float(rate.pre_exponential_factor)
+        self.b = float(rate.temperature_exponent)
+        self.Ta = float(rate.activation_energy) / GAS_CONSTANT
+        self.lnA = float(np.log(np.float64(self.A))) if self.A > 0 else None
+
+    def exp_arg(self) -> Optional[str]:
+        """C expression x with k = exp(x), or None if k has a direct form."""
+        if self.Ta == 0.0:
+            if self.b == 0.0 or (self.b.is_integer() and abs(self.b) <= 3):
+                return None
+            return f"({_hexd(self.lnA)} + {_hexd(self.b)}*lnT)"
+        if self.lnA is None:
+            return None
+        if self.b == 0.0:
+            return f"({_hexd(self.lnA)} - {_hexd(self.Ta)}*invT)"
+        return (f"({_hexd(self.lnA)} + {_hexd(self.b)}*lnT"
+                f" - {_hexd(self.Ta)}*invT)")
+
+    def direct(self) -> str:
+        """C expression of k for the forms without an exponential."""
+        if self.Ta == 0.0 and self.b == 0.0:
+            return _hexd(self.A)
+        if self.Ta == 0.0 and self.b.is_integer() and abs(self.b) <= 3:
+            base = "T" if self.b > 0 else "invT"
+            return "*".join([_hexd(self.A)] + [base] * int(abs(self.b)))
+        if self.lnA is None:
+            return "0.0"
+        raise AssertionError("rate has an exponential form")
+
+    def expr(self) -> str:
+        x = self.exp_arg()
+        return f"exp{x}" if x is not None else self.direct()
+
+
+class _Reaction:
+    def __init__(self, j, r, sol, index):
+        self.j = j
+        self.equation = r.equation
+        self.reversible = bool(r.reversible)
+        rt = r.reaction_type
+        if rt.startswith("falloff"):
+            self.kind = "falloff"
+            self.ftype = rt.split("-")[1]
+            self.low = _Rate(r.rate.low_rate)
+            self.high = _Rate(r.rate.high_rate)
+            self.fc = [float(v) for v in r.rate.falloff_coeffs]
+            if self.ftype not in ("Troe", "Lindemann"):
+                raise NotImplementedError(f"falloff type {self.ftype}")
+        elif rt == "three-body-Arrhenius":
+            self.kind = "three-body"
+            self.rate = _Rate(r.rate)
+        elif rt in ("Arrhenius", "elementary", "reaction"):
+            self.kind = "elementary"
+            self.rate = _Rate(r.rate)
+        else:
+            raise NotImplementedError(f"reaction type '{rt}' ({r.equation})")
+        # forward exponents pair reactants with the ``orders`` values
+        # positionally, as chem_expr.py:436-446 zips them
+        exps = list(r.orders.values()) if r.orders else \
+            list(r.reactants.values())
+        self.fwd = [(index(sp), float(nu)) for sp, nu in
+                    zip(r.reactants, exps)]
+        self.rev = [(index(sp), float(nu)) for sp, nu in r.products.items()]
+        self.nu_r: Dict[int, float] = {}
+        self.nu_p: Dict[int, float] = {}
+        for sp in r.reactants:
+            self.nu_r[index(sp)] = float(
+                sol.reactant_stoich_coeff(index(sp), j))
+        for sp in r.products:
+            self.nu_p[index(sp)] = float(
+                sol.product_stoich_coeff(index(sp), j))
+        self.dnu = sum(self.nu_p.values()) - sum(self.nu_r.values())
+        self.eff: Dict[int, float] = {}
+        self.default_eff = 1.0
+        if self.kind != "elementary":
+            tb = r.third_body
+            self.default_eff = float(tb.default_efficiency)
+            for sp, e in tb.efficiencies.items():
+                if sp in sol.species_names:
+                    self.eff[index(sp)] = float(e)
+
+
+class _Model:
+    def __init__(self, sol):
+        self.S = int(sol.n_species)
+        self.R = int(sol.n_reactions)
+        self.names = list(sol.species_names)
+        self.W = [float(w) for w in sol.molecular_weights]
+        self.invW = [float(v) for v in 1.0 / np.asarray(
+            sol.molecular_weights, dtype=np.float64)]
+        self.tmid, self.hi, self.lo = [], [], []
+        for sp in sol.species():
+            c = [float(v) for v in sp.thermo.coeffs]
+            self.tmid.append(c[0])
+            self.hi.append(c[1:8])
+            self.lo.append(c[8:15])
+        index = sol.species_index
+        self.rx = [_Reaction(j, r, sol, index)
+                   for j, r in enumerate(sol.reactions())]
+        groups: Dict[float, List[int]] = {}
+        for k, t in enumerate(self.tmid):
+            groups.setdefault(t, []).append(k)
+        self.tmid_groups = list(groups.items())
+        self.n_falloff = sum(1 for r in self.rx if r.kind == "falloff")
+
+# }}}
+
+
+# {{{ emitter
+
+def _cint(x) -> str:
+    return str(int(x))
+
+
+def _table(qual: str, ctype: str, name: str, dims: List[int],
+           values: List[str]) -> str:
+    shape = "".join(f"[{d}]" for d in dims)
+    return f"{qual} {ctype} {name}{shape} = {{{', '.join(values)}}};"
+
+
+def _rate_record(rate: _Rate) -> Tuple[int, List[float]]:
+    """(form, [p0, p1, p2]) of an Arrhenius record (kinetics.cuh FORM_*)."""
+    if rate.Ta == 0.0 and rate.b == 0.0:
+        return 1, [rate.A, 0.0, 0.0]
+    if rate.Ta == 0.0 and rate.b.is_integer() and abs(rate.b) <= 3:
+        return 2, [rate.A, rate.b, 0.0]
+    ln_a = float(np.log(np.float64(rate.A))) if rate.A > 0 else (
+        -math.inf if rate.A == 0 else math.nan)
+    return 0, [ln_a, rate.b, rate.Ta]
+
+
+def _dlit(x: float) -> str:
+    x = float(x)
+    if math.isnan(x):
+        return "(double)NAN"
+    if math.isinf(x):
+        return "(double)INFINITY" if x > 0 else "-(double)INFINITY"
+    return _hexd(x)
+
+
+class _Emitter:
+    """Emits the mechanism tables; the kernels are the mechanism-independent
+    ``csrc/kinetics.cuh``."""
+
+    CONST_LIMIT = 60 * 1024
+
+    def __init__(self, name: str, sol, opts: CudaGenerationOptions):
+        self.name = name
+        self.m = _Model(sol)
+        self.opts = opts
+        self.block = int(opts.block_size) if opts.block_size else \
+            _default_block(self.m.S)
+
+    def render(self) -> str:
+        m = self.m
+        S, R = m.S, m.R
+        maxside = max([1] + [max(len(r.fwd), len(r.rev)) for r in m.rx])
+        falloff = [r for r in m.rx if r.kind == "falloff"]
+        nf = len(falloff)
+
+        flags, rates, nr_l, np_l, sp_l, nu_l, ord_l = [], [], [], [], [], [], []
+        dnu, defeff, tb_start, tb_idx, tb_de = [], [], [0], [], []
+        fo_slot, fo_form, fo_low, fo_troe = [], [], [], []
+        frac_row, frac = [], []
+        for r in m.rx:
+            f = 0
+            if r.kind == "three-body":
+                f |= 1
+            elif r.kind == "falloff":
+                f |= 2
+            if r.reversible:
+                f |= 4
+            rate = r.high if r.kind == "falloff" else r.rate
+            form, rec = _rate_record(rate)
+            f |= form << 3
+            rates.append(rec)
+            if r.kind == "falloff":
+                fo_slot.append(len(fo_low))
+                lform, lrec = _rate_record(r.low)
+                fo_form.append(lform)
+                fo_low.append(lrec)
+                if r.ftype == "Troe":
+                    f |= 32
+                    a, t3, t1 = r.fc[0], r.fc[1], r.fc[2]
+                    t2 = r.fc[3] if len(r.fc) == 4 else 0.0
+                    if len(r.fc) == 4:
+                        f |= 64
+                    fo_troe.append([1.0 - a, -1.0 / t3, a, -1.0 / t1, -t2])
+                else:
+                    fo_troe.append([0.0] * 5)
+            else:
+                fo_slot.append(-1)
+            r_sp = [k for k, _ in r.fwd]
+            r_ord = [e for _, e in r.fwd]
+            r_nu = [r.nu_r.get(k, 0.0) for k in r_sp]
+            p_sp = [k for k, _ in r.rev]
+            p_nu = [nu for _, nu in r.rev]
+            ints = all(float(v).is_integer() and abs(v) <= 127
+                       for v in r_nu + p_nu + r_ord)
+            if not ints:
+                f |= 128
+                frac_row.append(len(frac))
+                row = ([float(v) for v in r_nu] + [0.0] * (maxside - len(r_nu))
+                       + [float(v) for v in p_nu]
+                       + [0.0] * (maxside - len(p_nu))
+                       + [float(v) for v in r_ord]
+                       + [0.0] * (maxside - len(r_ord)))
+                frac.append(row)
+            else:
+                frac_row.append(0)
+            flags.append(f)
+            nr_l.append(len(r_sp))
+            np_l.append(len(p_sp))
+            sp_l.append(r_sp + [0] * (maxside - len(r_sp)) + p_sp
+                        + [0] * (maxside - len(p_sp)))
+            nu_l.append([int(v) if float(v).is_integer() and abs(v) <= 127
+                         else 0 for v in r_nu]
+                        + [0] * (maxside - len(r_nu))
+                        + [int(v) if float(v).is_integer() and abs(v) <= 127
+                           else 0 for v in p_nu]
+                        + [0] * (maxside - len(p_nu)))
+            ord_l.append([int(v) if float(v).is_integer() and abs(v) <= 127
+                          else 0 for v in r_ord]
+                         + [0] * (maxside - len(r_ord)))
+            dnu.append(r.dnu)
+            d = r.default_eff if r.kind != "elementary" else 1.0
+            defeff.append(d)
+            if r.kind != "elementary":
+                for k, e in sorted(r.eff.items()):
+                    if e != d:
+                        tb_idx.append(k)
+                        tb_de.append(e - d)
+            tb_start.append(len(tb_idx))
+
+        groups = m.tmid_groups
+        grp_start, grp_sp, grp_tmid = [0], [], []
+        for tmid, ks in groups:
+            grp_sp.extend(ks)
+            grp_start.append(len(grp_sp))
+            grp_tmid.append(tmid)
+
+        # table footprint decides constant vs global placement
+        nbytes = (8 * S * 17 + 4 * (len(groups) + 1) + 2 * S
+                  + 8 * len(groups) + R * (4 + 24 + 2 + 2 * 2 * maxside
+                                           + 3 * maxside + 16 + 4 + 4 + 4)
+                  + 4 * (R + 1) + max(1, len(tb_idx)) * 10
+                  + max(1, nf) * (4 + 24 + 40)
+                  + max(1, len(frac)) * 24 * maxside)
+        qual = "__constant__" if nbytes <= self.CONST_LIMIT else "__device__"
+
+        L: List[str] = []
+        w = L.append
+        w(f"// Generated by pyrometheus_gb300 (-l cuda) for mechanism "
+          f"'{self.name}':")
+        w(f"// {S} species, {R} reactions ({nf} falloff); FP64, sm_103a.")
+        w("// Tables only: the kernels are csrc/kinetics.cuh, the C ABI "
+          "csrc/kinetics_abi.cuh.")
+        w("#include <cmath>")
+        w('#include "pyro_common.cuh"')
+        w("")
+        w(f"#define NS {S}")
+        w(f"#define NR {R}")
+        w(f"#define NF {max(1, nf)}")
+        w(f"#define NF_REAL {nf}")
+        w(f"#define NTB {max(1, len(tb_idx))}")
+        w(f"#define NFRAC {max(1, len(frac))}")
+        w(f"#define NG {len(groups)}")
+        w(f"#define MAXSIDE {maxside}")
+        w(f"#define BLOCK {self.block}")
+        w(f"#define BLOCKS_PER_SM {int(self.opts.blocks_per_sm)}")
+        w(f"#define TABLE_BYTES {nbytes}")
+        w(f"#define LOG_P0_OVER_R {_hexd(math.log(ONE_ATM / GAS_CONSTANT))}")
+        w("")
+        w("// species: molecular weights, NASA-7 ranges [Tmid, hi(7), lo(7)]")
+        w(_table(qual, "double", "k_mw", [S], [_hexd(v) for v in m.W]))
+        w(_table(qual, "double", "k_inv_mw", [S], [_hexd(v) for v in m.invW]))
+        w(_table(qual, "double", "k_tmid", [S], [_hexd(v) for v in m.tmid]))
+        w(_table(qual, "double", "k_nasa_hi", [S, 7],
+                 ["{" + ", ".join(_hexd(v) for v in row) + "}"
+                  for row in m.hi]))
+        w(_table(qual, "double", "k_nasa_lo", [S, 7],
+                 ["{" + ", ".join(_hexd(v) for v in row) + "}"
+                  for row in m.lo]))
+        w(_table(qual, "int", "k_grp_start", [len(groups) + 1],
+                 [_cint(v) for v in grp_start]))
+        w(_table(qual, "short", "k_grp_sp", [S], [_cint(v) for v in grp_sp]))
+        w(_table(qual, "double", "k_grp_tmid", [len(groups)],
+                 [_hexd(v) for v in grp_tmid]))
+        w("")
+        w("// reactions (flags: kind | reversible | Arrhenius form | Troe...)")
+        w(_table(qual, "int", "k_rx_flags", [R], [_cint(v) for v in flags]))
+        w(_table(qual, "double", "k_rx_rate", [R, 3],
+                 ["{" + ", ".join(_dlit(v) for v in rec) + "}"
+                  for rec in rates]))
+        w(_table(qual, "signed char", "k_rx_nr", [R], [_cint(v) for v in nr_l]))
+        w(_table(qual, "signed char", "k_rx_np", [R], [_cint(v) for v in np_l]))
+        w(_table(qual, "short", "k_rx_sp", [R, 2 * maxside],
+                 ["{" + ", ".join(_cint(v) for v in row) + "}"
+                  for row in sp_l]))
+        w(_table(qual, "signed char", "k_rx_nu", [R, 2 * maxside],
+                 ["{" + ", ".join(_cint(v) for v in row) + "}"
+                  for row in nu_l]))
+        w(_table(qual, "signed char", "k_rx_ord", [R, maxside],
+                 ["{" + ", ".join(_cint(v) for v in row) + "}"
+                  for row in ord_l]))
+        w(_table(qual, "double", "k_rx_dnu", [R], [_hexd(v) for v in dnu]))
+        w(_table(qual, "double", "k_rx_defeff", [R],
+                 [_hexd(v) for v in defeff]))
+        w(_table(qual, "int", "k_rx_tb", [R + 1],
+                 [_cint(v) for v in tb_start]))
+        w(_table(qual, "short", "k_tb_idx", [max(1, len(tb_idx))],
+                 [_cint(v) for v in (tb_idx or [0])]))
+        w(_table(qual, "double", "k_tb_de", [max(1, len(tb_de))],
+                 [_hexd(v) for v in (tb_de or [0.0])]))
+        w(_table(qual, "int", "k_rx_fo", [R], [_cint(v) for v in fo_slot]))
+        w(_table(qual, "int", "k_fo_lowform", [max(1, nf)],
+                 [_cint(v) for v in (fo_form or [0])]))
+        w(_table(qual, "double", "k_fo_low", [max(1, nf), 3],
+                 ["{" + ", ".join(_dlit(v) for v in rec) + "}"
+                  for rec in (fo_low or [[0.0, 0.0, 0.0]])]))
+        w(_table(qual, "double", "k_fo_troe", [max(1, nf), 5],
+                 ["{" + ", ".join(_dlit(v) for v in rec) + "}"
+                  for rec in (fo_troe or [[0.0] * 5])]))
+        w(_table(qual, "int", "k_rx_frac", [R], [_cint(v) for v in frac_row]))
+        w(_table(qual, "double", "k_frac", [max(1, len(frac)), 3 * maxside],
+                 ["{" + ", ".join(_dlit(v) for v in row) + "}"
+                  for row in (frac or [[0.0] * (3 * maxside)])]))
+        w("")
+        w('#include "kinetics.cuh"')
+        w('#include "kinetics_abi.cuh"')
+        return "\n".join(L) + "\n"
+
+
+def _default_block(n_species: int) -> int:
+    """Threads per block so that three per-thread columns of NS doubles fit
+    in about 100 KB of shared memory (two resident blocks per SM)."""
+    per_thread = 3 * n_species * 8
+    b = (100 * 1024 // max(per_thread, 1)) // 32 * 32
+    return int(max(32, min(128, b)))
+
+# }}}
+
+
+class CudaCodeGenerator(CodeGenerator):
+    """The ``cuda`` target of the code-generator registry."""
+
+    @staticmethod
+    def get_name() -> str:
+        return "cuda"
+
+    @staticmethod
+    def supports_overloading() -> bool:
+        return True
+
+    @staticmethod
+    def generate(name: str, sol, opts: CodeGenerationOptions = None) -> str:
+        if opts is None:
+            opts = CudaGenerationOptions()
+        if opts.directive_offload is not None:
+            raise TypeError(
+                "OpenMP/ACC directive based offloading is not supported for "
+                "CUDA code generation")
+        if opts.scalar_type not in (None, "double"):
+            raise TypeError("the CUDA target computes in double precision "
+                            f"only (got scalar_type={opts.scalar_type!r})")
+        if not isinstance(opts, CudaGenerationOptions):
+            opts = CudaGenerationOptions(scalar_type=opts.scalar_type)
+        return _Emitter(name, sol, opts).render()
+
+    @staticmethod
+    def build_module(source: str, name: str = "mechanism",
+                     build_dir: Optional[str] = None) -> str:
+        """Compile generated source to a shared library (cached by content
+        hash); returns its path."""
+        return build_shared_library(source, name, build_dir)
+
+    @staticmethod
+    def get_thermochem_class(sol, opts: Optional[CodeGenerationOptions] = None,
+                             name: str = "Thermochemistry"):
+        """For the mechanism *sol*, return the drop-in CUDA
+        ``Thermochemistry`` class (``python.py:699-707`` counterpart)."""
+        from ..thermochemistry import make_thermochem_class
+        src = CudaCodeGenerator.generate(name, sol, opts)
+        lib = build_shared_library(
+            src, f"{sol.n_species}sp{sol.n_reactions}rx")
+        return make_thermochem_class(sol, lib, name)
+
+
+# {{{ build
+
+NVCC_ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+
+
+def default_build_dir() -> str:
+    return os.environ.get("PYRO_GB300_BUILD_DIR", os.path.join(
+        os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+        "_build"))
+
+
+def nvcc_path() -> str:
+    cand = os.environ.get("NVCC")
+    if cand:
+        return cand
+    for p in ("/usr/local/cuda/bin/nvcc",):
+        if os.path.exists(p):
+            return p
+    return "nvcc"
+
+
+def build_shared_library(source: str, name: str = "mechanism",
+                         build_dir: Optional[str] = None,
+                         extra_flags: Tuple[str, ...] = ()) -> str:
+    build_dir = build_dir or default_build_dir()
+    os.makedirs(build_dir, exist_ok=True)
+    flags = NVCC_ARCH + ["-O3", "-lineinfo", "-std=c++17", "-shared",
+                         "-Xcompiler", "-fPIC", "-Xcompiler",
+                         "-fvisibility=hidden", f"-I{CSRC}"] + list(
+        extra_flags)
+    deps = b""
+    for fn in sorted(os.listdir(CSRC)):
+        if fn.endswith((".cuh", ".h")):
+            with open(os.path.join(CSRC, fn), "rb") as f:
+                deps += f.read()
+    h = hashlib.sha256(source.encode() + deps + " ".join(flags).encode()
+                       ).hexdigest()[:16]
+    stem = "".join(ch if ch.isalnum() else "_" for ch in str(name))[:40]
+    lib = os.path.join(build_dir, f"libpyro_{stem}_{h}.so")
+    if os.path.exists(lib):
+        return lib
+    # content-addressed output written under a unique name and renamed into
+    # place, so concurrent builders (threads or processes) never collide
+    tag = f"{os.getpid()}_{threading.get_ident()}"
+    cu = lib[:-3] + f".{tag}.cu"
+    with open(cu, "w") as f:
+        f.write(source)
+    tmp = lib + f".{tag}.tmp"
+    cmd = [nvcc_path()] + flags + ["-o", tmp, cu]
+    proc = subprocess.run(cmd, capture_output=True, text=True)
+    if proc.returncode != 0:
+        raise RuntimeError("nvcc failed:\n" + " ".join(cmd) + "\n"
+                           + proc.stdout + proc.stderr)
+    os.replace(cu, lib[:-3] + ".cu")
+    os.replace(tmp, lib)
+    return lib
+
+# }}}
+
+# vim: foldmethod=marker

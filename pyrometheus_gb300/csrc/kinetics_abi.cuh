@@ -1,0 +1,174 @@
+// C ABI of a generated mechanism library (declared in
+// include/pyrometheus_gb300.h).  Included by the generated translation unit
+// after kinetics.cuh.  Every entry point is asynchronous on `stream`,
+// allocates nothing, and returns a PyroStatus.
+#pragma once
+
+#include "kinetics.cuh"
+
+namespace {
+
+int grid_for(int64_t n) {
+  return pyro_grid(n, BLOCK, pyro_sm_count() * BLOCKS_PER_SM);
+}
+
+constexpr size_t smem_cols(int q) { return (size_t)q * NS * BLOCK * 8; }
+
+// Opt a kernel into more than 48 KB of dynamic shared memory when needed.
+int prepare_smem(const void* fn, size_t bytes) {
+  if (bytes > 48 * 1024) {
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)bytes) != cudaSuccess) {
+      (void)cudaGetLastError();
+      return PYRO_ERR_LAUNCH;
+    }
+  }
+  return PYRO_OK;
+}
+
+}  // namespace
+
+PYRO_EXPORT int pyro_mechanism_info(int* n_species, int* n_reactions,
+                                    int* n_falloff, int* block_size,
+                                    int* table_bytes) {
+  if (n_species) *n_species = NS;
+  if (n_reactions) *n_reactions = NR;
+  if (n_falloff) *n_falloff = NF_REAL;
+  if (block_size) *block_size = BLOCK;
+  if (table_bytes) *table_bytes = TABLE_BYTES;
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_species_property(int which, const double* T,
+                                      int64_t t_inc, double* out, int64_t ldo,
+                                      int64_t n, cudaStream_t stream) {
+  if (n < 0 || which < 0 || which > 6) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!T || !out || ldo < n) return PYRO_ERR_ARGUMENT;
+  k_species_prop<<<grid_for(n), BLOCK, 0, stream>>>(which, T, t_inc, out,
+                                                    ldo, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_mixture_property(int which, const double* T,
+                                      int64_t t_inc, const double* Y,
+                                      int64_t ldy, const double* aux,
+                                      int64_t aux_inc, double* out, int64_t n,
+                                      cudaStream_t stream) {
+  if (n < 0 || which < 0 || which > 7) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!Y || !out || ldy < n) return PYRO_ERR_ARGUMENT;
+  if (which >= 2 && !T) return PYRO_ERR_ARGUMENT;
+  if (which >= 6 && !aux) return PYRO_ERR_ARGUMENT;
+  k_mixture_prop<<<grid_for(n), BLOCK, 0, stream>>>(which, T, t_inc, Y, ldy,
+                                                    aux, aux_inc, out, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_species_scale(int which, const double* aux,
+                                   int64_t aux_inc, const double* Y,
+                                   int64_t ldy, double* out, int64_t ldo,
+                                   int64_t n, cudaStream_t stream) {
+  if (n < 0 || which < 0 || which > 1) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!aux || !Y || !out || ldy < n || ldo < n) return PYRO_ERR_ARGUMENT;
+  k_species_scale<<<grid_for(n), BLOCK, 0, stream>>>(which, aux, aux_inc, Y,
+                                                     ldy, out, ldo, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_reaction_quantity(int mode, const double* T,
+                                       int64_t t_inc, const double* conc,
+                                       int64_t ldc, double* out, int64_t ldo,
+                                       int64_t n, cudaStream_t stream) {
+  if (n < 0 || mode < 0 || mode > 4) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!T || !out || ldo < n) return PYRO_ERR_ARGUMENT;
+  if (mode != 0 && (!conc || ldc < n)) return PYRO_ERR_ARGUMENT;
+  const size_t sm = smem_cols(2);
+  if (prepare_smem((const void*)k_reaction_quantity, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  k_reaction_quantity<<<grid_for(n), BLOCK, sm, stream>>>(mode, T, t_inc,
+                                                          conc, ldc, out, ldo,
+                                                          n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_net_production_rates(const double* rho, int64_t rho_inc,
+                                          const double* T, int64_t t_inc,
+                                          const double* Y, int64_t ldy,
+                                          double* wdot, int64_t ldw, int64_t n,
+                                          cudaStream_t stream) {
+  if (n < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!rho || !T || !Y || !wdot || ldy < n || ldw < n)
+    return PYRO_ERR_ARGUMENT;
+  const size_t sm = smem_cols(3);
+  if (prepare_smem((const void*)k_net_production_rates, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  k_net_production_rates<<<grid_for(n), BLOCK, sm, stream>>>(
+      rho, rho_inc, T, t_inc, Y, ldy, wdot, ldw, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_creation_destruction_rates(
+    const double* rho, int64_t rho_inc, const double* T, int64_t t_inc,
+    const double* Y, int64_t ldy, double* cdot, double* ddot, int64_t ldo,
+    int64_t n, cudaStream_t stream) {
+  if (n < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!rho || !T || !Y || (!cdot && !ddot) || ldy < n || ldo < n)
+    return PYRO_ERR_ARGUMENT;
+  const size_t sm = smem_cols(4);
+  if (prepare_smem((const void*)k_creation_destruction, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  k_creation_destruction<<<grid_for(n), BLOCK, sm, stream>>>(
+      rho, rho_inc, T, t_inc, Y, ldy, cdot, ddot, ldo, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_temperature(const double* target, int64_t target_inc,
+                                 const double* t0, int64_t t0_inc,
+                                 const double* Y, int64_t ldy, int do_energy,
+                                 double tol, int max_iter, double* T_out,
+                                 int* fail_count, int64_t n,
+                                 cudaStream_t stream) {
+  if (n < 0 || max_iter < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!target || !t0 || !Y || !T_out || ldy < n) return PYRO_ERR_ARGUMENT;
+  k_temperature<<<grid_for(n), BLOCK, 0, stream>>>(
+      target, target_inc, t0, t0_inc, Y, ldy, do_energy, tol, max_iter, T_out,
+      fail_count, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_fused_step(const double* p, int64_t p_inc,
+                                const double* T, int64_t t_inc,
+                                const double* Y, int64_t ldy,
+                                const double* target, int64_t target_inc,
+                                const double* t0, int64_t t0_inc,
+                                int do_energy, double tol, int max_iter,
+                                double* wdot, int64_t ldw, double* T_out,
+                                int* fail_count, int64_t n,
+                                cudaStream_t stream) {
+  if (n < 0 || max_iter < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!p || !T || !Y || !target || !t0 || !wdot || !T_out || ldy < n ||
+      ldw < n)
+    return PYRO_ERR_ARGUMENT;
+  const size_t sm = smem_cols(3);
+  if (prepare_smem((const void*)k_fused_step, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  k_fused_step<<<grid_for(n), BLOCK, sm, stream>>>(
+      p, p_inc, T, t_inc, Y, ldy, target, target_inc, t0, t0_inc, do_energy,
+      tol, max_iter, wdot, ldw, T_out, fail_count, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}

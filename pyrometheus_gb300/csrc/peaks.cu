@@ -1,0 +1,92 @@
+// Live FP64 roofline denominators for the benchmark: DFMA throughput of the
+// GPU and the FP64-pipe cost of CUDA's double-precision exp and log.
+//
+// Each kernel runs independent dependency chains per thread (enough ILP to
+// cover latency) over a grid of several waves; the host times a launch with
+// CUDA events.  Results are written through caller-provided device memory.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pyro_common.cuh"
+
+namespace {
+
+__global__ void k_dfma(double* out, int iters, double a, double b) {
+  double x0 = threadIdx.x * 1e-3, x1 = x0 + 1, x2 = x0 + 2, x3 = x0 + 3;
+  double x4 = x0 + 4, x5 = x0 + 5, x6 = x0 + 6, x7 = x0 + 7;
+  for (int i = 0; i < iters; ++i) {
+    x0 = fma(x0, a, b); x1 = fma(x1, a, b); x2 = fma(x2, a, b);
+    x3 = fma(x3, a, b); x4 = fma(x4, a, b); x5 = fma(x5, a, b);
+    x6 = fma(x6, a, b); x7 = fma(x7, a, b);
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] =
+      x0 + x1 + x2 + x3 + x4 + x5 + x6 + x7;
+}
+
+__global__ void k_exp(double* out, int iters) {
+  double x0 = -1.0 - threadIdx.x * 1e-6, x1 = x0 - 0.1, x2 = x0 - 0.2,
+         x3 = x0 - 0.3, s = 0.0;
+  for (int i = 0; i < iters; ++i) {
+    s += exp(x0) + exp(x1) + exp(x2) + exp(x3);
+    x0 -= 1e-7; x1 -= 1e-7; x2 -= 1e-7; x3 -= 1e-7;
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+__global__ void k_log(double* out, int iters) {
+  double x0 = 1.0 + threadIdx.x * 1e-6, x1 = x0 + 0.1, x2 = x0 + 0.2,
+         x3 = x0 + 0.3, s = 0.0;
+  for (int i = 0; i < iters; ++i) {
+    s += log(x0) + log(x1) + log(x2) + log(x3);
+    x0 += 1e-7; x1 += 1e-7; x2 += 1e-7; x3 += 1e-7;
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+// Number of doubles the scratch buffer of pyro_measure_fp64 must hold.
+PYRO_EXPORT int64_t pyro_peaks_scratch_doubles() {
+  return (int64_t)pyro_sm_count() * 8 * 256;
+}
+
+// results[0] = DFMA FLOP/s (2 per FMA), results[1] = exp(double)/s,
+// results[2] = log(double)/s.  scratch: pyro_peaks_scratch_doubles()
+// doubles of device memory.  Synchronous.
+PYRO_EXPORT int pyro_measure_fp64(double* scratch, double* results,
+                                  int repeats) {
+  if (!scratch || !results || repeats < 1) return PYRO_ERR_ARGUMENT;
+  const int blocks = pyro_sm_count() * 8, threads = 256;
+  const double n = (double)blocks * threads;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return PYRO_ERR_LAUNCH;
+  if (cudaEventCreate(&e1) != cudaSuccess) return PYRO_ERR_LAUNCH;
+  double best[3] = {0.0, 0.0, 0.0};
+  const int it_fma = 4096, it_exp = 256, it_log = 256;
+  for (int r = 0; r < repeats + 1; ++r) {
+    float ms = 0.f;
+    cudaEventRecord(e0);
+    k_dfma<<<blocks, threads>>>(scratch, it_fma, 1.0000001, 1e-9);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r && ms > 0) best[0] = fmax(best[0], 16.0 * it_fma * n / (ms * 1e-3));
+    cudaEventRecord(e0);
+    k_exp<<<blocks, threads>>>(scratch, it_exp);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r && ms > 0) best[1] = fmax(best[1], 4.0 * it_exp * n / (ms * 1e-3));
+    cudaEventRecord(e0);
+    k_log<<<blocks, threads>>>(scratch, it_log);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r && ms > 0) best[2] = fmax(best[2], 4.0 * it_log * n / (ms * 1e-3));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaGetLastError() != cudaSuccess) return PYRO_ERR_LAUNCH;
+  for (int q = 0; q < 3; ++q) results[q] = best[q];
+  return PYRO_OK;
+}

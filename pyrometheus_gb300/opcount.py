@@ -1,0 +1,145 @@
+"""Algorithmic FP64 work per state of the per-state kernels.
+
+The rate kernels are bound by the FP64 pipe (GB300: ~1.2 TFLOP/s of DFMA
+against ~7 TB/s of HBM), so their roofline is FP64 arithmetic.  This module
+counts, for a mechanism, the FP64 operations the formulation of
+``csrc/kinetics.cuh`` performs per state -- ``+ - *`` and comparisons-free
+arithmetic as 1 flop, FMA as 2, division as 1 -- and, separately, the
+transcendental calls (``exp``, ``log``, ``log10``, ``exp10``, ``pow``).
+
+A transcendental is charged the FP64 work CUDA's double-precision libm
+spends on it, measured on the GPU by the benchmark's microbenchmark
+(``flops per exp = DFMA FLOP/s / exp/s``), so that
+``algorithmic flops / kernel time / DFMA peak`` reads as the fraction of the
+FP64 pipe doing the algorithm's work.
+"""
+
+from __future__ import annotations
+
+from collections import Counter
+from typing import Dict
+
+TRANSCENDENTALS = ("exp", "log", "log10", "exp10", "pow")
+
+
+def _tables(sol):
+    from .codegen.cuda import _Model
+    return _Model(sol)
+
+
+def _arrhenius(rate, c: Counter):
+    if rate.Ta == 0.0 and rate.b == 0.0:
+        return
+    if rate.Ta == 0.0 and rate.b.is_integer() and abs(rate.b) <= 3:
+        c["flops"] += int(abs(rate.b))
+        return
+    c["flops"] += 4          # two FMAs
+    c["exp"] += 1
+
+
+def _product(terms, c: Counter):
+    for _, e in terms:
+        if e == 1.0:
+            c["flops"] += 1
+        elif e == 2.0:
+            c["flops"] += 2
+        else:
+            c["flops"] += 1
+            c["pow"] += 1
+
+
+def production_rates_counts(sol) -> Counter:
+    """Per-state counts of the net production rates (given rho, T, Y)."""
+    m = _tables(sol)
+    S = m.S
+    c = Counter()
+    c["log"] += 1                 # ln T
+    c["flops"] += 1 + 1           # 1/T, c0
+    c["flops"] += 3 * S           # c_k = (1/W_k) rho Y_k, total
+    c["flops"] += 17 * S          # g_k/RT (Horner with scaled coefficients)
+    c["flops"] += 0               # accumulators start at zero
+    for r in m.rx:
+        if r.kind != "elementary":
+            d = r.default_eff
+            c["flops"] += 0 if d in (0.0, 1.0) else 1
+            c["flops"] += 2 * sum(1 for e in r.eff.values() if e != d)
+        if r.kind == "falloff":
+            _arrhenius(r.high, c)
+            _arrhenius(r.low, c)
+            c["flops"] += 2       # Pr
+            if r.ftype == "Troe":
+                c["flops"] += 2 + 2 + 2   # T*a, products, sum
+                c["exp"] += 2
+                if len(r.fc) == 4:
+                    c["flops"] += 2
+                    c["exp"] += 1
+                c["log10"] += 2
+                c["flops"] += 3 + 4 + 1 + 2 + 1   # x, denominator, f, 1+f^2, /
+                c["exp10"] += 1
+            c["flops"] += 4       # kf = k_hi (F Pr / (1 + Pr))
+        else:
+            _arrhenius(r.rate, c)
+            if r.kind == "three-body":
+                c["flops"] += 1
+        _product(r.fwd, c)
+        if r.reversible:
+            n_terms = len(r.nu_p) + len(r.nu_r)
+            c["flops"] += n_terms + sum(1 for v in list(r.nu_p.values())
+                                        + list(r.nu_r.values()) if v != 1.0)
+            c["flops"] += 2 if r.dnu != 0 else 0
+            c["flops"] += 1       # exponent sum or kf * exp(lk)
+            c["exp"] += 1
+            if r.kind == "three-body":
+                c["flops"] += 1
+            _product(r.rev, c)
+        c["flops"] += 1           # q = rf - rr
+        for nu in list(r.nu_r.values()) + list(r.nu_p.values()):
+            c["flops"] += 1 if nu == 1.0 else 2
+    return c
+
+
+def temperature_counts(sol, iterations: float) -> Counter:
+    """Per-state counts of the temperature Newton with *iterations* mean
+    iterations (mass-weighted polynomials folded once per state)."""
+    m = _tables(sol)
+    S = m.S
+    ng = len(m.tmid_groups)
+    c = Counter()
+    c["flops"] += S * (1 + 1 + 24)      # w_k, sum, 12 FMAs
+    per_it = ng * (8 + 10 + 4 + 2) + 2 + 3   # cp, h, scaled q, sums; e-form; dT
+    c["flops"] += int(round(per_it * iterations))
+    return c
+
+
+def fused_step_counts(sol, newton_iterations: float) -> Counter:
+    """Density + net production rates + temperature Newton per state."""
+    m = _tables(sol)
+    c = Counter()
+    c["flops"] += 2 * m.S + 4           # 1/W_mix and rho
+    c.update(production_rates_counts(sol))
+    c.update(temperature_counts(sol, newton_iterations))
+    return c
+
+
+def weighted_flops(counts: Dict[str, float], weights: Dict[str, float]
+                   ) -> float:
+    """``flops + sum_t weight_t * count_t``."""
+    total = float(counts.get("flops", 0))
+    for t in TRANSCENDENTALS:
+        total += weights.get(t, 0.0) * float(counts.get(t, 0))
+    return total
+
+
+def libm_weights(dfma_flops: float, exp_rate: float, log_rate: float
+                 ) -> Dict[str, float]:
+    """FP64 flops charged per transcendental from measured throughputs."""
+    w_exp = dfma_flops / exp_rate
+    w_log = dfma_flops / log_rate
+    return {"exp": w_exp, "exp10": w_exp, "log": w_log, "log10": w_log,
+            "pow": w_exp + w_log}
+
+
+def bytes_per_state(sol) -> int:
+    """HBM bytes per state of the fused step: p, T, Y, e in; wdot, T out."""
+    S = sol.n_species
+    return 8 * (2 + S + 1) + 8 * (S + 1)

@@ -1,0 +1,475 @@
+"""Drop-in ``Thermochemistry`` on torch CUDA tensors.
+
+The class mirrors the generated numpy/JAX class of
+``pyrometheus/codegen/python.py:106-642``: the same attribute names
+(``python.py:180-199``), method names and argument order, and array shapes
+(species-major: ``Y[S, N]``; outputs ``[S, N]`` / ``[R, N]``; per-state
+scalars ``[N]``; Python scalars broadcast).  Every method runs a kernel of the
+mechanism's generated CUDA library through its C ABI on the current torch
+stream; there is no CPU path.  Inputs may be Python numbers, numpy arrays or
+torch tensors; they are moved to the device as float64.  Outputs are fresh
+CUDA float64 tensors, as the reference returns fresh arrays.
+
+``get_temperature`` keeps the reference's contract: Newton on
+``e(T) = e0`` (``do_energy=True``) or ``h(T) = h0`` with ``|dT| < 1e-6`` and
+at most 500 iterations, raising ``RuntimeError("Temperature iteration failed
+to converge")`` when any state does not converge (``python.py:375-396``).
+"""
+
+from __future__ import annotations
+
+import ctypes
+from typing import Optional
+
+import numpy as np
+
+from .mechanism import gas_constant, one_atm
+
+try:
+    import torch
+except ImportError:  # pragma: no cover - torch is a hard dependency
+    torch = None
+
+_STATUS = {
+    0: "ok",
+    1: "invalid argument",
+    2: "CUDA launch failed",
+    3: "Newton iteration did not converge",
+    4: "unsupported option",
+}
+
+SPECIES_PROPS = {"cp_r": 0, "h_rt": 1, "s_r": 2, "g_rt": 3, "dcp_r": 4,
+                 "dh_rt": 5, "ds_r": 6}
+MIXTURE_PROPS = {"mmw": 0, "rspec": 1, "cp": 2, "cv": 3, "h": 4, "e": 5,
+                 "density": 6, "pressure": 7}
+REACTION_MODES = {"log_keq": 0, "k_fwd": 1, "net": 2, "fwd": 3, "rev": 4}
+
+_P = ctypes.c_void_p
+_I64 = ctypes.c_int64
+_INT = ctypes.c_int
+_D = ctypes.c_double
+
+_SIGNATURES = {
+    "pyro_mechanism_info": [_P, _P, _P, _P, _P],
+    "pyro_species_property": [_INT, _P, _I64, _P, _I64, _I64, _P],
+    "pyro_mixture_property": [_INT, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
+                              _P],
+    "pyro_species_scale": [_INT, _P, _I64, _P, _I64, _P, _I64, _I64, _P],
+    "pyro_reaction_quantity": [_INT, _P, _I64, _P, _I64, _P, _I64, _I64, _P],
+    "pyro_net_production_rates": [_P, _I64, _P, _I64, _P, _I64, _P, _I64,
+                                  _I64, _P],
+    "pyro_creation_destruction_rates": [_P, _I64, _P, _I64, _P, _I64, _P, _P,
+                                        _I64, _I64, _P],
+    "pyro_temperature": [_P, _I64, _P, _I64, _P, _I64, _INT, _D, _INT, _P, _P,
+                         _I64, _P],
+    "pyro_fused_step": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
+                        _INT, _D, _INT, _P, _I64, _P, _P, _I64, _P],
+}
+
+
+def _is_scalar(x) -> bool:
+    return getattr(x, "ndim", 0) == 0
+
+
+def load_library(path: str) -> ctypes.CDLL:
+    """Open a generated mechanism library and declare its C ABI."""
+    lib = ctypes.CDLL(path)
+    for name, args in _SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.argtypes = args
+        fn.restype = ctypes.c_int
+    return lib
+
+
+def _check(status: int, what: str):
+    if status != 0:
+        raise RuntimeError(f"{what}: {_STATUS.get(status, status)} "
+                           f"(status {status})")
+
+
+class _Vec:
+    """A per-state scalar on the device: pointer + increment (0 broadcasts
+    one value)."""
+
+    __slots__ = ("t", "inc", "n", "scalar")
+
+    def __init__(self, t, inc, n, scalar):
+        self.t, self.inc, self.n, self.scalar = t, inc, n, scalar
+
+    @property
+    def ptr(self):
+        return self.t.data_ptr()
+
+
+class CudaThermochemistryBase:
+    """Base class of the generated CUDA ``Thermochemistry`` classes."""
+
+    _lib: ctypes.CDLL = None
+    _lib_path: str = ""
+    _sol = None
+
+    def __init__(self, pyro_np=None, device=None):
+        if torch is None or not torch.cuda.is_available():
+            raise RuntimeError(
+                "pyrometheus_gb300: the CUDA Thermochemistry needs a CUDA "
+                "device (there is no CPU path)")
+        self.pyro_np = pyro_np if pyro_np is not None else torch
+        self.device = torch.device(device if device is not None else "cuda")
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        sol = self._sol
+        self.model_name = getattr(sol, "source", "")
+        self.num_elements = int(sol.n_elements)
+        self.num_species = int(sol.n_species)
+        self.num_reactions = int(sol.n_reactions)
+        self.num_falloff = sum(1 for r in sol.reactions()
+                               if r.reaction_type.startswith("falloff"))
+        self.one_atm = one_atm
+        self.gas_constant = gas_constant
+        self.big_number = 1.0e300
+        self.species_names = list(sol.species_names)
+        self.species_indices = {n: i for i, n in
+                                enumerate(self.species_names)}
+        self.molecular_weights = np.array(sol.molecular_weights,
+                                          dtype=np.float64)
+        self.inv_molecular_weights = 1 / self.molecular_weights
+        ns, nr = ctypes.c_int(), ctypes.c_int()
+        _check(self._lib.pyro_mechanism_info(ctypes.byref(ns),
+                                             ctypes.byref(nr), None, None,
+                                             None), "mechanism_info")
+        if ns.value != self.num_species or nr.value != self.num_reactions:
+            raise RuntimeError("generated library does not match mechanism")
+        self._fail = torch.zeros(1, dtype=torch.int32, device=self.device)
+
+    # {{{ argument plumbing
+
+    @property
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(
+            self.device).cuda_stream)
+
+    def _dev(self, x):
+        if isinstance(x, torch.Tensor):
+            t = x.to(device=self.device, dtype=torch.float64)
+        else:
+            t = torch.as_tensor(np.asarray(x, dtype=np.float64),
+                                device=self.device)
+        return t
+
+    def _scalar_vec(self, x, n: Optional[int] = None) -> _Vec:
+        t = self._dev(x)
+        if t.numel() == 1:
+            return _Vec(t.reshape(1).contiguous(), 0, 1, t.dim() == 0)
+        t = t.reshape(-1).contiguous()
+        return _Vec(t, 1, t.numel(), False)
+
+    def _species_mat(self, y, rows: int):
+        """Species-major [rows, N] device matrix; returns (tensor, n,
+        single) where *single* marks a 1-D (one state) input."""
+        t = self._dev(y)
+        single = t.dim() == 1
+        if single:
+            t = t.reshape(rows, 1)
+        if t.dim() != 2 or t.shape[0] != rows:
+            raise ValueError(f"expected a [{rows}, N] array, got "
+                             f"{tuple(t.shape)}")
+        if t.stride(1) != 1 or t.stride(0) < max(1, t.shape[1]):
+            t = t.contiguous()
+        return t, t.shape[1], single
+
+    @staticmethod
+    def _n(*vecs):
+        n = 1
+        for v in vecs:
+            vn = v.n if isinstance(v, _Vec) else int(v)
+            if vn != 1:
+                if n != 1 and vn != n:
+                    raise ValueError(f"incompatible batch sizes {n} and "
+                                     f"{vn}")
+                n = vn
+        return n
+
+    def _expand_mat(self, m, n):
+        if m.shape[1] == n:
+            return m
+        if m.shape[1] == 1:
+            return m.expand(m.shape[0], n).contiguous()
+        raise ValueError("incompatible batch sizes")
+
+    def _out(self, rows, n):
+        return torch.empty((rows, n), dtype=torch.float64, device=self.device)
+
+    @staticmethod
+    def _shape_rows(out, single):
+        return out[:, 0] if single else out
+
+    @staticmethod
+    def _shape_vec(out, single):
+        return out[0] if single else out
+
+    # }}}
+
+    # {{{ mixture and species properties (python.py:242-358)
+
+    def get_species_name(self, species_index):
+        return self.species_names[species_index]
+
+    def get_species_index(self, species_name):
+        return self.species_indices[species_name]
+
+    def _mixture(self, which, temperature, mass_fractions, aux=None):
+        y, ny, single = self._species_mat(mass_fractions, self.num_species)
+        tv = self._scalar_vec(temperature) if temperature is not None \
+            else None
+        av = self._scalar_vec(aux) if aux is not None else None
+        n = self._n(ny, *(v for v in (tv, av) if v is not None))
+        y = self._expand_mat(y, n)
+        out = torch.empty(n, dtype=torch.float64, device=self.device)
+        _check(self._lib.pyro_mixture_property(
+            MIXTURE_PROPS[which], tv.ptr if tv else None,
+            tv.inc if tv else 0, y.data_ptr(), y.stride(0),
+            av.ptr if av else None, av.inc if av else 0, out.data_ptr(), n,
+            self._stream), f"mixture property {which}")
+        single = single and (tv is None or tv.n == 1)
+        return self._shape_vec(out, single)
+
+    def get_specific_gas_constant(self, mass_fractions):
+        return self._mixture("rspec", None, mass_fractions)
+
+    def get_mixture_molecular_weight(self, mass_fractions):
+        return self._mixture("mmw", None, mass_fractions)
+
+    def get_density(self, p, temperature, mass_fractions):
+        return self._mixture("density", temperature, mass_fractions, p)
+
+    def get_pressure(self, rho, temperature, mass_fractions):
+        return self._mixture("pressure", temperature, mass_fractions, rho)
+
+    def get_mixture_specific_heat_cp_mass(self, temperature, mass_fractions):
+        return self._mixture("cp", temperature, mass_fractions)
+
+    def get_mixture_specific_heat_cv_mass(self, temperature, mass_fractions):
+        return self._mixture("cv", temperature, mass_fractions)
+
+    def get_mixture_enthalpy_mass(self, temperature, mass_fractions):
+        return self._mixture("h", temperature, mass_fractions)
+
+    def get_mixture_internal_energy_mass(self, temperature, mass_fractions):
+        return self._mixture("e", temperature, mass_fractions)
+
+    def _scale(self, which, aux, mass_fractions):
+        y, ny, single = self._species_mat(mass_fractions, self.num_species)
+        av = self._scalar_vec(aux)
+        n = self._n(ny, av)
+        y = self._expand_mat(y, n)
+        out = self._out(self.num_species, n)
+        _check(self._lib.pyro_species_scale(
+            which, av.ptr, av.inc, y.data_ptr(), y.stride(0), out.data_ptr(),
+            out.stride(0), n, self._stream), "species scale")
+        return self._shape_rows(out, single and av.n == 1)
+
+    def get_concentrations(self, rho, mass_fractions):
+        return self._scale(0, rho, mass_fractions)
+
+    def get_mole_fractions(self, mix_mol_weight, mass_fractions):
+        return self._scale(1, mix_mol_weight, mass_fractions)
+
+    def get_mass_average_property(self, mass_fractions, spec_property):
+        y, _, _ = self._species_mat(mass_fractions, self.num_species)
+        p, _, _ = self._species_mat(spec_property, self.num_species)
+        w = torch.as_tensor(self.inv_molecular_weights, device=self.device)
+        return (y * p * w[:, None]).sum(dim=0)
+
+    def _species(self, which, temperature):
+        tv = self._scalar_vec(temperature)
+        n = tv.n
+        out = self._out(self.num_species, n)
+        _check(self._lib.pyro_species_property(
+            SPECIES_PROPS[which], tv.ptr, tv.inc, out.data_ptr(),
+            out.stride(0), n, self._stream), f"species property {which}")
+        return self._shape_rows(out, _is_scalar(temperature))
+
+    def get_species_specific_heats_r(self, temperature):
+        return self._species("cp_r", temperature)
+
+    def get_species_enthalpies_rt(self, temperature):
+        return self._species("h_rt", temperature)
+
+    def get_species_entropies_r(self, temperature):
+        return self._species("s_r", temperature)
+
+    def get_species_gibbs_rt(self, temperature):
+        return self._species("g_rt", temperature)
+
+    def get_species_specific_heats_r_derivative(self, temperature):
+        return self._species("dcp_r", temperature)
+
+    def get_species_enthalpies_rt_derivative(self, temperature):
+        return self._species("dh_rt", temperature)
+
+    def get_species_entropies_rt_derivative(self, temperature):
+        return self._species("ds_r", temperature)
+
+    # }}}
+
+    # {{{ kinetics (python.py:360-562)
+
+    def _reaction(self, mode, temperature, concentrations=None):
+        tv = self._scalar_vec(temperature)
+        if concentrations is not None:
+            c, nc, single = self._species_mat(concentrations,
+                                              self.num_species)
+            n = self._n(tv, nc)
+            c = self._expand_mat(c, n)
+        else:
+            c, n, single = None, tv.n, True
+        single = single and _is_scalar(temperature)
+        out = self._out(self.num_reactions, n)
+        _check(self._lib.pyro_reaction_quantity(
+            REACTION_MODES[mode], tv.ptr, tv.inc,
+            c.data_ptr() if c is not None else None,
+            c.stride(0) if c is not None else n, out.data_ptr(),
+            out.stride(0), n, self._stream), f"reaction quantity {mode}")
+        return self._shape_rows(out, single)
+
+    def get_equilibrium_constants(self, temperature):
+        return self._reaction("log_keq", temperature)
+
+    def get_fwd_rate_coefficients(self, temperature, concentrations):
+        return self._reaction("k_fwd", temperature, concentrations)
+
+    def get_falloff_rates(self, temperature, concentrations, k_fwd):
+        """Overwrites the falloff slots of *k_fwd* in place and returns None,
+        like ``python.py:399-450``."""
+        k = self._reaction("k_fwd", temperature, concentrations)
+        idx = [j for j, r in enumerate(self._sol.reactions())
+               if r.reaction_type.startswith("falloff")]
+        for j in idx:
+            k_fwd[j] = k[j]
+
+    def get_net_rates_of_progress(self, temperature, concentrations):
+        return self._reaction("net", temperature, concentrations)
+
+    def get_fwd_rates_of_progress(self, temperature, concentrations):
+        return self._reaction("fwd", temperature, concentrations)
+
+    def get_rev_rates_of_progress(self, temperature, concentrations):
+        return self._reaction("rev", temperature, concentrations)
+
+    def get_net_production_rates(self, rho, temperature, mass_fractions):
+        """``python.py:486-495`` -- the hot path."""
+        y, ny, single = self._species_mat(mass_fractions, self.num_species)
+        rv = self._scalar_vec(rho)
+        tv = self._scalar_vec(temperature)
+        n = self._n(ny, rv, tv)
+        y = self._expand_mat(y, n)
+        out = self._out(self.num_species, n)
+        _check(self._lib.pyro_net_production_rates(
+            rv.ptr, rv.inc, tv.ptr, tv.inc, y.data_ptr(), y.stride(0),
+            out.data_ptr(), out.stride(0), n, self._stream),
+            "net production rates")
+        return self._shape_rows(out, single and n == 1)
+
+    def get_creation_destruction_rates(self, rho, temperature,
+                                       mass_fractions):
+        y, ny, single = self._species_mat(mass_fractions, self.num_species)
+        rv = self._scalar_vec(rho)
+        tv = self._scalar_vec(temperature)
+        n = self._n(ny, rv, tv)
+        y = self._expand_mat(y, n)
+        cd = self._out(self.num_species, n)
+        dd = self._out(self.num_species, n)
+        _check(self._lib.pyro_creation_destruction_rates(
+            rv.ptr, rv.inc, tv.ptr, tv.inc, y.data_ptr(), y.stride(0),
+            cd.data_ptr(), dd.data_ptr(), cd.stride(0), n, self._stream),
+            "creation/destruction rates")
+        s = single and n == 1
+        return self._shape_rows(cd, s), self._shape_rows(dd, s)
+
+    def get_creation_rates(self, rho, temperature, mass_fractions):
+        return self.get_creation_destruction_rates(rho, temperature,
+                                                   mass_fractions)[0]
+
+    def get_destruction_rates(self, rho, temperature, mass_fractions):
+        return self.get_creation_destruction_rates(rho, temperature,
+                                                   mass_fractions)[1]
+
+    # }}}
+
+    # {{{ temperature (python.py:375-396; flamelets/make_pyro.py:255-299)
+
+    def _temperature(self, target, t_guess, y, do_energy, tol, max_iter,
+                     check=True):
+        ym, ny, single = self._species_mat(y, self.num_species)
+        ev = self._scalar_vec(target)
+        tv = self._scalar_vec(t_guess)
+        n = self._n(ny, ev, tv)
+        ym = self._expand_mat(ym, n)
+        out = torch.empty(n, dtype=torch.float64, device=self.device)
+        self._fail.zero_()
+        _check(self._lib.pyro_temperature(
+            ev.ptr, ev.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
+            1 if do_energy else 0, float(tol), int(max_iter),
+            out.data_ptr(), self._fail.data_ptr(), n, self._stream),
+            "temperature")
+        if check and int(self._fail.item()) > 0:
+            raise RuntimeError("Temperature iteration failed to converge")
+        return self._shape_vec(out, single and ev.n == 1)
+
+    def get_temperature(self, enthalpy_or_energy, t_guess, y,
+                        do_energy=False):
+        return self._temperature(enthalpy_or_energy, t_guess, y, do_energy,
+                                 1.0e-6, 500)
+
+    def get_temperature_from_enthalpy(self, enthalpy, mass_fractions,
+                                      temp_init):
+        """Enthalpy form used by the flamelet equations
+        (``flamelets/make_pyro.py:255-299``), iterated per state to
+        ``|dT| < 1e-10``."""
+        return self._temperature(enthalpy, temp_init, mass_fractions, False,
+                                 1.0e-10, 500)
+
+    # }}}
+
+    # {{{ fused state step
+
+    def get_net_production_rates_and_temperature(
+            self, pressure, temperature, mass_fractions, energy, t_guess,
+            do_energy=True, check=True):
+        """One pass per state of ``rho = get_density(p, T, Y)``,
+        ``get_net_production_rates(rho, T, Y)`` and
+        ``get_temperature(energy, t_guess, Y, do_energy)``.
+
+        :returns: ``(wdot[S, N], T_new[N])``.
+        """
+        ym, ny, single = self._species_mat(mass_fractions, self.num_species)
+        pv = self._scalar_vec(pressure)
+        tv = self._scalar_vec(temperature)
+        ev = self._scalar_vec(energy)
+        gv = self._scalar_vec(t_guess)
+        n = self._n(ny, pv, tv, ev, gv)
+        ym = self._expand_mat(ym, n)
+        wdot = self._out(self.num_species, n)
+        tout = torch.empty(n, dtype=torch.float64, device=self.device)
+        self._fail.zero_()
+        _check(self._lib.pyro_fused_step(
+            pv.ptr, pv.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
+            ev.ptr, ev.inc, gv.ptr, gv.inc, 1 if do_energy else 0, 1.0e-6,
+            500, wdot.data_ptr(), wdot.stride(0), tout.data_ptr(),
+            self._fail.data_ptr(), n, self._stream), "fused step")
+        if check and int(self._fail.item()) > 0:
+            raise RuntimeError("Temperature iteration failed to converge")
+        return wdot, tout
+
+    # }}}
+
+
+def make_thermochem_class(sol, lib_path: str, name: str = "Thermochemistry"):
+    """A ``Thermochemistry`` class bound to the compiled library."""
+    lib = load_library(lib_path)
+    return type(name, (CudaThermochemistryBase,),
+                {"_lib": lib, "_lib_path": lib_path, "_sol": sol,
+                 "__doc__": f"CUDA thermochemistry for {sol.n_species} "
+                            f"species / {sol.n_reactions} reactions."})
+
+# vim: foldmethod=marker

@@ -1,0 +1,96 @@
+"""The C-ABI libraries load and export every symbol the public header
+declares (no GPU needed: no compute is called)."""
+
+import ctypes
+import os
+import re
+
+import pytest
+
+from conftest import ROOT
+
+HEADER_DIR = os.path.join(ROOT, "include")
+
+
+def declared(header):
+    with open(os.path.join(HEADER_DIR, header)) as f:
+        text = f.read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\bint\s+(pyro_\w+)\s*\(", text)))
+
+
+def test_header_parses():
+    names = declared("pyrometheus_gb300.h")
+    assert "pyro_net_production_rates" in names
+    assert len(names) >= 9
+
+
+def test_mechanism_library_exports_header_symbols():
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.codegen.cuda import (CudaCodeGenerator,
+                                                build_shared_library)
+    sol = synthetic.config1_mechanism()
+    lib = build_shared_library(CudaCodeGenerator.generate("t", sol), "abi")
+    so = ctypes.CDLL(lib)
+    for name in declared("pyrometheus_gb300.h"):
+        assert hasattr(so, name), name
+    ns, nr, nf = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    assert so.pyro_mechanism_info(ctypes.byref(ns), ctypes.byref(nr),
+                                  ctypes.byref(nf), None, None) == 0
+    assert (ns.value, nr.value, nf.value) == (9, 24, 2)
+
+
+def test_argument_errors_without_launch():
+    """Argument checks happen before any CUDA call, so they run without a
+    GPU: a negative size or a short leading dimension is rejected."""
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.codegen.cuda import (CudaCodeGenerator,
+                                                build_shared_library)
+    from pyrometheus_gb300.thermochemistry import load_library
+    sol = synthetic.config1_mechanism()
+    so = load_library(build_shared_library(
+        CudaCodeGenerator.generate("t", sol), "abi"))
+    assert so.pyro_net_production_rates(None, 0, None, 0, None, 0, None, 0,
+                                        -1, None) == 1
+    assert so.pyro_net_production_rates(None, 0, None, 0, None, 0, None, 0,
+                                        0, None) == 0
+    assert so.pyro_net_production_rates(1, 0, 1, 0, 1, 4, 1, 8, 8,
+                                        None) == 1
+    assert so.pyro_species_property(9, 1, 0, 1, 8, 8, None) == 1
+
+
+def test_no_cpu_fallback():
+    """Without a CUDA device the drop-in class refuses to run."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
+    cls = get_thermochem_class(synthetic.config1_mechanism())
+    with pytest.raises(RuntimeError, match="CUDA"):
+        cls()
+
+
+def test_generator_options_like_reference():
+    from pyrometheus_gb300 import CodeGenerationOptions, synthetic
+    from pyrometheus_gb300.codegen.cuda import CudaCodeGenerator
+    sol = synthetic.config1_mechanism()
+    with pytest.raises(TypeError):
+        CudaCodeGenerator.generate(
+            "t", sol, CodeGenerationOptions(directive_offload="acc"))
+    with pytest.raises(TypeError):
+        CudaCodeGenerator.generate(
+            "t", sol, CodeGenerationOptions(scalar_type="float"))
+    assert CudaCodeGenerator.get_name() == "cuda"
+    assert CudaCodeGenerator.supports_overloading()
+
+
+def test_cli_writes_source(tmp_path):
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.cli import main
+    from pyrometheus_gb300.yaml_mech import dump_mechanism
+    mech = tmp_path / "m.yaml"
+    mech.write_text(dump_mechanism(synthetic.config1_mechanism()))
+    out = tmp_path / "m.cu"
+    main(["-l", "cuda", "-m", str(mech), "-o", str(out), "-n", "m"])
+    src = out.read_text()
+    assert "#define NS 9" in src and '#include "kinetics.cuh"' in src
