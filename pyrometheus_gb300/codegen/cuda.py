@@ -62,11 +62,18 @@ class CudaGenerationOptions(CodeGenerationOptions):
     ``block_size``: threads per block of the per-state kernels (``None``:
     as many as let two blocks' per-thread shared-memory columns fit on an
     SM, at most 128);
-    ``blocks_per_sm``: grid cap, in blocks per SM, of the grid-stride loops.
+    ``blocks_per_sm``: grid cap, in blocks per SM, of the grid-stride loops;
+    ``unrolled``: emit the straight-line variant of the net-production-rate
+    and fused-step kernels (the table-driven kernels serve every other
+    method, and the rare states the fast path flags);
+    ``accum_in_smem``: keep that variant's production-rate accumulators in
+    a shared-memory column instead of registers.
     """
 
     block_size: Optional[int] = None
     blocks_per_sm: int = 8
+    unrolled: bool = True
+    accum_in_smem: bool = False
 
 
 # {{{ mechanism model
@@ -414,8 +421,224 @@ class _Emitter:
                   for row in (frac or [[0.0] * (3 * maxside)])]))
         w("")
         w('#include "kinetics.cuh"')
+        if self.opts.unrolled:
+            L.extend(_UnrolledEmitter(m, self.opts.accum_in_smem).render())
         w('#include "kinetics_abi.cuh"')
         return "\n".join(L) + "\n"
+
+
+class _UnrolledEmitter:
+    """Straight-line variant of the net-production-rate kernels.
+
+    Every reaction becomes its own block of FP64 code with compile-time
+    species offsets: the scheduler interleaves independent reactions (ILP
+    across reactions), rate accumulators live in registers, and only the
+    concentrations and Gibbs energies stay in shared memory (two columns
+    instead of three, so more warps fit per SM).  Exponentials are
+    branch-free (the table method on a sanitised argument); a state with an
+    exponent outside |x| < 708 raises a flag and is recomputed exactly by
+    the table-driven path on thread-private arrays.
+    """
+
+    def __init__(self, m: _Model, accum_in_smem: bool = False):
+        self.m = m
+        self.acc_smem = accum_in_smem
+        self.L: List[str] = []
+
+    def W(self, k):
+        return f"w[{k}]" if self.acc_smem else f"wd[{k}]"
+
+    def w(self, s):
+        self.L.append(s)
+
+    @staticmethod
+    def C(k):
+        return f"c[{k}]"
+
+    @staticmethod
+    def G(k):
+        return f"g[{k}]"
+
+    def rate_expr(self, rate: _Rate, tag: str) -> Tuple[Optional[str], str]:
+        """(exponent variable or None, statement defining e_<tag>)."""
+        form, rec = _rate_record(rate)
+        if form == 1:
+            return None, f"const double e_{tag} = {_dlit(rec[0])};"
+        if form == 2:
+            b = int(rec[1])
+            base = "T" if b > 0 else "invT"
+            ex = "*".join([_dlit(rec[0])] + [base] * abs(b))
+            return None, f"const double e_{tag} = {ex};"
+        ln_a, b, ta = rec
+        if b == 0.0:
+            x = f"fma({_dlit(-ta)}, invT, {_dlit(ln_a)})"
+        elif ta == 0.0:
+            x = f"fma({_dlit(b)}, lnT, {_dlit(ln_a)})"
+        else:
+            x = (f"fma({_dlit(b)}, lnT, fma({_dlit(-ta)}, invT, "
+                 f"{_dlit(ln_a)}))")
+        return (f"x_{tag}", f"const double x_{tag} = {x}; "
+                f"const double e_{tag} = fx(x_{tag}, bad);")
+
+    def third_body(self, r: _Reaction) -> str:
+        d = r.default_eff
+        terms = []
+        if d != 0.0:
+            terms.append("ctot" if d == 1.0 else f"{_hexd(d)} * ctot")
+        for k, e in sorted(r.eff.items()):
+            if e != d:
+                terms.append(f"{_hexd(e - d)} * {self.C(k)}")
+        return " + ".join(terms) if terms else "0.0"
+
+    def prod(self, terms) -> str:
+        parts = []
+        for k, nu in terms:
+            c = self.C(k)
+            if nu == 1.0:
+                parts.append(c)
+            elif nu == 2.0:
+                parts.append(f"{c} * {c}")
+            else:
+                parts.append(f"pow({c}, {_hexd(nu)})")
+        return " * ".join(parts) if parts else "1.0"
+
+    def log_keq(self, r: _Reaction) -> str:
+        def side(d):
+            parts = [self.G(k) if nu == 1.0 else f"{_hexd(nu)} * {self.G(k)}"
+                     for k, nu in d.items()]
+            return "(" + " + ".join(parts) + ")" if parts else "0.0"
+        e = f"{side(r.nu_p)} - {side(r.nu_r)}"
+        if r.dnu != 0:
+            e = f"fma({_hexd(-r.dnu)}, c0, {e})"
+        return e
+
+    def troe_term(self, coef: float, scale: str, fac: float) -> Optional[str]:
+        """fac * exp(coef * scale) with the exponent's range known from
+        T in [200, 5000] K: folded to 0 or fac when it under-/overflows
+        the double range or rounds to exp(0)."""
+        if fac == 0.0:
+            return None
+        if scale == "T":
+            lo, hi = sorted((coef * 200.0, coef * 5000.0))
+        else:  # invT
+            lo, hi = sorted((coef / 200.0, coef / 5000.0))
+        if hi < -745.2:
+            return None
+        if max(abs(lo), abs(hi)) < 1e-17:
+            return _hexd(fac)
+        return f"{_hexd(fac)} * fx({_hexd(coef)} * {scale}, bad)"
+
+    def reaction(self, r: _Reaction):
+        w = self.w
+        w(f"  {{  // R{r.j}: {r.equation}")
+        if r.kind != "elementary":
+            w(f"    const double m = {self.third_body(r)};")
+        xf = None
+        if r.kind == "falloff":
+            xh, sh = self.rate_expr(r.high, "hi")
+            xl, sl = self.rate_expr(r.low, "lo")
+            w(f"    {sh}")
+            w(f"    {sl}")
+            w("    const double pr = m * e_lo / e_hi;")
+            if r.ftype == "Troe":
+                a, t3, t1 = r.fc[0], r.fc[1], r.fc[2]
+                terms = [self.troe_term(-1.0 / t3, "T", 1.0 - a),
+                         self.troe_term(-1.0 / t1, "T", a)]
+                if len(r.fc) == 4:
+                    terms.append(self.troe_term(-r.fc[3], "invT", 1.0))
+                terms = [t for t in terms if t is not None] or ["0.0"]
+                w(f"    const double log_fc = log10({' + '.join(terms)});")
+                w("    double fac = -1.0 / 0.14;")
+                w("    if (pr > 0.0) {")
+                w("      const double xx = log10(pr) + (-0.4 - 0.67 * log_fc);")
+                w("      fac = xx / ((0.75 - 1.27 * log_fc) - 0.14 * xx);")
+                w("    }")
+                w("    const double blend = fx(log_fc / (1.0 + fac * fac) * "
+                  "2.302585092994045684, bad);")
+            else:
+                w("    const double blend = 1.0;")
+            w("    const double kf = e_hi * (blend * pr / (1.0 + pr));")
+        else:
+            xf, sf = self.rate_expr(r.rate, "f")
+            w(f"    {sf}")
+            w("    const double kf = " + ("e_f * m" if r.kind == "three-body"
+                                          else "e_f") + ";")
+        if r.reversible:
+            w(f"    const double lk = {self.log_keq(r)};")
+            if xf is not None:
+                w("    const double kr = fx(x_f + lk, bad)" +
+                  (" * m" if r.kind == "three-body" else "") + ";")
+            else:
+                w("    const double kr = kf * fx(lk, bad);")
+            w(f"    const double q = kf * {self.prod(r.fwd)} - kr * "
+              f"{self.prod(r.rev)};")
+        else:
+            w(f"    const double q = kf * {self.prod(r.fwd)};")
+        net: Dict[int, float] = {}
+        for k, nu in r.nu_p.items():
+            net[k] = net.get(k, 0.0) + nu
+        for k, nu in r.nu_r.items():
+            net[k] = net.get(k, 0.0) - nu
+        for k, nu in sorted(net.items()):
+            acc = self.W(k)
+            if nu == 1.0:
+                w(f"    {acc} += q;")
+            elif nu == -1.0:
+                w(f"    {acc} -= q;")
+            elif nu != 0.0:
+                w(f"    {acc} = fma({_hexd(nu)}, q, {acc});")
+        w("  }")
+
+    def render(self) -> List[str]:
+        m = self.m
+        w = self.w
+        w("")
+        w("// ---- unrolled hot path (generated) ----")
+        w("#define PYRO_UNROLLED 1")
+        w(f"#define PYRO_HOT_COLS {3 if self.acc_smem else 2}")
+        w("namespace pyro_unrolled {")
+        w("")
+        w("// exp on a sanitised argument: out-of-range lanes set *bad* and")
+        w("// are recomputed exactly afterwards")
+        w("__device__ __forceinline__ double fx(double x, bool& bad) {")
+        w("  const bool out = (__double2hiint(x) & 0x7fffffff) >= 0x40862000;")
+        w("  bad |= out;")
+        w("  return pyro_exp_core(out ? 0.0 : x);")
+        w("}")
+        w("")
+        w("__device__ __forceinline__ void net_rates(double T, double rho, "
+          "const double* __restrict__ Y, int64_t ldy, int64_t i, "
+          "pyro::Cols c, pyro::Cols g, pyro::Cols w, double (&wd)[NS]) {")
+        w("  const double lnT = log(T);")
+        w("  const double invT = 1.0 / T;")
+        w("  const double c0 = LOG_P0_OVER_R - lnT;")
+        w("  double ctot = 0.0;")
+        for k in range(m.S):
+            w(f"  {{ const double v = {_hexd(m.invW[k])} * rho * "
+              f"__ldg(Y + (int64_t){k} * ldy + i); c[{k}] = v; ctot += v; }}")
+        w("  pyro::gibbs_all(T, lnT, invT, g);")
+        for k in range(m.S):
+            w(f"  {self.W(k)} = 0.0;")
+        w("  bool bad = false;")
+        for r in m.rx:
+            self.reaction(r)
+        w("  if (bad) {  // exact recompute through the table-driven path")
+        w("    double lc[NS], lg[NS], lw[NS];")
+        w("    const pyro::LocalCols C{lc}, G{lg}, W{lw};")
+        w("    const pyro::StateScalars s = "
+          "pyro::state_from_mass(T, rho, Y, ldy, i, C);")
+        w("    pyro::production_rates(s, C, G, W);")
+        w("#pragma unroll")
+        w("    for (int k = 0; k < NS; ++k) " +
+          ("w[k] = lw[k];" if self.acc_smem else "wd[k] = lw[k];"))
+        w("  }")
+        if self.acc_smem:
+            w("#pragma unroll")
+            w("  for (int k = 0; k < NS; ++k) wd[k] = w[k];")
+        w("}")
+        w("")
+        w("}  // namespace pyro_unrolled")
+        return self.L
 
 
 def _default_block(n_species: int) -> int:

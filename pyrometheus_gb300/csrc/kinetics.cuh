@@ -27,6 +27,26 @@
 
 #include "pyro_common.cuh"
 
+// PYRO_FAST_EXP (default 1): Tang's table-driven exp of pyro_math.cuh for
+// every exponential of the rate evaluation; 0 uses CUDA's exp.
+#ifndef PYRO_FAST_EXP
+#define PYRO_FAST_EXP 1
+#endif
+#if PYRO_FAST_EXP
+#include "pyro_math.cuh"
+#define PEXP(x) pyro_exp(x)
+#define PEXP10(x) pyro_exp10(x)
+#define PEXP_PRELOAD() PYRO_EXP_PRELOAD()
+#define PYRO_STATIC_SMEM (PYRO_EXP_N * sizeof(double))
+#else
+#define PYRO_STATIC_SMEM 0
+#define PEXP(x) exp(x)
+#define PEXP10(x) exp10(x)
+#define PEXP_PRELOAD() \
+  do {                 \
+  } while (0)
+#endif
+
 #define RX_KIND_MASK 3
 #define RX_ELEMENTARY 0
 #define RX_THREE_BODY 1
@@ -47,13 +67,17 @@
 
 namespace pyro {
 
-// Column accessors into the per-thread shared-memory slices.
-struct Cols {
+// Per-thread column of NS doubles: a shared-memory slice (stride BLOCK, the
+// threads of a block interleaved) or a thread-private array (stride 1).
+template <int STRIDE>
+struct ColsT {
   double* base;
   __device__ __forceinline__ double& operator[](int k) const {
-    return base[k * BLOCK];
+    return base[k * STRIDE];
   }
 };
+using Cols = ColsT<BLOCK>;
+using LocalCols = ColsT<1>;
 
 __device__ __forceinline__ Cols col(double* smem, int q) {
   return Cols{smem + (size_t)q * NS * BLOCK + threadIdx.x};
@@ -65,7 +89,7 @@ __device__ __forceinline__ double arrhenius(int form, double p0, double p1,
                                             double invT, double& x) {
   if (form == FORM_EXP) {
     x = fma(p1, lnT, fma(-p2, invT, p0));
-    return exp(x);
+    return PEXP(x);
   }
   x = 0.0;
   if (form == FORM_CONST) return p0;
@@ -96,8 +120,9 @@ struct Nasa {
 };
 
 // g_k/RT = h/RT - s/R for every species (chem_expr.py:80-117).
+template <class CT>
 __device__ __forceinline__ void gibbs_all(double T, double lnT, double invT,
-                                          Cols g) {
+                                          CT g) {
   for (int k = 0; k < NS; ++k) {
     const Nasa a(k, T > k_tmid[k]);
     // a0 (1 - ln T) + a5 / T - a6 - T (a1/2 + T (a2/6 + T (a3/12 + T a4/20)))
@@ -111,8 +136,9 @@ __device__ __forceinline__ void gibbs_all(double T, double lnT, double invT,
 // log K for reaction j (chem_expr.py:274-302; python.py:360-373):
 // sum nu'' g - sum nu' g - dnu ln(p0 / RT); irreversible slots hold the
 // reference's placeholder -0.17364695002734 T.
+template <class CT>
 __device__ __forceinline__ double log_keq(int j, int f, double T, double c0,
-                                          Cols g) {
+                                          CT g) {
   if (!(f & RX_REVERSIBLE)) return IRREVERSIBLE_LOG_KEQ_SLOPE * T;
   const int nr = k_rx_nr[j], np = k_rx_np[j];
   double sp = 0.0, sr = 0.0;
@@ -148,9 +174,10 @@ __device__ __forceinline__ double log_keq(int j, int f, double T, double c0,
 //       (python.py:399-473)
 //   rf = kf prod c^ord'  (orders paired positionally, chem_expr.py:436-446)
 //   rr = kf exp(log K) prod c^nu''  (0 when irreversible or !want_rev)
+template <class CT>
 __device__ __forceinline__ void reaction_rates(int j, double T, double lnT,
                                                double invT, double c0,
-                                               double ctot, Cols c, Cols g,
+                                               double ctot, CT c, CT g,
                                                bool want_rev, double& kf,
                                                double& rf, double& rr) {
   const int f = k_rx_flags[j];
@@ -180,16 +207,16 @@ __device__ __forceinline__ void reaction_rates(int j, double T, double lnT,
     double blend = 1.0;
     if (f & RX_TROE) {
       // log10 Fcent, Troe broadening (chem_expr.py:348-420)
-      double fsum = k_fo_troe[s][0] * exp(T * k_fo_troe[s][1]) +
-                    k_fo_troe[s][2] * exp(T * k_fo_troe[s][3]);
-      if (f & RX_TROE_T2) fsum += exp(k_fo_troe[s][4] * invT);
+      double fsum = k_fo_troe[s][0] * PEXP(T * k_fo_troe[s][1]) +
+                    k_fo_troe[s][2] * PEXP(T * k_fo_troe[s][3]);
+      if (f & RX_TROE_T2) fsum += PEXP(k_fo_troe[s][4] * invT);
       const double log_fc = log10(fsum);
       double fac = -1.0 / 0.14;
       if (pr > 0.0) {
         const double xx = log10(pr) + (-0.4 - 0.67 * log_fc);
         fac = xx / ((0.75 - 1.27 * log_fc) - 0.14 * xx);
       }
-      blend = exp10(log_fc / (1.0 + fac * fac));
+      blend = PEXP10(log_fc / (1.0 + fac * fac));
     }
     kf = k_hi * (blend * pr / (1.0 + pr));
   } else {
@@ -217,10 +244,10 @@ __device__ __forceinline__ void reaction_rates(int j, double T, double lnT,
     double kr;
     if (exp_form) {
       // k_r = exp(ln k_f + log K) [* M]: reuses the forward exponent
-      kr = exp(x + lk);
+      kr = PEXP(x + lk);
       if (kind == RX_THREE_BODY) kr *= m;
     } else {
-      kr = kf * exp(lk);
+      kr = kf * PEXP(lk);
     }
     double pv = 1.0;
     for (int a = 0; a < MAXSIDE; ++a) {
@@ -236,7 +263,8 @@ __device__ __forceinline__ void reaction_rates(int j, double T, double lnT,
 }
 
 // Scatter a rate into per-species accumulators with weights -nu' / +nu''.
-__device__ __forceinline__ void scatter_net(int j, double q, Cols w) {
+template <class CT>
+__device__ __forceinline__ void scatter_net(int j, double q, CT w) {
   const int f = k_rx_flags[j];
   const int nr = k_rx_nr[j], np = k_rx_np[j];
   if (f & RX_FRACTIONAL) {
@@ -269,8 +297,9 @@ __device__ __forceinline__ void scatter_net(int j, double q, Cols w) {
 
 // creation += nu'' rf + nu' rr ; destruction += nu' rf + nu'' rr
 // (chem_expr.py:525-567)
+template <class CT>
 __device__ __forceinline__ void scatter_cd(int j, double rf, double rr,
-                                           Cols cd, Cols dd) {
+                                           CT cd, CT dd) {
   const int f = k_rx_flags[j];
   const int nr = k_rx_nr[j], np = k_rx_np[j];
   const bool frac = (f & RX_FRACTIONAL) != 0;
@@ -298,9 +327,10 @@ struct StateScalars {
   double T, lnT, invT, c0, ctot;
 };
 
+template <class CT>
 __device__ __forceinline__ StateScalars state_from_mass(
     double T, double rho, const double* __restrict__ Y, int64_t ldy,
-    int64_t i, Cols c) {
+    int64_t i, CT c) {
   StateScalars s;
   s.T = T;
   s.lnT = log(T);
@@ -337,8 +367,9 @@ __device__ __forceinline__ StateScalars state_from_conc(
 }
 
 // Net production rates of one state into w (python.py:486-495).
+template <class CT>
 __device__ __forceinline__ void production_rates(const StateScalars& s,
-                                                 Cols c, Cols g, Cols w) {
+                                                 CT c, CT g, CT w) {
   gibbs_all(s.T, s.lnT, s.invT, g);
   for (int k = 0; k < NS; ++k) w[k] = 0.0;
   for (int j = 0; j < NR; ++j) {
@@ -545,6 +576,7 @@ __global__ void __launch_bounds__(BLOCK)
                         int64_t ldc, double* __restrict__ out, int64_t ldo,
                         int64_t n) {
   extern __shared__ double smem[];
+  PEXP_PRELOAD();
   const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1);
   PYRO_LOOP(i) {
     const double T = pyro_ld(Tp, t_inc, i);
@@ -575,6 +607,7 @@ __global__ void __launch_bounds__(BLOCK)
                            double* __restrict__ wdot, int64_t ldw,
                            int64_t n) {
   extern __shared__ double smem[];
+  PEXP_PRELOAD();
   const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
                    w = pyro::col(smem, 2);
   PYRO_LOOP(i) {
@@ -594,6 +627,7 @@ __global__ void __launch_bounds__(BLOCK)
                            double* __restrict__ ddot, int64_t ldo,
                            int64_t n) {
   extern __shared__ double smem[];
+  PEXP_PRELOAD();
   const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
                    cd = pyro::col(smem, 2), dd = pyro::col(smem, 3);
   PYRO_LOOP(i) {
@@ -647,6 +681,7 @@ __global__ void __launch_bounds__(BLOCK)
                  int64_t ldw, double* __restrict__ Tout,
                  int* __restrict__ fail_count, int64_t n) {
   extern __shared__ double smem[];
+  PEXP_PRELOAD();
   const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
                    w = pyro::col(smem, 2);
   PYRO_LOOP(i) {

@@ -6,6 +6,70 @@
 
 #include "kinetics.cuh"
 
+#ifdef PYRO_UNROLLED
+// Straight-line variants (pyro_unrolled::net_rates is generated per
+// mechanism): shared memory holds only concentrations and Gibbs energies.
+__global__ void __launch_bounds__(BLOCK)
+    k_net_production_rates_u(const double* __restrict__ rhop,
+                             int64_t rho_inc, const double* __restrict__ Tp,
+                             int64_t t_inc, const double* __restrict__ Y,
+                             int64_t ldy, double* __restrict__ wdot,
+                             int64_t ldw, int64_t n) {
+  extern __shared__ double smem[];
+  PEXP_PRELOAD();
+  const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
+                   w = pyro::col(smem, PYRO_HOT_COLS - 1);
+  PYRO_LOOP(i) {
+    double wd[NS];
+    pyro_unrolled::net_rates(pyro_ld(Tp, t_inc, i), pyro_ld(rhop, rho_inc, i),
+                             Y, ldy, i, c, g, w, wd);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) wdot[(int64_t)k * ldw + i] = wd[k];
+  }
+}
+
+__global__ void __launch_bounds__(BLOCK)
+    k_fused_step_u(const double* __restrict__ Pp, int64_t p_inc,
+                   const double* __restrict__ Tp, int64_t t_inc,
+                   const double* __restrict__ Y, int64_t ldy,
+                   const double* __restrict__ target, int64_t target_inc,
+                   const double* __restrict__ t0, int64_t t0_inc,
+                   int do_energy, double tol, int max_iter,
+                   double* __restrict__ wdot, int64_t ldw,
+                   double* __restrict__ Tout, int* __restrict__ fail_count,
+                   int64_t n) {
+  extern __shared__ double smem[];
+  PEXP_PRELOAD();
+  const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
+                   w = pyro::col(smem, PYRO_HOT_COLS - 1);
+  PYRO_LOOP(i) {
+    const double T = pyro_ld(Tp, t_inc, i);
+    double inv_mmw = 0.0;
+    for (int k = 0; k < NS; ++k)
+      inv_mmw = fma(k_inv_mw[k], __ldg(Y + (int64_t)k * ldy + i), inv_mmw);
+    const double rho =
+        pyro_ld(Pp, p_inc, i) * (1.0 / inv_mmw) / (GAS_CONSTANT * T);
+    double wd[NS];
+    pyro_unrolled::net_rates(T, rho, Y, ldy, i, c, g, w, wd);
+#pragma unroll
+    for (int k = 0; k < NS; ++k) wdot[(int64_t)k * ldw + i] = wd[k];
+    double Tn;
+    const bool ok = pyro::temperature_newton(
+        pyro_ld(target, target_inc, i), pyro_ld(t0, t0_inc, i), Y, ldy, i,
+        do_energy != 0, tol, max_iter, Tn);
+    Tout[i] = Tn;
+    if (!ok && fail_count) atomicAdd(fail_count, 1);
+  }
+}
+#define HOT_COLS PYRO_HOT_COLS
+#define K_NET k_net_production_rates_u
+#define K_FUSED k_fused_step_u
+#else
+#define HOT_COLS 3
+#define K_NET k_net_production_rates
+#define K_FUSED k_fused_step
+#endif
+
 namespace {
 
 int grid_for(int64_t n) {
@@ -14,9 +78,10 @@ int grid_for(int64_t n) {
 
 constexpr size_t smem_cols(int q) { return (size_t)q * NS * BLOCK * 8; }
 
-// Opt a kernel into more than 48 KB of dynamic shared memory when needed.
+// Opt a kernel into more than 48 KB of shared memory (dynamic plus the
+// static exp table) when needed.
 int prepare_smem(const void* fn, size_t bytes) {
-  if (bytes > 48 * 1024) {
+  if (bytes + PYRO_STATIC_SMEM > 48 * 1024) {
     if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)bytes) != cudaSuccess) {
       (void)cudaGetLastError();
@@ -107,11 +172,10 @@ PYRO_EXPORT int pyro_net_production_rates(const double* rho, int64_t rho_inc,
   if (n == 0) return PYRO_OK;
   if (!rho || !T || !Y || !wdot || ldy < n || ldw < n)
     return PYRO_ERR_ARGUMENT;
-  const size_t sm = smem_cols(3);
-  if (prepare_smem((const void*)k_net_production_rates, sm) != PYRO_OK)
-    return PYRO_ERR_LAUNCH;
-  k_net_production_rates<<<grid_for(n), BLOCK, sm, stream>>>(
-      rho, rho_inc, T, t_inc, Y, ldy, wdot, ldw, n);
+  const size_t sm = smem_cols(HOT_COLS);
+  if (prepare_smem((const void*)K_NET, sm) != PYRO_OK) return PYRO_ERR_LAUNCH;
+  K_NET<<<grid_for(n), BLOCK, sm, stream>>>(rho, rho_inc, T, t_inc, Y, ldy,
+                                            wdot, ldw, n);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
@@ -163,10 +227,10 @@ PYRO_EXPORT int pyro_fused_step(const double* p, int64_t p_inc,
   if (!p || !T || !Y || !target || !t0 || !wdot || !T_out || ldy < n ||
       ldw < n)
     return PYRO_ERR_ARGUMENT;
-  const size_t sm = smem_cols(3);
-  if (prepare_smem((const void*)k_fused_step, sm) != PYRO_OK)
+  const size_t sm = smem_cols(HOT_COLS);
+  if (prepare_smem((const void*)K_FUSED, sm) != PYRO_OK)
     return PYRO_ERR_LAUNCH;
-  k_fused_step<<<grid_for(n), BLOCK, sm, stream>>>(
+  K_FUSED<<<grid_for(n), BLOCK, sm, stream>>>(
       p, p_inc, T, t_inc, Y, ldy, target, target_inc, t0, t0_inc, do_energy,
       tol, max_iter, wdot, ldw, T_out, fail_count, n);
   PYRO_CHECK_LAUNCH();

@@ -1,0 +1,56 @@
+// Table-driven double-precision exponential for FP64-bound kernels.
+//
+// Method: P. T. P. Tang, "Table-driven implementation of the exponential
+// function in IEEE floating-point arithmetic", ACM TOMS 15(2), 1989, with a
+// larger table so the polynomial is short:
+//
+//   x = (2048 m + j) ln2/2048 + r,   |r| <= ln2/4096,
+//   exp(x) = 2^m * 2^(j/2048) * exp(r),
+//   exp(r) - 1 ~= r + r^2/2 + r^3/6   (truncation < 0.15 ulp at |r| max).
+//
+// k = round(x 2048/ln2) comes from adding 1.5 * 2^52 (its low word is k);
+// r uses a two-constant Cody-Waite split of ln2/2048 whose leading part has
+// 32 significant bits, so k * L1 is exact for |x| < 708.  The 2^(j/2048)
+// values (correctly rounded, exp_table.cuh) are staged in shared memory once
+// per block.  Cost: 8 FP64 instructions per call (CUDA's exp costs about
+// 20 DFMA-equivalents on GB300's FP64 pipe).  |x| >= 708, inf and nan go to
+// CUDA's exp, which handles overflow, gradual underflow and specials.
+#pragma once
+
+#include "exp_table.cuh"
+
+__shared__ double pyro_exp_smem[PYRO_EXP_N];
+
+// Every kernel that calls pyro_exp stages the table first.
+#define PYRO_EXP_PRELOAD()                                              \
+  do {                                                                  \
+    for (int q_ = threadIdx.x; q_ < PYRO_EXP_N; q_ += blockDim.x)       \
+      pyro_exp_smem[q_] = pyro_exp_table[q_];                           \
+    __syncthreads();                                                    \
+  } while (0)
+
+// The table method alone, valid for |x| < 708 (no range check).
+__device__ __forceinline__ double pyro_exp_core(double x) {
+  const double s = fma(x, PYRO_EXP_INV_L, 0x1.8p52);
+  const double kd = s - 0x1.8p52;
+  const int k = __double2loint(s);
+  double r = fma(-kd, PYRO_EXP_L1, x);
+  r = fma(-kd, PYRO_EXP_L2, r);
+  const double p = fma(r * r, fma(r, 1.0 / 6.0, 0.5), r);
+  const double t = pyro_exp_smem[k & (PYRO_EXP_N - 1)];
+  const double v = fma(t, p, t);
+  const unsigned m = (unsigned)(k >> 11);
+  return __hiloint2double(__double2hiint(v) + (int)(m << 20),
+                          __double2loint(v));
+}
+
+__device__ __forceinline__ double pyro_exp(double x) {
+  const int hx = __double2hiint(x) & 0x7fffffff;
+  if (hx >= 0x40862000) return exp(x);  // |x| >= 708, inf, nan
+  return pyro_exp_core(x);
+}
+
+// 10^x as exp(x ln 10) (the reference evaluates 10**x with numpy's power).
+__device__ __forceinline__ double pyro_exp10(double x) {
+  return pyro_exp(x * 2.302585092994045684);
+}

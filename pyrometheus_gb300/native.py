@@ -25,7 +25,15 @@ def build_peaks() -> str:
     return _build("peaks.cu", "peaks")
 
 
-BUILDERS = [build_peaks]
+def build_mathcheck() -> str:
+    return _build("mathcheck.cu", "mathcheck")
+
+
+def build_runtime() -> str:
+    return _build("runtime.cu", "runtime")
+
+
+BUILDERS = [build_peaks, build_mathcheck, build_runtime]
 
 
 @lru_cache(maxsize=None)
@@ -53,3 +61,43 @@ def measure_fp64(scratch, repeats: int = 3):
     if st != 0:
         raise RuntimeError(f"pyro_measure_fp64 failed (status {st})")
     return res[0], res[1], res[2]
+
+
+@lru_cache(maxsize=None)
+def mathcheck_lib() -> ctypes.CDLL:
+    lib = ctypes.CDLL(build_mathcheck())
+    lib.pyro_exp_check.restype = ctypes.c_int
+    lib.pyro_exp_check.argtypes = [ctypes.c_void_p] * 3 + [
+        ctypes.c_int, ctypes.c_int64, ctypes.c_void_p]
+    return lib
+
+
+@lru_cache(maxsize=None)
+def runtime_lib() -> ctypes.CDLL:
+    lib = ctypes.CDLL(build_runtime())
+    lib.pyro_memcpy2d_async.restype = ctypes.c_int
+    lib.pyro_memcpy2d_async.argtypes = [
+        ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p, ctypes.c_int64,
+        ctypes.c_int64, ctypes.c_int64, ctypes.c_void_p]
+    return lib
+
+
+def copy_columns_async(dst, src, col0_dst: int, col0_src: int, ncols: int,
+                       stream) -> None:
+    """Copy columns [col0_src, col0_src + ncols) of the 2-D (or 1-D)
+    float64 tensor *src* into columns starting at *col0_dst* of *dst* (host
+    or device, row-major, unit column stride) with one pitched DMA."""
+    if src.dim() == 1:
+        src2, dst2 = src.view(1, -1), dst.view(1, -1)
+    else:
+        src2, dst2 = src, dst
+    rows = src2.shape[0]
+    es = src2.element_size()
+    st = runtime_lib().pyro_memcpy2d_async(
+        ctypes.c_void_p(dst2.data_ptr() + col0_dst * es),
+        dst2.stride(0) * es,
+        ctypes.c_void_p(src2.data_ptr() + col0_src * es),
+        src2.stride(0) * es, ncols * es, rows,
+        ctypes.c_void_p(stream.cuda_stream))
+    if st != 0:
+        raise RuntimeError(f"pyro_memcpy2d_async failed (status {st})")

@@ -7,11 +7,14 @@ counts, for a mechanism, the FP64 operations the formulation of
 arithmetic as 1 flop, FMA as 2, division as 1 -- and, separately, the
 transcendental calls (``exp``, ``log``, ``log10``, ``exp10``, ``pow``).
 
-A transcendental is charged the FP64 work CUDA's double-precision libm
-spends on it, measured on the GPU by the benchmark's microbenchmark
-(``flops per exp = DFMA FLOP/s / exp/s``), so that
-``algorithmic flops / kernel time / DFMA peak`` reads as the fraction of the
-FP64 pipe doing the algorithm's work.
+A transcendental is charged the FP64 flops of the implementation the
+kernels use: the table-driven exponential (14 flops per call, see
+``csrc/pyro_math.cuh``) and, for ``log``/``log10``, CUDA's libm at the
+FP64-pipe cost the benchmark measures (``DFMA FLOP/s / log/s``).  Then
+``algorithmic flops / kernel time / DFMA peak`` is the fraction of the FP64
+pipe's FMA throughput doing the algorithm's work (additions and
+multiplications count one flop for a full pipe slot, so a perfectly busy
+pipe reads below 1 unless the work is all FMAs).
 """
 
 from __future__ import annotations
@@ -137,6 +140,22 @@ def libm_weights(dfma_flops: float, exp_rate: float, log_rate: float
     w_log = dfma_flops / log_rate
     return {"exp": w_exp, "exp10": w_exp, "log": w_log, "log10": w_log,
             "pow": w_exp + w_log}
+
+
+#: FP64 flops of one call of the table-driven exponential
+#: (csrc/pyro_math.cuh): 6 FMAs, one add, one multiply.
+TANG_EXP_FLOPS = 14.0
+
+
+def kernel_weights(dfma_flops: float, log_rate: float) -> Dict[str, float]:
+    """Flops charged per transcendental as the kernels evaluate them:
+    ``exp`` and ``10^x`` by the table method (14 flops, +1 for the ln 10
+    scaling), ``log``/``log10``/``pow`` by CUDA's libm at its measured
+    FP64-pipe cost."""
+    w_log = dfma_flops / log_rate
+    return {"exp": TANG_EXP_FLOPS, "exp10": TANG_EXP_FLOPS + 1.0,
+            "log": w_log, "log10": w_log + 1.0,
+            "pow": w_log + TANG_EXP_FLOPS}
 
 
 def bytes_per_state(sol) -> int:

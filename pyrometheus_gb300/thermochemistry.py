@@ -435,13 +435,25 @@ class CudaThermochemistryBase:
 
     def get_net_production_rates_and_temperature(
             self, pressure, temperature, mass_fractions, energy, t_guess,
-            do_energy=True, check=True):
+            do_energy=True, check=True, out=None, chunk=1 << 19):
         """One pass per state of ``rho = get_density(p, T, Y)``,
         ``get_net_production_rates(rho, T, Y)`` and
         ``get_temperature(energy, t_guess, Y, do_energy)``.
 
-        :returns: ``(wdot[S, N], T_new[N])``.
+        With host (CPU, preferably pinned) torch tensors for ``pressure``,
+        ``temperature``, ``energy`` ([N]) and ``mass_fractions`` ([S, N]) and
+        ``out = (wdot_host[S, N], T_host[N])``, the batch is streamed in
+        chunks of *chunk* states: host-to-device copies, the kernel and
+        device-to-host copies of successive chunks run on three streams
+        with double-buffered device chunks, so the transfers overlap the
+        FP64 work.  Results land in *out*.
+
+        :returns: ``(wdot[S, N], T_new[N])`` (the *out* tensors when given).
         """
+        if out is not None:
+            return self._fused_streamed(pressure, temperature, mass_fractions,
+                                        energy, t_guess, do_energy, check,
+                                        out, chunk)
         ym, ny, single = self._species_mat(mass_fractions, self.num_species)
         pv = self._scalar_vec(pressure)
         tv = self._scalar_vec(temperature)
@@ -460,6 +472,79 @@ class CudaThermochemistryBase:
         if check and int(self._fail.item()) > 0:
             raise RuntimeError("Temperature iteration failed to converge")
         return wdot, tout
+
+    def _fused_streamed(self, p, t, y, e, t_guess, do_energy, check, out,
+                        chunk):
+        from . import native
+        host = [x for x in (p, t, y, e)]
+        if not all(isinstance(x, torch.Tensor) and x.device.type == "cpu"
+                   and x.dtype == torch.float64 for x in host):
+            raise ValueError("streamed fused step: p, T, Y, e must be CPU "
+                             "float64 tensors")
+        out_w, out_t = out
+        S = self.num_species
+        n = int(y.shape[1])
+        if y.shape[0] != S or out_w.shape != (S, n) or out_t.shape != (n,):
+            raise ValueError("streamed fused step: shape mismatch")
+        for x in (p, t, e, out_t):
+            if x.shape != (n,) or x.stride(0) != 1:
+                raise ValueError("streamed fused step: [N] inputs must be "
+                                 "contiguous")
+        if y.stride(1) != 1 or out_w.stride(1) != 1:
+            raise ValueError("streamed fused step: [S, N] arrays must have "
+                             "unit column stride")
+        if n == 0:
+            return out_w, out_t
+        tg = self._scalar_vec(t_guess)
+        if tg.n != 1:
+            raise ValueError("streamed fused step: t_guess must be a scalar")
+        dev = self.device
+        comp = torch.cuda.current_stream(dev)
+        if getattr(self, "_copy_streams", None) is None:
+            self._copy_streams = (torch.cuda.Stream(dev),
+                                  torch.cuda.Stream(dev))
+        h2d, d2h = self._copy_streams
+        m0 = int(min(chunk, n))
+        f64 = dict(dtype=torch.float64, device=dev)
+        bufs = []
+        for _ in range(2):
+            b = {"p": torch.empty(m0, **f64), "t": torch.empty(m0, **f64),
+                 "e": torch.empty(m0, **f64), "y": torch.empty((S, m0), **f64),
+                 "w": torch.empty((S, m0), **f64),
+                 "to": torch.empty(m0, **f64)}
+            for v in list(b.values()):
+                v.record_stream(h2d)
+                v.record_stream(d2h)
+            b["ready"] = torch.cuda.Event()
+            b["done"] = torch.cuda.Event()
+            b["free"] = torch.cuda.Event()
+            bufs.append(b)
+        self._fail.zero_()
+        h2d.wait_stream(comp)
+        for c, s0 in enumerate(range(0, n, m0)):
+            m = min(m0, n - s0)
+            b = bufs[c % 2]
+            if c >= 2:
+                h2d.wait_event(b["free"])
+            for key, src in (("p", p), ("t", t), ("e", e), ("y", y)):
+                native.copy_columns_async(b[key], src, 0, s0, m, h2d)
+            b["ready"].record(h2d)
+            comp.wait_event(b["ready"])
+            _check(self._lib.pyro_fused_step(
+                b["p"].data_ptr(), 1, b["t"].data_ptr(), 1,
+                b["y"].data_ptr(), m0, b["e"].data_ptr(), 1, tg.ptr, tg.inc,
+                1 if do_energy else 0, 1.0e-6, 500, b["w"].data_ptr(), m0,
+                b["to"].data_ptr(), self._fail.data_ptr(), m,
+                ctypes.c_void_p(comp.cuda_stream)), "fused step")
+            b["done"].record(comp)
+            d2h.wait_event(b["done"])
+            native.copy_columns_async(out_w, b["w"], s0, 0, m, d2h)
+            native.copy_columns_async(out_t, b["to"], s0, 0, m, d2h)
+            b["free"].record(d2h)
+        comp.wait_stream(d2h)
+        if check and int(self._fail.item()) > 0:
+            raise RuntimeError("Temperature iteration failed to converge")
+        return out_w, out_t
 
     # }}}
 
