@@ -554,3 +554,59 @@ def reference_class(sol, name: str = "Thermochemistry"):
 # }}}
 
 # vim: foldmethod=marker
+
+
+# {{{ jax stand-in for the reference's block-Thomas
+
+def _scan(f, init, xs):
+    """``jax.lax.scan`` over the leading axis of a tuple of arrays."""
+    leaves = xs if isinstance(xs, tuple) else (xs,)
+    n = leaves[0].shape[0]
+    if n == 0:
+        # empty scan: outputs shaped like the carry (as in the reference's
+        # two scans), with a zero-length leading axis
+        if isinstance(init, tuple):
+            return init, tuple(np.empty((0,) + np.shape(c)) for c in init)
+        return init, np.empty((0,) + np.shape(init))
+    carry = init
+    outs = []
+    for i in range(n):
+        item = tuple(x[i] for x in leaves) if isinstance(xs, tuple) \
+            else leaves[0][i]
+        carry, y = f(carry, item)
+        outs.append(y)
+    if outs and isinstance(outs[0], tuple):
+        stacked = tuple(np.stack([o[k] for o in outs])
+                        for k in range(len(outs[0])))
+    else:
+        stacked = np.stack(outs) if outs else None
+    return carry, stacked
+
+
+def reference_block_thomas():
+    """The reference's ``flamelets.linear_solver.block_thomas`` with
+    ``jax``/``jax.numpy`` mapped to a numpy ``lax.scan`` and numpy."""
+    if not reference_available():
+        raise RuntimeError("reference checkout not found")
+    jax = types.ModuleType("jax")
+    lax = types.ModuleType("jax.lax")
+    lax.scan = _scan
+    jax.lax = lax
+    jax.numpy = np
+    path = os.path.join(REFERENCE_ROOT, "pyrometheus", "flamelets",
+                        "linear_solver.py")
+    saved = {k: sys.modules.get(k) for k in ("jax", "jax.numpy", "jax.lax")}
+    try:
+        sys.modules.update({"jax": jax, "jax.numpy": np, "jax.lax": lax})
+        ns = {"__name__": "reference_linear_solver"}
+        with open(path) as f:
+            exec(compile(f.read(), path, "exec"), ns)
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    return ns["block_thomas"]
+
+# }}}

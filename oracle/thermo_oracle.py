@@ -408,16 +408,21 @@ class Thermochemistry:
         ydot = self.tab.W[:, None] * w / rho
         return np.concatenate([tdot[None, :], ydot], axis=0)
 
-    def reactor_jacobian_fd(self, p, t, y, rel=1e-7):
-        """Central differences of :meth:`reactor_source` w.r.t. ``(T, Y)``
-        with step ``rel * max(|x|, 1e-10)``; ``[N, S+1, S+1]``."""
+    def reactor_jacobian_fd(self, p, t, y, rel=1e-7, absolute_y=False):
+        """Central differences of :meth:`reactor_source` w.r.t. ``(T, Y)``;
+        ``[N, S+1, S+1]``.  Steps: ``rel * T`` for T; ``rel * max(|Y|,
+        1e-10)`` for Y, or ``rel`` itself with *absolute_y* (the
+        reference's mass-fraction steps, ``test/test.py:349-356``)."""
         t = np.atleast_1d(np.asarray(t, dtype=np.float64))
         y = np.asarray(y, dtype=np.float64).reshape(self.tab.S, -1)
         x = np.concatenate([t[None, :], y], axis=0)
         n1, n = x.shape
         jac = np.empty((n, n1, n1))
         for i in range(n1):
-            h = rel * np.maximum(np.abs(x[i]), 1e-10)
+            if absolute_y and i > 0:
+                h = np.full(n, float(rel))
+            else:
+                h = rel * np.maximum(np.abs(x[i]), 1e-10)
             xp, xm = x.copy(), x.copy()
             xp[i] += h
             xm[i] -= h

@@ -67,13 +67,16 @@ class CudaGenerationOptions(CodeGenerationOptions):
     and fused-step kernels (the table-driven kernels serve every other
     method, and the rare states the fast path flags);
     ``accum_in_smem``: keep that variant's production-rate accumulators in
-    a shared-memory column instead of registers.
+    a shared-memory column instead of registers;
+    ``hot_block``: threads per block of the unrolled kernels (``None``: one
+    block per SM with about 134 KB of shared-memory columns).
     """
 
     block_size: Optional[int] = None
     blocks_per_sm: int = 8
     unrolled: bool = True
     accum_in_smem: bool = False
+    hot_block: Optional[int] = None
 
 
 # {{{ mechanism model
@@ -326,6 +329,31 @@ class _Emitter:
                         tb_de.append(e - d)
             tb_start.append(len(tb_idx))
 
+        # species -> (reaction, slot) incidences and species -> third-body
+        # entries, for the Jacobian / VJP kernels (csrc/jacobian.cuh)
+        inc: List[List[Tuple[int, int]]] = [[] for _ in range(S)]
+        for j, row in enumerate(sp_l):
+            for a in range(nr_l[j]):
+                inc[row[a]].append((j, a))
+            for a in range(np_l[j]):
+                inc[row[maxside + a]].append((j, maxside + a))
+        si_start, si_rx, si_pos = [0], [], []
+        for k in range(S):
+            for j, a in inc[k]:
+                si_rx.append(j)
+                si_pos.append(a)
+            si_start.append(len(si_rx))
+        tbinc: List[List[Tuple[int, float]]] = [[] for _ in range(S)]
+        for j in range(R):
+            for t in range(tb_start[j], tb_start[j + 1]):
+                tbinc[tb_idx[t]].append((j, tb_de[t]))
+        st_start, st_rx, st_de = [0], [], []
+        for k in range(S):
+            for j, de in tbinc[k]:
+                st_rx.append(j)
+                st_de.append(de)
+            st_start.append(len(st_rx))
+
         groups = m.tmid_groups
         grp_start, grp_sp, grp_tmid = [0], [], []
         for tmid, ks in groups:
@@ -339,7 +367,8 @@ class _Emitter:
                                            + 3 * maxside + 16 + 4 + 4 + 4)
                   + 4 * (R + 1) + max(1, len(tb_idx)) * 10
                   + max(1, nf) * (4 + 24 + 40)
-                  + max(1, len(frac)) * 24 * maxside)
+                  + max(1, len(frac)) * 24 * maxside
+                  + 8 * (S + 1) + 3 * len(si_rx) + 10 * len(st_rx) + 16)
         qual = "__constant__" if nbytes <= self.CONST_LIMIT else "__device__"
 
         L: List[str] = []
@@ -419,10 +448,30 @@ class _Emitter:
         w(_table(qual, "double", "k_frac", [max(1, len(frac)), 3 * maxside],
                  ["{" + ", ".join(_dlit(v) for v in row) + "}"
                   for row in (frac or [[0.0] * (3 * maxside)])]))
+        w("// species -> reaction slots; species -> third-body entries")
+        w(_table(qual, "int", "k_si_start", [S + 1],
+                 [_cint(v) for v in si_start]))
+        w(_table(qual, "short", "k_si_rx", [max(1, len(si_rx))],
+                 [_cint(v) for v in (si_rx or [0])]))
+        w(_table(qual, "signed char", "k_si_pos", [max(1, len(si_pos))],
+                 [_cint(v) for v in (si_pos or [0])]))
+        w(_table(qual, "int", "k_st_start", [S + 1],
+                 [_cint(v) for v in st_start]))
+        w(_table(qual, "short", "k_st_rx", [max(1, len(st_rx))],
+                 [_cint(v) for v in (st_rx or [0])]))
+        w(_table(qual, "double", "k_st_de", [max(1, len(st_de))],
+                 [_hexd(v) for v in (st_de or [0.0])]))
+        jw = S * S + 5 * R + 10 * S
+        jwarps = max(1, min(8, (227 * 1024 - 16384) // (8 * jw)))
+        w(f"#define JWARPS {jwarps}")
+        vblock = max(32, min(128, (100 * 1024 // (5 * S * 8)) // 32 * 32))
+        w(f"#define VBLOCK {vblock}")
         w("")
         w('#include "kinetics.cuh"')
+        w('#include "jacobian.cuh"')
         if self.opts.unrolled:
-            L.extend(_UnrolledEmitter(m, self.opts.accum_in_smem).render())
+            L.extend(_UnrolledEmitter(m, self.opts.accum_in_smem,
+                                      self.opts.hot_block).render())
         w('#include "kinetics_abi.cuh"')
         return "\n".join(L) + "\n"
 
@@ -440,9 +489,12 @@ class _UnrolledEmitter:
     the table-driven path on thread-private arrays.
     """
 
-    def __init__(self, m: _Model, accum_in_smem: bool = False):
+    def __init__(self, m: _Model, accum_in_smem: bool = False,
+                 hot_block: Optional[int] = None):
         self.m = m
         self.acc_smem = accum_in_smem
+        self.hot_block = int(hot_block) if hot_block else \
+            _default_hot_block(m.S, 3 if accum_in_smem else 2)
         self.L: List[str] = []
 
     def W(self, k):
@@ -596,6 +648,7 @@ class _UnrolledEmitter:
         w("// ---- unrolled hot path (generated) ----")
         w("#define PYRO_UNROLLED 1")
         w(f"#define PYRO_HOT_COLS {3 if self.acc_smem else 2}")
+        w(f"#define HOT_BLOCK {self.hot_block}")
         w("namespace pyro_unrolled {")
         w("")
         w("// exp on a sanitised argument: out-of-range lanes set *bad* and")
@@ -606,9 +659,10 @@ class _UnrolledEmitter:
         w("  return pyro_exp_core(out ? 0.0 : x);")
         w("}")
         w("")
+        w("using HCols = pyro::ColsT<HOT_BLOCK>;")
         w("__device__ __forceinline__ void net_rates(double T, double rho, "
           "const double* __restrict__ Y, int64_t ldy, int64_t i, "
-          "pyro::Cols c, pyro::Cols g, pyro::Cols w, double (&wd)[NS]) {")
+          "HCols c, HCols g, HCols w, double (&wd)[NS]) {")
         w("  const double lnT = log(T);")
         w("  const double invT = 1.0 / T;")
         w("  const double c0 = LOG_P0_OVER_R - lnT;")
@@ -639,6 +693,15 @@ class _UnrolledEmitter:
         w("")
         w("}  // namespace pyro_unrolled")
         return self.L
+
+
+def _default_hot_block(n_species: int, cols: int) -> int:
+    """Threads per block of the unrolled hot kernels: one block per SM
+    whose shared-memory columns use about 134 KB (the rest of the SM's
+    228 KB stays L1 for the accumulators' register spills), 32..256."""
+    per_thread = cols * n_species * 8
+    b = (134 * 1024 // max(per_thread, 1)) // 32 * 32
+    return int(max(32, min(256, b)))
 
 
 def _default_block(n_species: int) -> int:

@@ -1,0 +1,314 @@
+// Batched block-Thomas solver for block-tridiagonal systems of uneven
+// lengths (FP64, sm_103a): the flamelet Newton/time-step linear solve
+// (pyrometheus/flamelets/linear_solver.py:6-103).
+//
+// For one system with diagonal blocks C_i (i < N), sub-diagonal L_i and
+// super-diagonal U_i (i < N-1), right-hand side b_i:
+//
+//   forward:  C'_0 = C_0, b'_0 = b_0,
+//             S_i = C'_i^-1 U_i,  t_i = C'_i^-1 b'_i,
+//             C'_{i+1} = C_{i+1} - L_i S_i,  b'_{i+1} = b_{i+1} - L_i t_i
+//   backward: x_{N-1} = t_{N-1},  x_i = t_i - S_i x_{i+1}
+//
+// which is the reference's recurrence (its backward step re-solves with
+// C'_i; here the factor is used once and S_i, t_i are kept).  Each C'_i is
+// LU-factorised with partial pivoting, like the LAPACK getrf behind
+// jnp.linalg.solve.
+//
+// Work split: one CTA per system, the working blocks (C', L, U -> S and the
+// previous S) in shared memory, threads parallel over matrix elements /
+// right-hand-side columns; a persistent grid takes systems from an atomic
+// counter in longest-first order (LPT), so uneven lengths balance across
+// SMs in one launch.  Layout (packed, row-major blocks): system s owns rows
+// [row_off[s], row_off[s+1]) of C[rows][nv][nv], L, U (the last row's L/U
+// unused), b[rows][nv], x[rows][nv]; work holds S_i and t_i,
+// rows * (nv*nv + nv) doubles.  No waits on other CTAs; the counter is reset
+// by the host before each launch.
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "pyro_common.cuh"
+
+namespace {
+
+struct BTSmem {
+  double* A;   // C'_i, then its LU factors (nv x ld)
+  double* R;   // right-hand sides: U_i | b'_i  -> S_i | t_i (nv x ld)
+  double* Lb;  // L_{i-1}
+  double* P;   // previous S | t (nv x ld)
+  int* piv;
+  int* sys;
+  int ld;      // nv + 1 (last column holds the vector)
+};
+
+__device__ __forceinline__ void load_block(double* dst, int ld,
+                                           const double* __restrict__ src,
+                                           int nv) {
+  for (int e = threadIdx.x; e < nv * nv; e += blockDim.x) {
+    const int i = e / nv, j = e - (e / nv) * nv;
+    dst[i * ld + j] = __ldg(src + e);
+  }
+}
+
+// In-place LU with partial pivoting of A (nv x nv); piv[k] = row swapped
+// with k.  Returns through *singular (shared) when a pivot is zero.
+__device__ void lu_factor(double* A, int ld, int nv, int* piv,
+                          int* singular) {
+  __shared__ double red_v[32];
+  __shared__ int red_i[32];
+  for (int k = 0; k < nv; ++k) {
+    // argmax |A[i][k]|, i >= k (first warp)
+    if (threadIdx.x < 32) {
+      double best = -1.0;
+      int bi = k;
+      for (int i = k + threadIdx.x; i < nv; i += 32) {
+        const double v = fabs(A[i * ld + k]);
+        if (v > best) {
+          best = v;
+          bi = i;
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const double ov = __shfl_xor_sync(0xffffffffu, best, o);
+        const int oi = __shfl_xor_sync(0xffffffffu, bi, o);
+        if (ov > best || (ov == best && oi < bi)) {
+          best = ov;
+          bi = oi;
+        }
+      }
+      if (threadIdx.x == 0) {
+        red_v[0] = best;
+        red_i[0] = bi;
+        piv[k] = bi;
+        if (best == 0.0) *singular = 1;
+      }
+    }
+    __syncthreads();
+    const int p = red_i[0];
+    if (p != k) {
+      for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+        const double t = A[k * ld + j];
+        A[k * ld + j] = A[p * ld + j];
+        A[p * ld + j] = t;
+      }
+      __syncthreads();
+    }
+    const double inv = 1.0 / A[k * ld + k];
+    for (int i = k + 1 + threadIdx.x; i < nv; i += blockDim.x)
+      A[i * ld + k] *= inv;
+    __syncthreads();
+    const int m = nv - k - 1;
+    for (int e = threadIdx.x; e < m * m; e += blockDim.x) {
+      const int i = k + 1 + e / m, j = k + 1 + (e - (e / m) * m);
+      A[i * ld + j] = fma(-A[i * ld + k], A[k * ld + j], A[i * ld + j]);
+    }
+    __syncthreads();
+  }
+}
+
+// Solve A X = R for ncol right-hand-side columns of R (in place) with the
+// factors and pivots of lu_factor.
+__device__ void lu_solve(const double* A, double* R, int ld, int nv,
+                         int ncol, int col0, const int* piv) {
+  // row permutation
+  if (threadIdx.x < 32) {
+    for (int k = 0; k < nv; ++k) {
+      const int p = piv[k];
+      if (p != k)
+        for (int c = col0 + threadIdx.x; c < col0 + ncol; c += 32) {
+          const double t = R[k * ld + c];
+          R[k * ld + c] = R[p * ld + c];
+          R[p * ld + c] = t;
+        }
+      __syncwarp();
+    }
+  }
+  __syncthreads();
+  // forward, unit lower
+  for (int k = 0; k < nv - 1; ++k) {
+    const int m = nv - k - 1;
+    for (int e = threadIdx.x; e < m * ncol; e += blockDim.x) {
+      const int i = k + 1 + e / ncol, c = col0 + (e - (e / ncol) * ncol);
+      R[i * ld + c] = fma(-A[i * ld + k], R[k * ld + c], R[i * ld + c]);
+    }
+    __syncthreads();
+  }
+  // backward, upper
+  for (int k = nv - 1; k >= 0; --k) {
+    const double inv = 1.0 / A[k * ld + k];
+    for (int c = col0 + threadIdx.x; c < col0 + ncol; c += blockDim.x)
+      R[k * ld + c] *= inv;
+    __syncthreads();
+    for (int e = threadIdx.x; e < k * ncol; e += blockDim.x) {
+      const int i = e / ncol, c = col0 + (e - (e / ncol) * ncol);
+      R[i * ld + c] = fma(-A[i * ld + k], R[k * ld + c], R[i * ld + c]);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void k_block_thomas(const double* __restrict__ Lm,
+                               const double* __restrict__ Cm,
+                               const double* __restrict__ Um,
+                               const double* __restrict__ B,
+                               double* __restrict__ X,
+                               const int64_t* __restrict__ row_off,
+                               const int* __restrict__ order, int nsys,
+                               int nv, double* __restrict__ work,
+                               int* __restrict__ counter,
+                               int* __restrict__ status) {
+  extern __shared__ double smem[];
+  const int ld = nv + 1;
+  double* A = smem;
+  double* R = A + nv * ld;
+  double* Lb = R + nv * ld;
+  double* P = Lb + nv * ld;
+  int* piv = (int*)(P + nv * ld);
+  __shared__ int s_sys;
+  __shared__ int s_sing;
+  const int64_t wrow = (int64_t)nv * nv + nv;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_sys = atomicAdd(counter, 1);
+      s_sing = 0;
+    }
+    __syncthreads();
+    const int q = s_sys;
+    if (q >= nsys) break;
+    const int s = order[q];
+    const int64_t r0 = row_off[s];
+    const int N = (int)(row_off[s + 1] - r0);
+    for (int i = 0; i < N; ++i) {
+      const int64_t row = r0 + i;
+      load_block(A, ld, Cm + row * nv * nv, nv);
+      for (int j = threadIdx.x; j < nv; j += blockDim.x)
+        A[j * ld + nv] = __ldg(B + row * nv + j);  // b in column nv of A
+      if (i > 0) load_block(Lb, ld, Lm + (row - 1) * nv * nv, nv);
+      __syncthreads();
+      if (i > 0) {
+        // C' = C - L S_prev ; b' = b - L t_prev (t_prev in column nv of P)
+        for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) {
+          const int r = e / ld, c = e - (e / ld) * ld;
+          double acc = A[r * ld + c];
+          for (int k = 0; k < nv; ++k)
+            acc = fma(-Lb[r * ld + k], P[k * ld + c], acc);
+          A[r * ld + c] = acc;
+        }
+        __syncthreads();
+      }
+      // right-hand sides: U_i (if any) and b'_i
+      const bool has_u = i < N - 1;
+      if (has_u) load_block(R, ld, Um + row * nv * nv, nv);
+      for (int j = threadIdx.x; j < nv; j += blockDim.x)
+        R[j * ld + nv] = A[j * ld + nv];
+      __syncthreads();
+      lu_factor(A, ld, nv, piv, &s_sing);
+      if (has_u)
+        lu_solve(A, R, ld, nv, nv + 1, 0, piv);
+      else
+        lu_solve(A, R, ld, nv, 1, nv, piv);
+      // keep S_i | t_i for the backward sweep and as the next P
+      double* w = work + row * wrow;
+      for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) {
+        const int r = e / ld, c = e - (e / ld) * ld;
+        const double v = R[e];
+        P[e] = v;
+        if (c < nv) {
+          if (has_u) w[r * nv + c] = v;
+        } else {
+          w[nv * nv + r] = v;
+        }
+      }
+      __syncthreads();
+    }
+    // backward sweep: x_{N-1} = t_{N-1}; x_i = t_i - S_i x_{i+1}
+    // (x_{i+1} and x_i alternate between two rows of R)
+    double* xs = R;
+    double* xn = R + ld;
+    {
+      const int64_t row = r0 + N - 1;
+      for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+        const double v = P[j * ld + nv];
+        X[row * nv + j] = v;
+        xs[j] = v;
+      }
+      __syncthreads();
+    }
+    for (int i = N - 2; i >= 0; --i) {
+      const int64_t row = r0 + i;
+      const double* w = work + row * wrow;
+      for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+        double v = w[nv * nv + j];
+        for (int k = 0; k < nv; ++k) v = fma(-w[j * nv + k], xs[k], v);
+        xn[j] = v;
+        X[row * nv + j] = v;
+      }
+      __syncthreads();
+      double* t = xs;
+      xs = xn;
+      xn = t;
+    }
+    if (threadIdx.x == 0 && s_sing && status) atomicOr(status, 1);
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+// Doubles of workspace pyro_block_thomas needs for `rows` packed rows.
+PYRO_EXPORT int64_t pyro_block_thomas_work_doubles(int nv, int64_t rows) {
+  return rows * ((int64_t)nv * nv + nv);
+}
+
+// Shared memory of one CTA for block size nv.
+PYRO_EXPORT int64_t pyro_block_thomas_smem_bytes(int nv) {
+  return (int64_t)4 * nv * (nv + 1) * 8 + (int64_t)nv * 4;
+}
+
+// Solve nsys block-tridiagonal systems (packed as described above).
+// order: a permutation of 0..nsys-1 (longest first balances best); counter
+// and status: device ints (counter is zeroed here, status gets bit 0 set
+// for a zero pivot); threads: CTA size (multiple of 32, <= 1024); ctas:
+// grid size (0: as many as fit, resident).  Asynchronous on `stream`.
+PYRO_EXPORT int pyro_block_thomas(const double* L, const double* C,
+                                  const double* U, const double* b, double* x,
+                                  const int64_t* row_off, const int* order,
+                                  int nsys, int nv, double* work, int* counter,
+                                  int* status, int threads, int ctas,
+                                  cudaStream_t stream) {
+  if (nsys < 0 || nv < 1 || nv > 64 || threads < 32 || threads > 1024 ||
+      threads % 32)
+    return PYRO_ERR_ARGUMENT;
+  if (nsys == 0) return PYRO_OK;
+  if (!L || !C || !U || !b || !x || !row_off || !order || !work || !counter)
+    return PYRO_ERR_ARGUMENT;
+  const size_t smem = (size_t)pyro_block_thomas_smem_bytes(nv);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute((const void*)k_block_thomas,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  if (ctas <= 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_block_thomas, threads, smem) != cudaSuccess ||
+        per_sm < 1) {
+      (void)cudaGetLastError();
+      per_sm = 1;
+    }
+    ctas = per_sm * pyro_sm_count();
+  }
+  if (ctas > nsys) ctas = nsys;
+  if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  k_block_thomas<<<ctas, threads, smem, stream>>>(L, C, U, b, x, row_off,
+                                                  order, nsys, nv, work,
+                                                  counter, status);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}

@@ -1,0 +1,619 @@
+// Analytic Jacobian and vector-Jacobian product of the adiabatic
+// constant-pressure reactor source (FP64, sm_103a).
+//
+// State x = (T, Y_1..Y_S), source f = (dT/dt, dY_1/dt..dY_S/dt):
+//   rho = p / (R T sigma),  sigma = sum_k Y_k / W_k,  c_k = rho Y_k / W_k,
+//   dY_k/dt = W_k w_k / rho,
+//   dT/dt   = -Q / (rho cp),  Q = sum_k H_k w_k,  H_k = R T (h/RT)_k,
+//   cp = R sum_k (Y_k/W_k) (cp/R)_k,
+// with w_k the net production rates (python.py:486-495).  This is the
+// right-hand side the reference differentiates with jax.jacfwd for its
+// reactors and flamelets (examples/free_flame/reactors.py:115-125,
+// flamelets/equations.py:124-129, 361-389); here the derivative is written
+// out by hand:
+//
+//   per reaction:  q = kf prod c^o' - kr prod c^nu'',  with dq/dT at fixed c
+//   (Arrhenius exponent derivatives b/T + Ta/T^2, d log K/dT =
+//   (dnu - sum nu'' h/RT + sum nu' h/RT) / T, Troe blending through
+//   log10 Fcent(T) and log10 Pr), dq/dM (third body / falloff) and the
+//   mass-action dq/dc_m;
+//   chain rule through c(T, Y) and rho(T, Y), then the dT/dt row.
+//
+// k_reactor_jacobian: one warp per state.  The S x S block dw/dc lives in
+// shared memory; each lane owns whole columns (species m), walking the
+// reactions that contain m, so columns are accumulated without atomics.
+// The third-body default efficiency contributes a rank-1 term that is added
+// in the assembly instead of S entries per reaction.  The (S+1)^2 output is
+// written row by row, 32 consecutive doubles per warp store.
+//
+// k_reactor_vjp: one thread per state, reverse accumulation.  Each reaction
+// gets one scalar adjoint mu_r = sum_k lambda_k nu_kr, so the cost is a
+// small multiple of the production rates and J is never formed.
+#pragma once
+
+#include "kinetics.cuh"
+
+namespace pyro {
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// d(exponent)/dT of an Arrhenius record (FORM_EXP: b/T + Ta/T^2).
+__device__ __forceinline__ double darr_dT(int form, double b, double ta,
+                                          double invT) {
+  if (form == FORM_EXP) return fma(ta, invT, b) * invT;
+  if (form == FORM_CONST) return 0.0;
+  return b * invT;
+}
+
+struct RxnDeriv {
+  double q;      // net rate of progress
+  double dqdT;   // at fixed concentrations
+  double dqdM;   // w.r.t. the third-body concentration (0 if none)
+  double kf;     // forward rate coefficient ([M], falloff folded in)
+  double kr;     // reverse rate coefficient (0 if irreversible)
+};
+
+// d(prod_b c_b^e_b)/dc at position a of a reaction side.
+template <class CT>
+__device__ __forceinline__ double dprod(int j, int side, int a, int cnt,
+                                        bool frac, CT c) {
+  const int base = side ? MAXSIDE : 0;
+  double others = 1.0;
+  double ea = 1.0;
+  for (int b = 0; b < MAXSIDE; ++b) {
+    if (b >= cnt) break;
+    const double cv = c[k_rx_sp[j][base + b]];
+    double e;
+    if (side == 0)
+      e = frac ? k_frac[k_rx_frac[j]][2 * MAXSIDE + b] : (double)k_rx_ord[j][b];
+    else
+      e = frac ? k_frac[k_rx_frac[j]][MAXSIDE + b]
+               : (double)k_rx_nu[j][MAXSIDE + b];
+    if (b == a)
+      ea = e;
+    else
+      others *= ipow_or_pow(cv, e);
+  }
+  const double cm = c[k_rx_sp[j][base + a]];
+  double d;
+  if (ea == 1.0)
+    d = 1.0;
+  else if (ea == 2.0)
+    d = 2.0 * cm;
+  else
+    d = ea * pow(cm, ea - 1.0);
+  return d * others;
+}
+
+// Net rate, its temperature and third-body derivatives, and the rate
+// coefficients of reaction j.  h: column of h/RT.
+template <class CT>
+__device__ __forceinline__ RxnDeriv reaction_deriv(int j,
+                                                   const StateScalars& s,
+                                                   CT c, CT g, CT h) {
+  const double T = s.T, lnT = s.lnT, invT = s.invT;
+  const int f = k_rx_flags[j];
+  const int kind = f & RX_KIND_MASK;
+  const int form = (f >> RX_FORM_SHIFT) & 3;
+  double m = 1.0;
+  if (kind != RX_ELEMENTARY) {
+    const double d = k_rx_defeff[j];
+    m = d == 0.0 ? 0.0 : (d == 1.0 ? s.ctot : d * s.ctot);
+    for (int t = k_rx_tb[j]; t < k_rx_tb[j + 1]; ++t)
+      m = fma(k_tb_de[t], c[k_tb_idx[t]], m);
+  }
+  RxnDeriv out;
+  double x = 0.0, dlnkf = 0.0, dkfdM = 0.0, ek = 0.0;
+  bool exp_form = false;
+  if (kind == RX_FALLOFF) {
+    const int sl = k_rx_fo[j];
+    const int lform = k_fo_lowform[sl];
+    double xh, xl;
+    const double k_hi = arrhenius(form, k_rx_rate[j][0], k_rx_rate[j][1],
+                                  k_rx_rate[j][2], T, lnT, invT, xh);
+    const double k_lo = arrhenius(lform, k_fo_low[sl][0], k_fo_low[sl][1],
+                                  k_fo_low[sl][2], T, lnT, invT, xl);
+    const double dxh = darr_dT(form, k_rx_rate[j][1], k_rx_rate[j][2], invT);
+    const double dxl = darr_dT(lform, k_fo_low[sl][1], k_fo_low[sl][2], invT);
+    const double pr = m * k_lo / k_hi;
+    double blend = 1.0, dlnF_dT = 0.0, phi_x = 0.0;
+    if (f & RX_TROE) {
+      const double ln10 = 2.302585092994045684;
+      const double e3 = PEXP(T * k_fo_troe[sl][1]);
+      const double e1 = PEXP(T * k_fo_troe[sl][3]);
+      double fsum = k_fo_troe[sl][0] * e3 + k_fo_troe[sl][2] * e1;
+      double dfsum = k_fo_troe[sl][0] * k_fo_troe[sl][1] * e3 +
+                     k_fo_troe[sl][2] * k_fo_troe[sl][3] * e1;
+      if (f & RX_TROE_T2) {
+        const double e2 = PEXP(k_fo_troe[sl][4] * invT);
+        fsum += e2;
+        dfsum -= k_fo_troe[sl][4] * invT * invT * e2;
+      }
+      const double L = log10(fsum);
+      const double dL = dfsum / (fsum * ln10);
+      double fac = -1.0 / 0.14, dfac = 0.0, fx = 0.0;
+      if (pr > 0.0) {
+        const double xx = log10(pr) + (-0.4 - 0.67 * L);
+        const double nn = 0.75 - 1.27 * L;
+        const double den = nn - 0.14 * xx;
+        fac = xx / den;
+        fx = nn / (den * den);
+        const double fn = -xx / (den * den);
+        const double dxx = (dxl - dxh) / ln10 - 0.67 * dL;
+        dfac = fx * dxx + fn * (-1.27 * dL);
+      }
+      const double opf = 1.0 + fac * fac;
+      blend = PEXP10(L / opf);
+      const double dphi = dL / opf - 2.0 * L * fac / (opf * opf) * dfac;
+      dlnF_dT = ln10 * dphi;
+      phi_x = -2.0 * L * fac * fx / (opf * opf);
+    }
+    out.kf = k_hi * (blend * pr / (1.0 + pr));
+    dlnkf = dxh + dlnF_dT + (dxl - dxh) / (1.0 + pr);
+    dkfdM = blend * k_lo / (1.0 + pr) * (phi_x + 1.0 / (1.0 + pr));
+  } else {
+    ek = arrhenius(form, k_rx_rate[j][0], k_rx_rate[j][1], k_rx_rate[j][2], T,
+                   lnT, invT, x);
+    exp_form = form == FORM_EXP;
+    dlnkf = darr_dT(form, k_rx_rate[j][1], k_rx_rate[j][2], invT);
+    if (kind == RX_THREE_BODY) {
+      out.kf = ek * m;
+      dkfdM = ek;
+    } else {
+      out.kf = ek;
+    }
+  }
+  const int nr = k_rx_nr[j], np = k_rx_np[j];
+  const bool frac = (f & RX_FRACTIONAL) != 0;
+  const int fr = k_rx_frac[j];
+  double pf = 1.0;
+  for (int a = 0; a < MAXSIDE; ++a) {
+    if (a >= nr) break;
+    const double e = frac ? k_frac[fr][2 * MAXSIDE + a] : (double)k_rx_ord[j][a];
+    pf *= ipow_or_pow(c[k_rx_sp[j][a]], e);
+  }
+  out.kr = 0.0;
+  double pv = 0.0, dlnkr = 0.0, dkrdM = 0.0;
+  if (f & RX_REVERSIBLE) {
+    const double lk = log_keq(j, f, T, s.c0, g);
+    // d log K / dT = (dnu - sum nu'' h/RT + sum nu' h/RT) / T
+    double dh = 0.0, dnu = k_rx_dnu[j];
+    pv = 1.0;
+    for (int a = 0; a < MAXSIDE; ++a) {
+      if (a < np) {
+        const int k = k_rx_sp[j][MAXSIDE + a];
+        const double nu =
+            frac ? k_frac[fr][MAXSIDE + a] : (double)k_rx_nu[j][MAXSIDE + a];
+        dh = fma(nu, h[k], dh);
+        pv *= ipow_or_pow(c[k], nu);
+      }
+      if (a < nr) {
+        const double nu = frac ? k_frac[fr][a] : (double)k_rx_nu[j][a];
+        dh = fma(-nu, h[k_rx_sp[j][a]], dh);
+      }
+    }
+    const double dlk = (dnu - dh) * invT;
+    if (exp_form) {
+      const double ekr = PEXP(x + lk);
+      out.kr = kind == RX_THREE_BODY ? ekr * m : ekr;
+      dkrdM = kind == RX_THREE_BODY ? ekr : 0.0;
+    } else {
+      const double eK = PEXP(lk);
+      out.kr = out.kf * eK;
+      dkrdM = dkfdM * eK;
+    }
+    dlnkr = dlnkf + dlk;
+  }
+  out.q = out.kf * pf - out.kr * pv;
+  out.dqdT = out.kf * dlnkf * pf - out.kr * dlnkr * pv;
+  out.dqdM = dkfdM * pf - dkrdM * pv;
+  return out;
+}
+
+// Signed stoichiometric weight (-nu' for a reactant slot, +nu'' for a
+// product slot) of slot `pos` of reaction j.
+__device__ __forceinline__ double slot_nu(int j, int pos) {
+  const int f = k_rx_flags[j];
+  const bool frac = (f & RX_FRACTIONAL) != 0;
+  if (pos < MAXSIDE)
+    return -(frac ? k_frac[k_rx_frac[j]][pos] : (double)k_rx_nu[j][pos]);
+  return frac ? k_frac[k_rx_frac[j]][pos] : (double)k_rx_nu[j][pos];
+}
+
+// Per-state thermo of one species: cp/R, h/RT, g/RT, d(cp/R)/dT.
+struct SpThermo {
+  double cp, h, g, dcp;
+};
+
+__device__ __forceinline__ SpThermo species_thermo(int k, double T,
+                                                   double lnT, double invT) {
+  const Nasa a(k, T > k_tmid[k]);
+  SpThermo t;
+  t.cp = fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
+  t.h = fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
+                          a[2] * (1.0 / 3.0)),
+                  a[1] * 0.5),
+            a[0]) +
+        a[5] * invT;
+  t.g = fma(a[0], 1.0 - lnT, fma(a[5], invT, -a[6])) -
+        T * fma(T, fma(T, fma(T, a[4] * (1.0 / 20.0), a[3] * (1.0 / 12.0)),
+                       a[2] * (1.0 / 6.0)),
+                a[1] * 0.5);
+  t.dcp = fma(T, fma(T, 4.0 * a[4], 3.0 * a[3]), 2.0 * a[2]) * T + a[1];
+  return t;
+}
+
+}  // namespace pyro
+
+#ifndef JWARPS
+#define JWARPS 4
+#endif
+// doubles of shared memory per warp of the Jacobian kernel
+#define JW_DOUBLES (NS * NS + 5 * NR + 10 * NS)
+
+__global__ void __launch_bounds__(JWARPS * 32)
+    k_reactor_jacobian(const double* __restrict__ Pp, int64_t p_inc,
+                       const double* __restrict__ Tp, int64_t t_inc,
+                       const double* __restrict__ Y, int64_t ldy,
+                       double* __restrict__ J, int64_t ldj, int64_t n) {
+  extern __shared__ double smem[];
+  PEXP_PRELOAD();
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* Jc = smem + (size_t)wid * JW_DOUBLES;  // Jc[k * NS + m] = dw_k/dc_m
+  double* rq = Jc + NS * NS;
+  double* rdT = rq + NR;
+  double* rdM = rdT + NR;
+  double* rkf = rdM + NR;
+  double* rkr = rkf + NR;
+  double* sc = rkr + NR;
+  double* sg = sc + NS;
+  double* sh = sg + NS;
+  double* scp = sh + NS;
+  double* sw = scp + NS;
+  double* sjt = sw + NS;
+  double* sa = sjt + NS;
+  double* su = sa + NS;
+  double* shj = su + NS;
+  using LC = pyro::LocalCols;
+  const LC c{sc}, g{sg}, h{sh};
+  constexpr int NC = NS + 1;
+  for (int64_t i = (int64_t)blockIdx.x * JWARPS + wid; i < n;
+       i += (int64_t)gridDim.x * JWARPS) {
+    const double T = pyro_ld(Tp, t_inc, i);
+    const double P = pyro_ld(Pp, p_inc, i);
+    const double lnT = log(T), invT = 1.0 / T;
+    // species thermo, sigma, cp, dcp/dT
+    double sig = 0.0, cpp = 0.0, dcpp = 0.0;
+    for (int k = lane; k < NS; k += 32) {
+      const double wk = __ldg(Y + (int64_t)k * ldy + i) * k_inv_mw[k];
+      const pyro::SpThermo th = pyro::species_thermo(k, T, lnT, invT);
+      scp[k] = th.cp;
+      sh[k] = th.h;
+      sg[k] = th.g;
+      sig += wk;
+      cpp = fma(wk, th.cp, cpp);
+      dcpp = fma(wk, th.dcp, dcpp);
+    }
+    const double sigma = pyro::warp_sum(sig);
+    const double cpm = GAS_CONSTANT * pyro::warp_sum(cpp);
+    const double dcpm = GAS_CONSTANT * pyro::warp_sum(dcpp);
+    const double rho = P / (GAS_CONSTANT * T * sigma);
+    double ct = 0.0;
+    for (int k = lane; k < NS; k += 32) {
+      const double v = k_inv_mw[k] * rho * __ldg(Y + (int64_t)k * ldy + i);
+      sc[k] = v;
+      ct += v;
+    }
+    pyro::StateScalars s;
+    s.T = T;
+    s.lnT = lnT;
+    s.invT = invT;
+    s.c0 = LOG_P0_OVER_R - lnT;
+    s.ctot = pyro::warp_sum(ct);
+    __syncwarp();
+    // per reaction: q, dq/dT|c, dq/dM, kf, kr
+    for (int r = lane; r < NR; r += 32) {
+      const pyro::RxnDeriv d = pyro::reaction_deriv(r, s, c, g, h);
+      rq[r] = d.q;
+      rdT[r] = d.dqdT;
+      rdM[r] = d.dqdM;
+      rkf[r] = d.kf;
+      rkr[r] = d.kr;
+    }
+    for (int q = lane; q < NS * NS; q += 32) Jc[q] = 0.0;
+    __syncwarp();
+    // per species: w_k, dw_k/dT|c, rank-1 third-body vector a_k
+    for (int k = lane; k < NS; k += 32) {
+      double w = 0.0, jt = 0.0, a = 0.0;
+      for (int t = k_si_start[k]; t < k_si_start[k + 1]; ++t) {
+        const int r = k_si_rx[t];
+        const double nu = pyro::slot_nu(r, k_si_pos[t]);
+        w = fma(nu, rq[r], w);
+        jt = fma(nu, rdT[r], jt);
+        if ((k_rx_flags[r] & RX_KIND_MASK) != RX_ELEMENTARY)
+          a = fma(nu * k_rx_defeff[r], rdM[r], a);
+      }
+      sw[k] = w;
+      sjt[k] = jt;
+      sa[k] = a;
+    }
+    // columns m of dw/dc owned by lane
+    for (int m = lane; m < NS; m += 32) {
+      for (int t = k_si_start[m]; t < k_si_start[m + 1]; ++t) {
+        const int r = k_si_rx[t];
+        const int pos = k_si_pos[t];
+        const int f = k_rx_flags[r];
+        const bool frac = (f & RX_FRACTIONAL) != 0;
+        double d;
+        if (pos < MAXSIDE)
+          d = rkf[r] * pyro::dprod(r, 0, pos, k_rx_nr[r], frac, c);
+        else
+          d = -rkr[r] * pyro::dprod(r, 1, pos - MAXSIDE, k_rx_np[r], frac, c);
+        const int nr = k_rx_nr[r], np = k_rx_np[r];
+        for (int a = 0; a < MAXSIDE; ++a) {
+          if (a < nr) {
+            double& e = Jc[k_rx_sp[r][a] * NS + m];
+            e = fma(pyro::slot_nu(r, a), d, e);
+          }
+          if (a < np) {
+            double& e = Jc[k_rx_sp[r][MAXSIDE + a] * NS + m];
+            e = fma(pyro::slot_nu(r, MAXSIDE + a), d, e);
+          }
+        }
+      }
+      for (int t = k_st_start[m]; t < k_st_start[m + 1]; ++t) {
+        const int r = k_st_rx[t];
+        const double d = k_st_de[t] * rdM[r];
+        const int nr = k_rx_nr[r], np = k_rx_np[r];
+        for (int a = 0; a < MAXSIDE; ++a) {
+          if (a < nr) {
+            double& e = Jc[k_rx_sp[r][a] * NS + m];
+            e = fma(pyro::slot_nu(r, a), d, e);
+          }
+          if (a < np) {
+            double& e = Jc[k_rx_sp[r][MAXSIDE + a] * NS + m];
+            e = fma(pyro::slot_nu(r, MAXSIDE + a), d, e);
+          }
+        }
+      }
+    }
+    __syncwarp();
+    // u_k = sum_m dw_k/dc_m c_m (with the rank-1 part), column sums of H J
+    const double RT = GAS_CONSTANT * T;
+    for (int k = lane; k < NS; k += 32) {
+      double u = sa[k] * s.ctot;
+      for (int mm = 0; mm < NS; ++mm) u = fma(Jc[k * NS + mm], sc[mm], u);
+      su[k] = u;
+    }
+    for (int jj = lane; jj < NS; jj += 32) {
+      double acc = 0.0;
+      for (int k = 0; k < NS; ++k) acc = fma(sh[k], Jc[k * NS + jj], acc);
+      shj[jj] = RT * acc;
+    }
+    __syncwarp();
+    double pQ = 0.0, pHA = 0.0, pHU = 0.0, pdQ = 0.0;
+    for (int k = lane; k < NS; k += 32) {
+      const double Hk = RT * sh[k];
+      pQ = fma(Hk, sw[k], pQ);
+      pHA = fma(Hk, sa[k], pHA);
+      pHU = fma(Hk, su[k], pHU);
+      // dQ/dT = sum_k (R cp_k w_k + H_k (dw_k/dT|c - u_k / T))
+      pdQ += GAS_CONSTANT * scp[k] * sw[k] + Hk * (sjt[k] - su[k] * invT);
+    }
+    const double Q = pyro::warp_sum(pQ), HA = pyro::warp_sum(pHA);
+    const double HU = pyro::warp_sum(pHU), dQdT = pyro::warp_sum(pdQ);
+    const double rcp = rho * cpm;
+    const double inv_rcp = 1.0 / rcp;
+    const double qr2 = Q * inv_rcp * inv_rcp;
+    const double inv_sig = 1.0 / sigma;
+    double* Ji = J + i * ldj;
+    // row 0: d(dT/dt)/dx
+    for (int col = lane; col < NC; col += 32) {
+      double v;
+      if (col == 0) {
+        v = -dQdT * inv_rcp + qr2 * (-rcp * invT + rho * dcpm);
+      } else {
+        const int jj = col - 1;
+        const double iw = k_inv_mw[jj];
+        const double dQdY = rho * iw * (shj[jj] + HA) - HU * inv_sig * iw;
+        const double drcp = -rcp * inv_sig * iw + rho * GAS_CONSTANT * scp[jj] * iw;
+        v = -dQdY * inv_rcp + qr2 * drcp;
+      }
+      Ji[col] = v;
+    }
+    // rows 1..S: d(dY_k/dt)/dx
+    for (int k = 0; k < NS; ++k) {
+      const double wk_rho = k_mw[k] / rho;
+      const double wk = sw[k], uk = su[k], ak = sa[k];
+      for (int col = lane; col < NC; col += 32) {
+        double v;
+        if (col == 0) {
+          v = wk_rho * (sjt[k] - uk * invT + wk * invT);
+        } else {
+          const int jj = col - 1;
+          const double iw = k_inv_mw[jj];
+          v = wk_rho * ((Jc[k * NS + jj] + ak) * rho * iw +
+                        (wk - uk) * inv_sig * iw);
+        }
+        Ji[(int64_t)(k + 1) * NC + col] = v;
+      }
+    }
+    __syncwarp();
+  }
+}
+
+// Source values f = (dT/dt, dY/dt) [S+1][ldf] (table-driven, one thread
+// per state).
+__global__ void __launch_bounds__(BLOCK)
+    k_reactor_source(const double* __restrict__ Pp, int64_t p_inc,
+                     const double* __restrict__ Tp, int64_t t_inc,
+                     const double* __restrict__ Y, int64_t ldy,
+                     double* __restrict__ F, int64_t ldf, int64_t n) {
+  extern __shared__ double smem[];
+  PEXP_PRELOAD();
+  const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
+                   w = pyro::col(smem, 2);
+  PYRO_LOOP(i) {
+    const double T = pyro_ld(Tp, t_inc, i);
+    const double lnT = log(T), invT = 1.0 / T;
+    double sigma = 0.0, cpp = 0.0;
+    for (int k = 0; k < NS; ++k) {
+      const double wk = __ldg(Y + (int64_t)k * ldy + i) * k_inv_mw[k];
+      sigma += wk;
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      cpp = fma(wk,
+                fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]),
+                cpp);
+    }
+    const double rho = pyro_ld(Pp, p_inc, i) / (GAS_CONSTANT * T * sigma);
+    const pyro::StateScalars s = pyro::state_from_mass(T, rho, Y, ldy, i, c);
+    pyro::production_rates(s, c, g, w);
+    double q = 0.0;
+    for (int k = 0; k < NS; ++k) {
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      const double hrt =
+          fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
+                            a[2] * (1.0 / 3.0)),
+                    a[1] * 0.5),
+              a[0]) +
+          a[5] * invT;
+      q = fma(GAS_CONSTANT * T * hrt, w[k], q);
+      F[(int64_t)(k + 1) * ldf + i] = k_mw[k] * w[k] / rho;
+    }
+    F[i] = -q / (rho * GAS_CONSTANT * cpp);
+  }
+}
+
+// Vector-Jacobian product v^T df/dx for x = (T, Y) and df/dp, with v
+// [S+1][ldv]; outputs gT[n], gY[S][ldg], gp[n] (gp may be NULL).
+#ifndef VBLOCK
+#define VBLOCK 32
+#endif
+
+__global__ void __launch_bounds__(VBLOCK)
+    k_reactor_vjp(const double* __restrict__ Pp, int64_t p_inc,
+                  const double* __restrict__ Tp, int64_t t_inc,
+                  const double* __restrict__ Y, int64_t ldy,
+                  const double* __restrict__ V, int64_t ldv,
+                  double* __restrict__ gT, double* __restrict__ gY,
+                  int64_t ldg, double* __restrict__ gp, int64_t n) {
+  extern __shared__ double smem[];
+  PEXP_PRELOAD();
+  using VC = pyro::ColsT<VBLOCK>;
+  double* col0 = smem + threadIdx.x;
+  const VC c{col0}, g{col0 + NS * VBLOCK}, h{col0 + 2 * NS * VBLOCK},
+      gc{col0 + 3 * NS * VBLOCK}, w{col0 + 4 * NS * VBLOCK};
+  for (int64_t i = (int64_t)blockIdx.x * VBLOCK + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * VBLOCK) {
+    const double T = pyro_ld(Tp, t_inc, i);
+    const double P = pyro_ld(Pp, p_inc, i);
+    const double lnT = log(T), invT = 1.0 / T;
+    double sigma = 0.0, cpp = 0.0, dcpp = 0.0;
+    for (int k = 0; k < NS; ++k) {
+      const double wk = __ldg(Y + (int64_t)k * ldy + i) * k_inv_mw[k];
+      const pyro::SpThermo th = pyro::species_thermo(k, T, lnT, invT);
+      h[k] = th.h;
+      g[k] = th.g;
+      sigma += wk;
+      cpp = fma(wk, th.cp, cpp);
+      dcpp = fma(wk, th.dcp, dcpp);
+      gc[k] = 0.0;
+      w[k] = 0.0;
+    }
+    const double cpm = GAS_CONSTANT * cpp, dcpm = GAS_CONSTANT * dcpp;
+    const double rho = P / (GAS_CONSTANT * T * sigma);
+    double ct = 0.0;
+    for (int k = 0; k < NS; ++k) {
+      const double v = k_inv_mw[k] * rho * __ldg(Y + (int64_t)k * ldy + i);
+      c[k] = v;
+      ct += v;
+    }
+    pyro::StateScalars s;
+    s.T = T;
+    s.lnT = lnT;
+    s.invT = invT;
+    s.c0 = LOG_P0_OVER_R - lnT;
+    s.ctot = ct;
+    const double RT = GAS_CONSTANT * T;
+    const double rcp = rho * cpm;
+    const double v0 = __ldg(V + i);
+    // lambda_k = v_k W_k / rho - v0 H_k / (rho cp)
+    const double l1 = 1.0 / rho, l2 = -v0 * RT / rcp;
+    double gTc = 0.0, A = 0.0;
+    for (int r = 0; r < NR; ++r) {
+      const pyro::RxnDeriv d = pyro::reaction_deriv(r, s, c, g, h);
+      const int f = k_rx_flags[r];
+      const int nr = k_rx_nr[r], np = k_rx_np[r];
+      double mu = 0.0;
+      for (int a = 0; a < MAXSIDE; ++a) {
+        if (a < nr) {
+          const int k = k_rx_sp[r][a];
+          const double nu = pyro::slot_nu(r, a);
+          const double lam =
+              fma(__ldg(V + (int64_t)(k + 1) * ldv + i) * k_mw[k], l1,
+                  l2 * h[k]);
+          mu = fma(nu, lam, mu);
+          w[k] = fma(nu, d.q, w[k]);
+        }
+        if (a < np) {
+          const int k = k_rx_sp[r][MAXSIDE + a];
+          const double nu = pyro::slot_nu(r, MAXSIDE + a);
+          const double lam =
+              fma(__ldg(V + (int64_t)(k + 1) * ldv + i) * k_mw[k], l1,
+                  l2 * h[k]);
+          mu = fma(nu, lam, mu);
+          w[k] = fma(nu, d.q, w[k]);
+        }
+      }
+      gTc = fma(mu, d.dqdT, gTc);
+      const bool frac = (f & RX_FRACTIONAL) != 0;
+      for (int a = 0; a < MAXSIDE; ++a) {
+        if (a < nr) {
+          const int k = k_rx_sp[r][a];
+          gc[k] = fma(mu * d.kf, pyro::dprod(r, 0, a, nr, frac, c), gc[k]);
+        }
+        if (a < np) {
+          const int k = k_rx_sp[r][MAXSIDE + a];
+          gc[k] = fma(-mu * d.kr, pyro::dprod(r, 1, a, np, frac, c), gc[k]);
+        }
+      }
+      if ((f & RX_KIND_MASK) != RX_ELEMENTARY) {
+        const double md = mu * d.dqdM;
+        A = fma(md, k_rx_defeff[r], A);
+        for (int t = k_rx_tb[r]; t < k_rx_tb[r + 1]; ++t)
+          gc[k_tb_idx[t]] = fma(md, k_tb_de[t], gc[k_tb_idx[t]]);
+      }
+    }
+    double GC = 0.0, Q = 0.0, S1 = 0.0, S3 = 0.0;
+    for (int k = 0; k < NS; ++k) {
+      gc[k] += A;
+      GC = fma(gc[k], c[k], GC);
+      Q = fma(RT * h[k], w[k], Q);
+      S1 = fma(__ldg(V + (int64_t)(k + 1) * ldv + i) * k_mw[k], w[k], S1);
+    }
+    for (int k = 0; k < NS; ++k) {
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      const double cpr =
+          fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
+      S3 = fma(GAS_CONSTANT * cpr, w[k], S3);
+    }
+    const double inv_sig = 1.0 / sigma;
+    const double qf = v0 * Q / (rcp * cpm);
+    gT[i] = gTc - GC * invT + S1 * invT / rho - v0 * S3 / rcp +
+            qf * (-cpm * invT + dcpm);
+    for (int k = 0; k < NS; ++k) {
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      const double cpr =
+          fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
+      const double iw = k_inv_mw[k];
+      gY[(int64_t)k * ldg + i] =
+          gc[k] * rho * iw + (S1 / rho - GC) * inv_sig * iw +
+          qf * (-cpm * inv_sig * iw + GAS_CONSTANT * cpr * iw);
+    }
+    if (gp) gp[i] = (GC - S1 / rho + v0 * Q / rcp) / P;
+  }
+}

@@ -8,8 +8,18 @@
 
 #ifdef PYRO_UNROLLED
 // Straight-line variants (pyro_unrolled::net_rates is generated per
-// mechanism): shared memory holds only concentrations and Gibbs energies.
-__global__ void __launch_bounds__(BLOCK)
+// mechanism): shared memory holds only concentrations and Gibbs energies
+// (and the accumulators when PYRO_HOT_COLS is 3); block size HOT_BLOCK.
+#define PYRO_HLOOP(i)                                                      \
+  for (int64_t i = (int64_t)blockIdx.x * HOT_BLOCK + threadIdx.x; i < n;   \
+       i += (int64_t)gridDim.x * HOT_BLOCK)
+
+__device__ __forceinline__ pyro::ColsT<HOT_BLOCK> hcol(double* smem, int q) {
+  return pyro::ColsT<HOT_BLOCK>{smem + (size_t)q * NS * HOT_BLOCK +
+                                threadIdx.x};
+}
+
+__global__ void __launch_bounds__(HOT_BLOCK)
     k_net_production_rates_u(const double* __restrict__ rhop,
                              int64_t rho_inc, const double* __restrict__ Tp,
                              int64_t t_inc, const double* __restrict__ Y,
@@ -17,9 +27,9 @@ __global__ void __launch_bounds__(BLOCK)
                              int64_t ldw, int64_t n) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
-  const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
-                   w = pyro::col(smem, PYRO_HOT_COLS - 1);
-  PYRO_LOOP(i) {
+  const auto c = hcol(smem, 0), g = hcol(smem, 1),
+             w = hcol(smem, PYRO_HOT_COLS - 1);
+  PYRO_HLOOP(i) {
     double wd[NS];
     pyro_unrolled::net_rates(pyro_ld(Tp, t_inc, i), pyro_ld(rhop, rho_inc, i),
                              Y, ldy, i, c, g, w, wd);
@@ -28,7 +38,7 @@ __global__ void __launch_bounds__(BLOCK)
   }
 }
 
-__global__ void __launch_bounds__(BLOCK)
+__global__ void __launch_bounds__(HOT_BLOCK)
     k_fused_step_u(const double* __restrict__ Pp, int64_t p_inc,
                    const double* __restrict__ Tp, int64_t t_inc,
                    const double* __restrict__ Y, int64_t ldy,
@@ -40,9 +50,9 @@ __global__ void __launch_bounds__(BLOCK)
                    int64_t n) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
-  const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
-                   w = pyro::col(smem, PYRO_HOT_COLS - 1);
-  PYRO_LOOP(i) {
+  const auto c = hcol(smem, 0), g = hcol(smem, 1),
+             w = hcol(smem, PYRO_HOT_COLS - 1);
+  PYRO_HLOOP(i) {
     const double T = pyro_ld(Tp, t_inc, i);
     double inv_mmw = 0.0;
     for (int k = 0; k < NS; ++k)
@@ -65,6 +75,7 @@ __global__ void __launch_bounds__(BLOCK)
 #define K_NET k_net_production_rates_u
 #define K_FUSED k_fused_step_u
 #else
+#define HOT_BLOCK BLOCK
 #define HOT_COLS 3
 #define K_NET k_net_production_rates
 #define K_FUSED k_fused_step
@@ -76,7 +87,14 @@ int grid_for(int64_t n) {
   return pyro_grid(n, BLOCK, pyro_sm_count() * BLOCKS_PER_SM);
 }
 
+int hot_grid_for(int64_t n) {
+  return pyro_grid(n, HOT_BLOCK, pyro_sm_count() * BLOCKS_PER_SM);
+}
+
 constexpr size_t smem_cols(int q) { return (size_t)q * NS * BLOCK * 8; }
+constexpr size_t hot_smem_cols(int q) {
+  return (size_t)q * NS * HOT_BLOCK * 8;
+}
 
 // Opt a kernel into more than 48 KB of shared memory (dynamic plus the
 // static exp table) when needed.
@@ -172,10 +190,10 @@ PYRO_EXPORT int pyro_net_production_rates(const double* rho, int64_t rho_inc,
   if (n == 0) return PYRO_OK;
   if (!rho || !T || !Y || !wdot || ldy < n || ldw < n)
     return PYRO_ERR_ARGUMENT;
-  const size_t sm = smem_cols(HOT_COLS);
+  const size_t sm = hot_smem_cols(HOT_COLS);
   if (prepare_smem((const void*)K_NET, sm) != PYRO_OK) return PYRO_ERR_LAUNCH;
-  K_NET<<<grid_for(n), BLOCK, sm, stream>>>(rho, rho_inc, T, t_inc, Y, ldy,
-                                            wdot, ldw, n);
+  K_NET<<<hot_grid_for(n), HOT_BLOCK, sm, stream>>>(rho, rho_inc, T, t_inc, Y,
+                                                    ldy, wdot, ldw, n);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
@@ -227,12 +245,74 @@ PYRO_EXPORT int pyro_fused_step(const double* p, int64_t p_inc,
   if (!p || !T || !Y || !target || !t0 || !wdot || !T_out || ldy < n ||
       ldw < n)
     return PYRO_ERR_ARGUMENT;
-  const size_t sm = smem_cols(HOT_COLS);
+  const size_t sm = hot_smem_cols(HOT_COLS);
   if (prepare_smem((const void*)K_FUSED, sm) != PYRO_OK)
     return PYRO_ERR_LAUNCH;
-  K_FUSED<<<grid_for(n), BLOCK, sm, stream>>>(
+  K_FUSED<<<hot_grid_for(n), HOT_BLOCK, sm, stream>>>(
       p, p_inc, T, t_inc, Y, ldy, target, target_inc, t0, t0_inc, do_energy,
       tol, max_iter, wdot, ldw, T_out, fail_count, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+// ---- reactor source, Jacobian, VJP (csrc/jacobian.cuh) -----------------
+
+PYRO_EXPORT int pyro_reactor_source(const double* p, int64_t p_inc,
+                                    const double* T, int64_t t_inc,
+                                    const double* Y, int64_t ldy, double* F,
+                                    int64_t ldf, int64_t n,
+                                    cudaStream_t stream) {
+  if (n < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!p || !T || !Y || !F || ldy < n || ldf < n) return PYRO_ERR_ARGUMENT;
+  const size_t sm = smem_cols(3);
+  if (prepare_smem((const void*)k_reactor_source, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  k_reactor_source<<<grid_for(n), BLOCK, sm, stream>>>(p, p_inc, T, t_inc, Y,
+                                                       ldy, F, ldf, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_reactor_jacobian(const double* p, int64_t p_inc,
+                                      const double* T, int64_t t_inc,
+                                      const double* Y, int64_t ldy, double* J,
+                                      int64_t ldj, int64_t n,
+                                      cudaStream_t stream) {
+  if (n < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!p || !T || !Y || !J || ldy < n ||
+      ldj < (int64_t)(NS + 1) * (NS + 1))
+    return PYRO_ERR_ARGUMENT;
+  const size_t sm = (size_t)JWARPS * JW_DOUBLES * sizeof(double);
+  if (prepare_smem((const void*)k_reactor_jacobian, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  const int64_t blocks = (n + JWARPS - 1) / JWARPS;
+  const int grid =
+      (int)(blocks < (int64_t)pyro_sm_count() * 8 ? blocks
+                                                   : (int64_t)pyro_sm_count() * 8);
+  k_reactor_jacobian<<<grid, JWARPS * 32, sm, stream>>>(p, p_inc, T, t_inc, Y,
+                                                        ldy, J, ldj, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_reactor_vjp(const double* p, int64_t p_inc,
+                                 const double* T, int64_t t_inc,
+                                 const double* Y, int64_t ldy,
+                                 const double* V, int64_t ldv, double* gT,
+                                 double* gY, int64_t ldg, double* gp,
+                                 int64_t n, cudaStream_t stream) {
+  if (n < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!p || !T || !Y || !V || !gT || !gY || ldy < n || ldv < n || ldg < n)
+    return PYRO_ERR_ARGUMENT;
+  const size_t sm = (size_t)5 * NS * VBLOCK * sizeof(double);
+  if (prepare_smem((const void*)k_reactor_vjp, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  k_reactor_vjp<<<pyro_grid(n, VBLOCK, pyro_sm_count() * 16), VBLOCK, sm,
+                  stream>>>(p, p_inc, T, t_inc, Y, ldy, V, ldv, gT, gY, ldg,
+                            gp, n);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }

@@ -33,7 +33,11 @@ def build_runtime() -> str:
     return _build("runtime.cu", "runtime")
 
 
-BUILDERS = [build_peaks, build_mathcheck, build_runtime]
+def build_block_thomas() -> str:
+    return _build("block_thomas.cu", "block_thomas")
+
+
+BUILDERS = [build_peaks, build_mathcheck, build_runtime, build_block_thomas]
 
 
 @lru_cache(maxsize=None)
@@ -101,3 +105,17 @@ def copy_columns_async(dst, src, col0_dst: int, col0_src: int, ncols: int,
         ctypes.c_void_p(stream.cuda_stream))
     if st != 0:
         raise RuntimeError(f"pyro_memcpy2d_async failed (status {st})")
+
+
+@lru_cache(maxsize=None)
+def block_thomas_lib() -> ctypes.CDLL:
+    lib = ctypes.CDLL(build_block_thomas())
+    P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    lib.pyro_block_thomas.restype = I
+    lib.pyro_block_thomas.argtypes = [P, P, P, P, P, P, P, I, I, P, P, P, I,
+                                      I, P]
+    lib.pyro_block_thomas_work_doubles.restype = I64
+    lib.pyro_block_thomas_work_doubles.argtypes = [I, I64]
+    lib.pyro_block_thomas_smem_bytes.restype = I64
+    lib.pyro_block_thomas_smem_bytes.argtypes = [I]
+    return lib

@@ -64,6 +64,12 @@ _SIGNATURES = {
                          _I64, _P],
     "pyro_fused_step": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
                         _INT, _D, _INT, _P, _I64, _P, _P, _I64, _P],
+    "pyro_reactor_source": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _I64,
+                            _P],
+    "pyro_reactor_jacobian": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _I64,
+                              _P],
+    "pyro_reactor_vjp": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P,
+                         _I64, _P, _I64, _P],
 }
 
 
@@ -547,6 +553,99 @@ class CudaThermochemistryBase:
         return out_w, out_t
 
     # }}}
+
+    # {{{ constant-pressure reactor source, Jacobian and VJP
+
+    def _reactor_args(self, pressure, temperature, mass_fractions):
+        ym, ny, single = self._species_mat(mass_fractions, self.num_species)
+        pv = self._scalar_vec(pressure)
+        tv = self._scalar_vec(temperature)
+        n = self._n(ny, pv, tv)
+        return pv, tv, self._expand_mat(ym, n), n, single
+
+    def get_reactor_source(self, pressure, temperature, mass_fractions):
+        """``[dT/dt, dY_1/dt, ...]`` ([S+1, N]) of an adiabatic
+        constant-pressure reactor: ``dY_k/dt = W_k w_k / rho``,
+        ``dT/dt = -sum_k H_k w_k / (rho cp)`` -- the right-hand side the
+        reference's reactors differentiate
+        (``examples/free_flame/reactors.py:115-125``)."""
+        pv, tv, ym, n, single = self._reactor_args(pressure, temperature,
+                                                   mass_fractions)
+        out = self._out(self.num_species + 1, n)
+        _check(self._lib.pyro_reactor_source(
+            pv.ptr, pv.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
+            out.data_ptr(), out.stride(0), n, self._stream), "reactor source")
+        return self._shape_rows(out, single and n == 1)
+
+    def get_reactor_jacobian(self, pressure, temperature, mass_fractions,
+                             out=None):
+        """Jacobian ``d[dT/dt, dY/dt] / d[T, Y]`` per state, ``[N, S+1,
+        S+1]`` (row-major per state), by the analytic warp-per-state
+        kernel."""
+        pv, tv, ym, n, single = self._reactor_args(pressure, temperature,
+                                                   mass_fractions)
+        nc = self.num_species + 1
+        if out is None:
+            out = torch.empty((n, nc, nc), dtype=torch.float64,
+                              device=self.device)
+        if (tuple(out.shape) != (n, nc, nc) or out.stride(2) != 1
+                or out.stride(1) != nc):
+            raise ValueError("out must be a [N, S+1, S+1] row-major tensor")
+        _check(self._lib.pyro_reactor_jacobian(
+            pv.ptr, pv.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
+            out.data_ptr(), out.stride(0) if n > 1 else nc * nc, n,
+            self._stream), "reactor Jacobian")
+        return out[0] if single and n == 1 else out
+
+    def get_reactor_vjp(self, pressure, temperature, mass_fractions,
+                        cotangent):
+        """``v^T df/dx`` for cotangents ``v`` ([S+1, N]) without forming
+        the Jacobian; returns ``(g_T[N], g_Y[S, N], g_p[N])``."""
+        pv, tv, ym, n, single = self._reactor_args(pressure, temperature,
+                                                   mass_fractions)
+        v, nv, _ = self._species_mat(cotangent, self.num_species + 1)
+        v = self._expand_mat(v, n)
+        gT = torch.empty(n, dtype=torch.float64, device=self.device)
+        gY = self._out(self.num_species, n)
+        gp = torch.empty(n, dtype=torch.float64, device=self.device)
+        _check(self._lib.pyro_reactor_vjp(
+            pv.ptr, pv.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
+            v.data_ptr(), v.stride(0), gT.data_ptr(), gY.data_ptr(),
+            gY.stride(0), gp.data_ptr(), n, self._stream), "reactor VJP")
+        return gT, gY, gp
+
+    def reactor_source(self, pressure, temperature, mass_fractions):
+        """Differentiable reactor source: a ``torch.autograd.Function``
+        whose backward is the VJP kernel (gradients for p, T and Y)."""
+        return ReactorSource.apply(self, self._dev(pressure),
+                                   self._dev(temperature),
+                                   self._dev(mass_fractions))
+
+    # }}}
+
+
+if torch is not None:
+    class ReactorSource(torch.autograd.Function):
+        """f = (dT/dt, dY/dt) of the constant-pressure reactor with a
+        hand-written VJP backward (``k_reactor_vjp``)."""
+
+        @staticmethod
+        def forward(ctx, thermo, p, t, y):
+            ctx.thermo = thermo
+            ctx.save_for_backward(p, t, y)
+            return thermo.get_reactor_source(p, t, y)
+
+        @staticmethod
+        def backward(ctx, grad):
+            p, t, y = ctx.saved_tensors
+            th = ctx.thermo
+            g = grad.reshape(th.num_species + 1, -1)
+            gT, gY, gp = th.get_reactor_vjp(p, t, y, g)
+            gp_out = gp.reshape(p.shape) if p.numel() > 1 else gp.sum(
+            ).reshape(p.shape)
+            gT_out = gT.reshape(t.shape) if t.numel() > 1 else gT.sum(
+            ).reshape(t.shape)
+            return None, gp_out, gT_out, gY.reshape(y.shape)
 
 
 def make_thermochem_class(sol, lib_path: str, name: str = "Thermochemistry"):

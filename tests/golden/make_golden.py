@@ -174,12 +174,37 @@ def golden(sol, n, seed, n_jac, fname):
           f"jac={n_jac}")
 
 
+def golden_block_thomas(fname="block_thomas.npz"):
+    """Systems of the benchmark's kind (diagonally dominant random blocks,
+    uneven lengths) solved by the reference's own block_thomas."""
+    from oracle.block_thomas_oracle import make_systems
+    bt = refgen.reference_block_thomas()
+    out = {}
+    for tag, nv, nsys, nmin, nmax, seed in (("nv4", 4, 5, 1, 9, 31),
+                                            ("nv10", 10, 4, 2, 40, 32),
+                                            ("nv54", 54, 2, 3, 12, 33)):
+        lengths, lo, c, up, b = make_systems(nsys, nv, nmin, nmax, seed)
+        x = np.empty_like(b)
+        r0 = 0
+        for n in lengths:
+            n = int(n)
+            x[r0:r0 + n] = bt(lo[r0:r0 + n - 1], c[r0:r0 + n],
+                              up[r0:r0 + n - 1], b[r0:r0 + n])
+            r0 += n
+        for k, v in (("lengths", lengths), ("L", lo), ("C", c), ("U", up),
+                     ("b", b), ("x", x)):
+            out[f"{tag}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+    print(f"wrote {fname}")
+
+
 def main():
     if not refgen.reference_available():
         raise SystemExit("reference checkout not found")
     golden(synthetic.config1_mechanism(), 256, 11, 24, "synthetic9.npz")
     golden(synthetic.config2_mechanism(), 48, 12, 6, "synthetic53.npz")
     golden(quirks_mechanism(), 128, 13, 12, "quirks9.npz")
+    golden_block_thomas()
 
 
 if __name__ == "__main__":

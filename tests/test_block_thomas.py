@@ -1,0 +1,102 @@
+"""Batched block-Thomas: the oracle against the reference's own
+``block_thomas`` (golden vectors from ``flamelets/linear_solver.py`` run in
+the build container) and against a dense solve; the CUDA solver against
+both (``-m gpu``)."""
+
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from oracle.block_thomas_oracle import (block_thomas, dense_matrix,
+                                        make_systems, solve_packed)
+
+TAGS = ["nv4", "nv10", "nv54"]
+
+
+def _golden(tag):
+    g = np.load(os.path.join(GOLDEN, "block_thomas.npz"))
+    return [g[f"{tag}_{k}"] for k in ("lengths", "L", "C", "U", "b", "x")]
+
+
+def _rel(x, ref):
+    return np.abs(x - ref).max() / np.abs(ref).max()
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_oracle_matches_reference_block_thomas(tag):
+    lengths, L, C, U, b, x = _golden(tag)
+    assert _rel(solve_packed(lengths, L, C, U, b), x) < 1e-14
+
+
+def test_oracle_against_dense_solve():
+    lengths, L, C, U, b = make_systems(1, 6, 5, 5, seed=3)
+    n = int(lengths[0])
+    x = block_thomas(L[:n - 1], C, U[:n - 1], b)
+    xd = np.linalg.solve(dense_matrix(L[:n - 1], C, U[:n - 1]),
+                         b.reshape(-1)).reshape(n, -1)
+    assert _rel(x, xd) < 1e-13
+
+
+torch = pytest.importorskip("torch")
+
+
+def _cuda():
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for the gpu tests")
+
+
+def _solve_cuda(lengths, L, C, U, b, threads=None, use_graph=False):
+    from pyrometheus_gb300.flamelet import BlockThomasSolver
+    dev = torch.device("cuda")
+    t = [torch.as_tensor(a, device=dev).contiguous() for a in (L, C, U, b)]
+    solver = BlockThomasSolver(C.shape[1], lengths, threads=threads,
+                               use_graph=use_graph)
+    x = solver.solve(*t)
+    solver.check_status()
+    return x.cpu().numpy(), solver, t
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("tag", TAGS)
+@pytest.mark.parametrize("threads", [32, 64, 128])
+def test_cuda_block_thomas_golden(tag, threads):
+    _cuda()
+    lengths, L, C, U, b, x = _golden(tag)
+    got, _, _ = _solve_cuda(lengths, L, C, U, b, threads=threads)
+    assert _rel(got, x) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nv", [10, 54])
+def test_cuda_block_thomas_uneven_batch(nv):
+    _cuda()
+    lengths, L, C, U, b = make_systems(37 if nv == 54 else 300, nv, 1, 200,
+                                       seed=nv)
+    ref = solve_packed(lengths, L, C, U, b)
+    got, solver, t = _solve_cuda(lengths, L, C, U, b)
+    r0 = 0
+    for n in lengths:
+        n = int(n)
+        assert _rel(got[r0:r0 + n], ref[r0:r0 + n]) < 1e-12
+        r0 += n
+
+
+@pytest.mark.gpu
+def test_cuda_graph_replay_and_single_system_api():
+    _cuda()
+    from pyrometheus_gb300.flamelet import block_thomas as bt_gpu
+    lengths, L, C, U, b = make_systems(64, 10, 16, 64, seed=5)
+    ref = solve_packed(lengths, L, C, U, b)
+    got, solver, t = _solve_cuda(lengths, L, C, U, b, use_graph=True)
+    assert _rel(got, ref) < 1e-12
+    # replay with new right-hand sides in the same buffers
+    b2 = np.random.default_rng(6).standard_normal(b.shape)
+    t[3].copy_(torch.as_tensor(b2))
+    x2 = solver.solve(*t).cpu().numpy()
+    assert _rel(x2, solve_packed(lengths, L, C, U, b2)) < 1e-12
+    # the reference's single-system signature
+    n = int(lengths[0])
+    xs = bt_gpu(L[:n - 1], C[:n], U[:n - 1], b[:n]).cpu().numpy()
+    assert _rel(xs, ref[:n]) < 1e-12

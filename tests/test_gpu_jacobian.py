@@ -1,0 +1,105 @@
+"""Reactor-source Jacobian (warp-per-state kernel) and VJP (thread-per-state
+kernel) against the reference's autodiff Jacobian (``torch.func.jacfwd``
+through the reference-generated class, stored in the golden vectors), against
+central finite differences of the oracle, and against each other.
+
+The reference checks its JAX Jacobian against central differences with an
+order-of-convergence criterion (``test/test.py:300-374``: EOC > 1.95 over
+delta in {1e-5, 1e-6, 1e-7}); the same criterion is applied here."""
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_SETS, load_golden
+
+torch = pytest.importorskip("torch")
+pytestmark = pytest.mark.gpu
+
+# Jacobian entries are sums of terms of both signs; compare each row at the
+# scale of its largest entry
+TOL_ROW = 1e-11
+
+
+def _cls(sol):
+    if not torch.cuda.is_available():
+        pytest.fail("CUDA device required for the gpu tests")
+    from pyrometheus_gb300 import get_thermochem_class
+    return get_thermochem_class(sol)
+
+
+def _row_err(j, ref):
+    scale = np.abs(ref).max(axis=2, keepdims=True)
+    scale = np.where(scale == 0, 1.0, scale)
+    return (np.abs(j - ref) / scale).max()
+
+
+@pytest.mark.parametrize("name", GOLDEN_SETS)
+def test_source_and_jacobian_against_reference_autodiff(name):
+    sol, g = load_golden(name)
+    th = _cls(sol)()
+    n = g["jac"].shape[0]
+    p, t, y = g["P"][:n], g["T"][:n], g["Y"][:, :n]
+    src = th.get_reactor_source(p, t, y).cpu().numpy()
+    ref = g["reactor_source"]
+    assert np.abs(src - ref).max() <= 1e-12 * np.abs(ref).max()
+    jac = th.get_reactor_jacobian(p, t, y).cpu().numpy()
+    assert _row_err(jac, g["jac"]) < TOL_ROW
+
+
+def test_jacobian_order_of_convergence_like_reference():
+    """Central differences of the oracle source converge to the CUDA
+    Jacobian at second order (test/test.py:360-374)."""
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    sol, g = load_golden("synthetic9")
+    th = _cls(sol)()
+    orc = Oracle(sol)
+    p, t, y = g["P"][5:7], g["T"][5:7], g["Y"][:, 5:7]
+    jac = th.get_reactor_jacobian(p, t, y).cpu().numpy()
+    errs = []
+    deltas = [1e-3, 1e-4, 1e-5]
+    for rel in deltas:
+        jfd = orc.reactor_jacobian_fd(p, t, y, rel=rel, absolute_y=True)
+        errs.append(np.linalg.norm(jac - jfd) / np.linalg.norm(jac))
+    order = np.polyfit(np.log(deltas), np.log(errs), 1)[0]
+    assert order > 1.95, (errs, order)
+
+
+def test_vjp_matches_jacobian_transpose():
+    from pyrometheus_gb300 import synthetic
+    sol, _ = load_golden("synthetic53")
+    th = _cls(sol)()
+    n = 257
+    t, p, y = synthetic.sample_states(sol, n, seed=3)
+    rng = np.random.default_rng(4)
+    v = rng.standard_normal((sol.n_species + 1, n))
+    jac = th.get_reactor_jacobian(p, t, y).cpu().numpy()
+    gT, gY, gp = th.get_reactor_vjp(p, t, y, v)
+    vj = np.einsum("in,nij->nj", v, jac)
+    scale = (np.abs(v).T[:, :, None] * np.abs(jac)).sum(axis=1)
+    got = np.concatenate([gT.cpu().numpy()[None, :], gY.cpu().numpy()]).T
+    assert np.all(np.abs(got - vj) <= 1e-12 * scale + 1e-300)
+    # dp through finite differences of the source
+    fp = th.get_reactor_source(p * (1 + 1e-6), t, y).cpu().numpy()
+    fm = th.get_reactor_source(p * (1 - 1e-6), t, y).cpu().numpy()
+    dfdp = (fp - fm) / (2e-6 * p)
+    gp_fd = (v * dfdp).sum(axis=0)
+    gps = gp.cpu().numpy()
+    assert np.all(np.abs(gps - gp_fd) <= 1e-6 * np.abs(v * dfdp).sum(axis=0))
+
+
+def test_autograd_function():
+    from pyrometheus_gb300 import synthetic
+    sol, _ = load_golden("synthetic9")
+    th = _cls(sol)()
+    n = 64
+    t, p, y = synthetic.sample_states(sol, n, seed=8)
+    T = torch.tensor(t, device="cuda", requires_grad=True)
+    Y = torch.tensor(y, device="cuda", requires_grad=True)
+    P = torch.tensor(p, device="cuda", requires_grad=True)
+    f = th.reactor_source(P, T, Y)
+    v = torch.randn_like(f)
+    (f * v).sum().backward()
+    gT, gY, gp = th.get_reactor_vjp(p, t, y, v)
+    assert torch.allclose(T.grad, gT, rtol=0, atol=0)
+    assert torch.allclose(Y.grad, gY, rtol=0, atol=0)
+    assert torch.allclose(P.grad, gp, rtol=0, atol=0)
