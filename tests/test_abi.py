@@ -16,7 +16,8 @@ def declared(header):
     with open(os.path.join(HEADER_DIR, header)) as f:
         text = f.read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
-    return sorted(set(re.findall(r"\bint\s+(pyro_\w+)\s*\(", text)))
+    return sorted(set(re.findall(r"\b(?:int|int64_t)\s+(pyro_\w+)\s*\(",
+                                 text)))
 
 
 def test_header_parses():
@@ -38,6 +39,15 @@ def test_mechanism_library_exports_header_symbols():
     assert so.pyro_mechanism_info(ctypes.byref(ns), ctypes.byref(nr),
                                   ctypes.byref(nf), None, None) == 0
     assert (ns.value, nr.value, nf.value) == (9, 24, 2)
+
+
+def test_block_thomas_library_exports_header_symbols():
+    from pyrometheus_gb300 import native
+    so = ctypes.CDLL(native.build_block_thomas())
+    for name in declared("pyro_block_thomas.h"):
+        assert hasattr(so, name), name
+    so.pyro_block_thomas_work_doubles.restype = ctypes.c_int64
+    assert so.pyro_block_thomas_work_doubles(10, 7) == 7 * 110
 
 
 def test_argument_errors_without_launch():

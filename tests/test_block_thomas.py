@@ -68,9 +68,24 @@ def test_cuda_block_thomas_golden(tag, threads):
     assert _rel(got, x) < 1e-12
 
 
+def _residual(L, C, U, b, x):
+    """max-norm of A x - b for one system, relative to |A| |x| + |b|."""
+    r = np.einsum("nij,nj->ni", C, x) - b
+    s = np.einsum("nij,nj->ni", np.abs(C), np.abs(x)) + np.abs(b)
+    r[:-1] += np.einsum("nij,nj->ni", U[:-1], x[1:])
+    s[:-1] += np.einsum("nij,nj->ni", np.abs(U[:-1]), np.abs(x[1:]))
+    r[1:] += np.einsum("nij,nj->ni", L[:-1], x[:-1])
+    s[1:] += np.einsum("nij,nj->ni", np.abs(L[:-1]), np.abs(x[:-1]))
+    return (np.abs(r) / s).max()
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("nv", [10, 54])
 def test_cuda_block_thomas_uneven_batch(nv):
+    """Against the reference algorithm on long systems: the two recurrences
+    round differently (this one keeps S_i and t_i, the reference re-solves
+    with C'_i), so the comparison is at 1e-11 on x plus a componentwise
+    backward error at the level of the reference's own."""
     _cuda()
     lengths, L, C, U, b = make_systems(37 if nv == 54 else 300, nv, 1, 200,
                                        seed=nv)
@@ -79,7 +94,11 @@ def test_cuda_block_thomas_uneven_batch(nv):
     r0 = 0
     for n in lengths:
         n = int(n)
-        assert _rel(got[r0:r0 + n], ref[r0:r0 + n]) < 1e-12
+        sl = slice(r0, r0 + n)
+        assert _rel(got[sl], ref[sl]) < 1e-11
+        be_got = _residual(L[sl], C[sl], U[sl], b[sl], got[sl])
+        be_ref = _residual(L[sl], C[sl], U[sl], b[sl], ref[sl])
+        assert be_got <= max(4.0 * be_ref, 1e-15)
         r0 += n
 
 
