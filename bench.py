@@ -59,6 +59,9 @@ def parse_args():
     ap.add_argument("--states", type=int, default=N_STATES)
     ap.add_argument("--cpu-seconds", type=float, default=12.0,
                     help="target duration of the CPU baseline sample")
+    ap.add_argument("--no-secondary", dest="secondary",
+                    action="store_false",
+                    help="skip the Jacobian/VJP and block-Thomas legs")
     return ap.parse_args()
 
 
@@ -273,6 +276,79 @@ def newton_iterations(sol, t, y, e, t0=1500.0, tol=1e-6):
     return float(its.mean())
 
 
+def _event_ms(fn, reps):
+    import torch
+    fn()
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def secondary_legs(sol, th, dev, dfma):
+    """The other rows of the workload set, each measured with CUDA events on
+    device-resident seeded inputs: the 54x54 reactor Jacobian and the VJP
+    over 1,048,576 states of the same mechanism, and the batched
+    block-Thomas solve (4,096 systems, N ~ U[64, 1024], nv = 10; and a
+    304-system sample at nv = 54)."""
+    import numpy as np
+    import torch
+
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.flamelet import BlockThomasSolver
+    out = {}
+    n = 1 << 20
+    t, p, y = synthetic.sample_states(sol, n, seed=77)
+    T = torch.as_tensor(t, device=dev)
+    P = torch.as_tensor(p, device=dev)
+    Y = torch.as_tensor(y, device=dev)
+    nc = sol.n_species + 1
+    J = torch.empty((n, nc, nc), dtype=torch.float64, device=dev)
+    ms_j = _event_ms(lambda: th.get_reactor_jacobian(P, T, Y, out=J), 2)
+    del J
+    V = torch.randn((nc, n), dtype=torch.float64, device=dev,
+                    generator=torch.Generator(device=dev).manual_seed(1))
+    ms_v = _event_ms(lambda: th.get_reactor_vjp(P, T, Y, V), 2)
+    out["jacobian"] = {
+        "states": n, "ms": ms_j, "states_per_s": n / ms_j * 1e3,
+        "output_bytes_per_state": nc * nc * 8,
+        "output_gbs": n * nc * nc * 8 / ms_j / 1e6}
+    out["vjp"] = {"states": n, "ms": ms_v, "states_per_s": n / ms_v * 1e3,
+                  "cotangents": "N(0,1), seeded"}
+    del V, T, P, Y
+    rng = np.random.default_rng(0)
+    bt = {}
+    for nv, nsys in ((10, 4096), (54, 304)):
+        lengths = rng.integers(64, 1025, size=nsys)
+        rows = int(lengths.sum())
+        g = torch.Generator(device=dev).manual_seed(nv)
+        f64 = dict(dtype=torch.float64, device=dev)
+        C = torch.randn((rows, nv, nv), generator=g, **f64) + 10.0 * \
+            torch.eye(nv, **f64)
+        L = torch.randn((rows, nv, nv), generator=g, **f64)
+        U = torch.randn((rows, nv, nv), generator=g, **f64)
+        b = torch.randn((rows, nv), generator=g, **f64)
+        solver = BlockThomasSolver(nv, lengths, device=dev, use_graph=True)
+        ms = _event_ms(lambda: solver.solve(L, C, U, b), 2)
+        flops = rows * (14.0 / 3.0) * nv ** 3
+        bt[f"nv{nv}"] = {
+            "systems": nsys, "rows": rows, "ms": ms,
+            "solves_per_s": nsys / ms * 1e3,
+            "fp64_tflops": flops / ms / 1e9,
+            "fp64_frac": flops / ms / 1e9 / (dfma / 1e12),
+            "hbm_gbs": rows * (5 * nv * nv + 4 * nv) * 8 / ms / 1e6,
+            "threads_per_system": solver.threads, "cuda_graph": True}
+        del C, L, U, b, solver
+    out["block_thomas"] = bt
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -378,6 +454,7 @@ def run_gb300(args):
         hbm_peak, hbm_src = 6800.0, "fallback 6.8 TB/s"
     hbm_achieved = bps * n / (ms_per_step * 1e-3) / 1e9
 
+    extra = secondary_legs(sol, th, dev, dfma) if args.secondary else None
     base = cpu_baseline(args.cpu_seconds)
     out = {
         "metric": METRIC,
@@ -410,6 +487,8 @@ def run_gb300(args):
         "cpu_baseline": base,
         "clocks": clk,
     }
+    if extra is not None:
+        out["secondary"] = extra
     print(json.dumps(out))
 
 

@@ -23,7 +23,8 @@ extern "C" {
 typedef struct CUstream_st* cudaStream_t;
 
 /* Doubles of workspace pyro_block_thomas needs for `rows` packed rows
- * (S_i = C'_i^-1 U_i and t_i = C'_i^-1 b'_i of every row). */
+ * (per row: the LU factors of the modified diagonal block C'_i, b'_i and
+ * the pivots, kept for the backward solves). */
 int64_t pyro_block_thomas_work_doubles(int nv, int64_t rows);
 
 /* Dynamic shared memory of one CTA for blocks of size nv. */

@@ -461,8 +461,18 @@ class _Emitter:
                  [_cint(v) for v in (st_rx or [0])]))
         w(_table(qual, "double", "k_st_de", [max(1, len(st_de))],
                  [_hexd(v) for v in (st_de or [0.0])]))
-        jw = S * S + 5 * R + 10 * S
-        jwarps = max(1, min(8, (227 * 1024 - 16384) // (8 * jw)))
+        # reactions ordered by kind for the warp-per-state Jacobian: lanes
+        # of a warp take consecutive entries, so same-kind reactions run
+        # side by side (no serialised falloff/third-body branches)
+        def kind_key(j):
+            r = m.rx[j]
+            rank = {"elementary": 0, "three-body": 1, "falloff": 2}[r.kind]
+            troe = 1 if r.kind == "falloff" and r.ftype == "Troe" else 0
+            return (rank, troe, flags[j] >> 3 & 3, j)
+        perm = sorted(range(R), key=kind_key)
+        w(_table(qual, "short", "k_rx_perm", [R], [_cint(v) for v in perm]))
+        jw = 5 * R + 10 * S
+        jwarps = max(1, min(16, (227 * 1024 - 16384) // (8 * jw)))
         w(f"#define JWARPS {jwarps}")
         vblock = max(32, min(128, (100 * 1024 // (5 * S * 8)) // 32 * 32))
         w(f"#define VBLOCK {vblock}")

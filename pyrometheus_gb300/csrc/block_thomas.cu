@@ -8,12 +8,12 @@
 //   forward:  C'_0 = C_0, b'_0 = b_0,
 //             S_i = C'_i^-1 U_i,  t_i = C'_i^-1 b'_i,
 //             C'_{i+1} = C_{i+1} - L_i S_i,  b'_{i+1} = b_{i+1} - L_i t_i
-//   backward: x_{N-1} = t_{N-1},  x_i = t_i - S_i x_{i+1}
+//   backward: x_{N-1} = t_{N-1},  x_i = C'_i^-1 (b'_i - U_i x_{i+1})
 //
-// which is the reference's recurrence (its backward step re-solves with
-// C'_i; here the factor is used once and S_i, t_i are kept).  Each C'_i is
-// LU-factorised with partial pivoting, like the LAPACK getrf behind
-// jnp.linalg.solve.
+// which is the reference's recurrence.  Each C'_i is LU-factorised once
+// with partial pivoting (the LAPACK getrf behind jnp.linalg.solve); its
+// factors, pivots and b'_i are kept for the backward solve instead of
+// factorising again, as the reference does.
 //
 // Work split: one CTA per system, the working blocks (C', L, U -> S and the
 // previous S) in shared memory, threads parallel over matrix elements /
@@ -21,8 +21,8 @@
 // counter in longest-first order (LPT), so uneven lengths balance across
 // SMs in one launch.  Layout (packed, row-major blocks): system s owns rows
 // [row_off[s], row_off[s+1]) of C[rows][nv][nv], L, U (the last row's L/U
-// unused), b[rows][nv], x[rows][nv]; work holds S_i and t_i,
-// rows * (nv*nv + nv) doubles.  No waits on other CTAs; the counter is reset
+// unused), b[rows][nv], x[rows][nv]; work holds, per row, the LU factors
+// of C'_i, b'_i and the pivots: rows * (nv*nv + 2*nv) doubles.  No waits on other CTAs; the counter is reset
 // by the host before each launch.
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -30,16 +30,6 @@
 #include "pyro_common.cuh"
 
 namespace {
-
-struct BTSmem {
-  double* A;   // C'_i, then its LU factors (nv x ld)
-  double* R;   // right-hand sides: U_i | b'_i  -> S_i | t_i (nv x ld)
-  double* Lb;  // L_{i-1}
-  double* P;   // previous S | t (nv x ld)
-  int* piv;
-  int* sys;
-  int ld;      // nv + 1 (last column holds the vector)
-};
 
 __device__ __forceinline__ void load_block(double* dst, int ld,
                                            const double* __restrict__ src,
@@ -148,6 +138,101 @@ __device__ void lu_solve(const double* A, double* R, int ld, int nv,
   }
 }
 
+// One system (rows r0 .. r0+N-1): forward elimination, then the backward
+// solves with the kept factors.  All threads of the CTA take part.
+__device__ void solve_system(const double* __restrict__ Lm,
+                             const double* __restrict__ Cm,
+                             const double* __restrict__ Um,
+                             const double* __restrict__ B,
+                             double* __restrict__ X, int64_t r0, int N,
+                             int nv, double* __restrict__ work,
+                             double* smem, int* s_sing) {
+  const int ld = nv + 1;
+  double* A = smem;          // C'_i | b'_i, then LU factors | b'_i
+  double* R = A + nv * ld;   // U_i | b'_i -> S_i | t_i
+  double* Lb = R + nv * ld;  // L_{i-1}
+  double* P = Lb + nv * ld;  // S_{i-1} | t_{i-1}
+  int* piv = (int*)(P + nv * ld);
+  const int64_t wrow = (int64_t)nv * nv + 2 * nv;
+  for (int i = 0; i < N; ++i) {
+    const int64_t row = r0 + i;
+    load_block(A, ld, Cm + row * nv * nv, nv);
+    for (int j = threadIdx.x; j < nv; j += blockDim.x)
+      A[j * ld + nv] = __ldg(B + row * nv + j);  // b in column nv of A
+    if (i > 0) load_block(Lb, ld, Lm + (row - 1) * nv * nv, nv);
+    __syncthreads();
+    if (i > 0) {
+      // C' = C - L S_prev ; b' = b - L t_prev (t_prev in column nv of P)
+      for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) {
+        const int r = e / ld, c = e - (e / ld) * ld;
+        double acc = A[r * ld + c];
+        for (int k = 0; k < nv; ++k)
+          acc = fma(-Lb[r * ld + k], P[k * ld + c], acc);
+        A[r * ld + c] = acc;
+      }
+      __syncthreads();
+    }
+    // right-hand sides: U_i (if any) and b'_i
+    const bool has_u = i < N - 1;
+    if (has_u) load_block(R, ld, Um + row * nv * nv, nv);
+    for (int j = threadIdx.x; j < nv; j += blockDim.x)
+      R[j * ld + nv] = A[j * ld + nv];
+    __syncthreads();
+    lu_factor(A, ld, nv, piv, s_sing);
+    // keep the factors, b'_i and the pivots for the backward solve
+    double* w = work + row * wrow;
+    for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) {
+      const int r = e / ld, c = e - (e / ld) * ld;
+      if (c < nv)
+        w[r * nv + c] = A[e];
+      else
+        w[nv * nv + r] = A[e];
+    }
+    for (int k = threadIdx.x; k < nv; k += blockDim.x)
+      w[nv * nv + nv + k] = (double)piv[k];
+    if (has_u)
+      lu_solve(A, R, ld, nv, nv + 1, 0, piv);
+    else
+      lu_solve(A, R, ld, nv, 1, nv, piv);
+    for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) P[e] = R[e];
+    __syncthreads();
+  }
+  // backward: x_{N-1} = t_{N-1}; x_i = C'_i^-1 (b'_i - U_i x_{i+1})
+  double* xs = Lb;  // x_{i+1}
+  {
+    const int64_t row = r0 + N - 1;
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+      const double v = P[j * ld + nv];
+      X[row * nv + j] = v;
+      xs[j] = v;
+    }
+    __syncthreads();
+  }
+  for (int i = N - 2; i >= 0; --i) {
+    const int64_t row = r0 + i;
+    const double* w = work + row * wrow;
+    const double* Ui = Um + row * nv * nv;
+    for (int e = threadIdx.x; e < nv * nv; e += blockDim.x) {
+      const int r = e / nv, c = e - (e / nv) * nv;
+      A[r * ld + c] = w[e];
+    }
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+      double v = w[nv * nv + j];
+      for (int k = 0; k < nv; ++k) v = fma(-__ldg(Ui + j * nv + k), xs[k], v);
+      R[j * ld + nv] = v;
+      piv[j] = (int)w[nv * nv + nv + j];
+    }
+    __syncthreads();
+    lu_solve(A, R, ld, nv, 1, nv, piv);
+    for (int j = threadIdx.x; j < nv; j += blockDim.x) {
+      const double v = R[j * ld + nv];
+      X[row * nv + j] = v;
+      xs[j] = v;
+    }
+    __syncthreads();
+  }
+}
+
 __global__ void k_block_thomas(const double* __restrict__ Lm,
                                const double* __restrict__ Cm,
                                const double* __restrict__ Um,
@@ -159,15 +244,8 @@ __global__ void k_block_thomas(const double* __restrict__ Lm,
                                int* __restrict__ counter,
                                int* __restrict__ status) {
   extern __shared__ double smem[];
-  const int ld = nv + 1;
-  double* A = smem;
-  double* R = A + nv * ld;
-  double* Lb = R + nv * ld;
-  double* P = Lb + nv * ld;
-  int* piv = (int*)(P + nv * ld);
   __shared__ int s_sys;
   __shared__ int s_sing;
-  const int64_t wrow = (int64_t)nv * nv + nv;
   for (;;) {
     if (threadIdx.x == 0) {
       s_sys = atomicAdd(counter, 1);
@@ -179,76 +257,7 @@ __global__ void k_block_thomas(const double* __restrict__ Lm,
     const int s = order[q];
     const int64_t r0 = row_off[s];
     const int N = (int)(row_off[s + 1] - r0);
-    for (int i = 0; i < N; ++i) {
-      const int64_t row = r0 + i;
-      load_block(A, ld, Cm + row * nv * nv, nv);
-      for (int j = threadIdx.x; j < nv; j += blockDim.x)
-        A[j * ld + nv] = __ldg(B + row * nv + j);  // b in column nv of A
-      if (i > 0) load_block(Lb, ld, Lm + (row - 1) * nv * nv, nv);
-      __syncthreads();
-      if (i > 0) {
-        // C' = C - L S_prev ; b' = b - L t_prev (t_prev in column nv of P)
-        for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) {
-          const int r = e / ld, c = e - (e / ld) * ld;
-          double acc = A[r * ld + c];
-          for (int k = 0; k < nv; ++k)
-            acc = fma(-Lb[r * ld + k], P[k * ld + c], acc);
-          A[r * ld + c] = acc;
-        }
-        __syncthreads();
-      }
-      // right-hand sides: U_i (if any) and b'_i
-      const bool has_u = i < N - 1;
-      if (has_u) load_block(R, ld, Um + row * nv * nv, nv);
-      for (int j = threadIdx.x; j < nv; j += blockDim.x)
-        R[j * ld + nv] = A[j * ld + nv];
-      __syncthreads();
-      lu_factor(A, ld, nv, piv, &s_sing);
-      if (has_u)
-        lu_solve(A, R, ld, nv, nv + 1, 0, piv);
-      else
-        lu_solve(A, R, ld, nv, 1, nv, piv);
-      // keep S_i | t_i for the backward sweep and as the next P
-      double* w = work + row * wrow;
-      for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) {
-        const int r = e / ld, c = e - (e / ld) * ld;
-        const double v = R[e];
-        P[e] = v;
-        if (c < nv) {
-          if (has_u) w[r * nv + c] = v;
-        } else {
-          w[nv * nv + r] = v;
-        }
-      }
-      __syncthreads();
-    }
-    // backward sweep: x_{N-1} = t_{N-1}; x_i = t_i - S_i x_{i+1}
-    // (x_{i+1} and x_i alternate between two rows of R)
-    double* xs = R;
-    double* xn = R + ld;
-    {
-      const int64_t row = r0 + N - 1;
-      for (int j = threadIdx.x; j < nv; j += blockDim.x) {
-        const double v = P[j * ld + nv];
-        X[row * nv + j] = v;
-        xs[j] = v;
-      }
-      __syncthreads();
-    }
-    for (int i = N - 2; i >= 0; --i) {
-      const int64_t row = r0 + i;
-      const double* w = work + row * wrow;
-      for (int j = threadIdx.x; j < nv; j += blockDim.x) {
-        double v = w[nv * nv + j];
-        for (int k = 0; k < nv; ++k) v = fma(-w[j * nv + k], xs[k], v);
-        xn[j] = v;
-        X[row * nv + j] = v;
-      }
-      __syncthreads();
-      double* t = xs;
-      xs = xn;
-      xn = t;
-    }
+    solve_system(Lm, Cm, Um, B, X, r0, N, nv, work, smem, &s_sing);
     if (threadIdx.x == 0 && s_sing && status) atomicOr(status, 1);
     __syncthreads();
   }
@@ -258,7 +267,7 @@ __global__ void k_block_thomas(const double* __restrict__ Lm,
 
 // Doubles of workspace pyro_block_thomas needs for `rows` packed rows.
 PYRO_EXPORT int64_t pyro_block_thomas_work_doubles(int nv, int64_t rows) {
-  return rows * ((int64_t)nv * nv + nv);
+  return rows * ((int64_t)nv * nv + 2 * nv);
 }
 
 // Shared memory of one CTA for block size nv.
@@ -312,3 +321,4 @@ PYRO_EXPORT int pyro_block_thomas(const double* L, const double* C,
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
+

@@ -19,12 +19,17 @@
 //   mass-action dq/dc_m;
 //   chain rule through c(T, Y) and rho(T, Y), then the dT/dt row.
 //
-// k_reactor_jacobian: one warp per state.  The S x S block dw/dc lives in
-// shared memory; each lane owns whole columns (species m), walking the
-// reactions that contain m, so columns are accumulated without atomics.
-// The third-body default efficiency contributes a rank-1 term that is added
-// in the assembly instead of S entries per reaction.  The (S+1)^2 output is
-// written row by row, 32 consecutive doubles per warp store.
+// k_reactor_jacobian: one warp per state.  Lanes take reactions in an
+// order sorted by kind (k_rx_perm), so a warp's lanes run the same code
+// path.  The S x S block dw/dc is accumulated in place in the state's own
+// output block (rows/columns 1..S of its (S+1)^2 slot: L1/L2-resident while
+// the warp works on it); each lane owns whole columns (species m), walking
+// the reactions that contain m, so no atomics are needed.  The third-body
+// default efficiency contributes a rank-1 term added in the assembly
+// instead of S entries per reaction.  Shared memory holds only per-reaction
+// and per-species vectors (about 17 KB per warp at 53 species / 325
+// reactions), so about a dozen warps fit per SM.  The output is written
+// row by row, 32 consecutive doubles per warp store.
 //
 // k_reactor_vjp: one thread per state, reverse accumulation.  Each reaction
 // gets one scalar adjoint mu_r = sum_k lambda_k nu_kr, so the cost is a
@@ -253,7 +258,7 @@ __device__ __forceinline__ SpThermo species_thermo(int k, double T,
 #define JWARPS 4
 #endif
 // doubles of shared memory per warp of the Jacobian kernel
-#define JW_DOUBLES (NS * NS + 5 * NR + 10 * NS)
+#define JW_DOUBLES (5 * NR + 10 * NS)
 
 __global__ void __launch_bounds__(JWARPS * 32)
     k_reactor_jacobian(const double* __restrict__ Pp, int64_t p_inc,
@@ -263,8 +268,7 @@ __global__ void __launch_bounds__(JWARPS * 32)
   extern __shared__ double smem[];
   PEXP_PRELOAD();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* Jc = smem + (size_t)wid * JW_DOUBLES;  // Jc[k * NS + m] = dw_k/dc_m
-  double* rq = Jc + NS * NS;
+  double* rq = smem + (size_t)wid * JW_DOUBLES;
   double* rdT = rq + NR;
   double* rdM = rdT + NR;
   double* rkf = rdM + NR;
@@ -283,6 +287,10 @@ __global__ void __launch_bounds__(JWARPS * 32)
   constexpr int NC = NS + 1;
   for (int64_t i = (int64_t)blockIdx.x * JWARPS + wid; i < n;
        i += (int64_t)gridDim.x * JWARPS) {
+    double* Ji = J + i * ldj;
+    // Jc(k, m) = dw_k/dc_m, accumulated in the interior of this state's
+    // output block
+#define Jc(k, m) Ji[(int64_t)((k) + 1) * NC + (m) + 1]
     const double T = pyro_ld(Tp, t_inc, i);
     const double P = pyro_ld(Pp, p_inc, i);
     const double lnT = log(T), invT = 1.0 / T;
@@ -316,7 +324,8 @@ __global__ void __launch_bounds__(JWARPS * 32)
     s.ctot = pyro::warp_sum(ct);
     __syncwarp();
     // per reaction: q, dq/dT|c, dq/dM, kf, kr
-    for (int r = lane; r < NR; r += 32) {
+    for (int qq = lane; qq < NR; qq += 32) {
+      const int r = k_rx_perm[qq];
       const pyro::RxnDeriv d = pyro::reaction_deriv(r, s, c, g, h);
       rq[r] = d.q;
       rdT[r] = d.dqdT;
@@ -324,7 +333,8 @@ __global__ void __launch_bounds__(JWARPS * 32)
       rkf[r] = d.kf;
       rkr[r] = d.kr;
     }
-    for (int q = lane; q < NS * NS; q += 32) Jc[q] = 0.0;
+    for (int k = 0; k < NS; ++k)
+      for (int mm = lane; mm < NS; mm += 32) Jc(k, mm) = 0.0;
     __syncwarp();
     // per species: w_k, dw_k/dT|c, rank-1 third-body vector a_k
     for (int k = lane; k < NS; k += 32) {
@@ -356,11 +366,11 @@ __global__ void __launch_bounds__(JWARPS * 32)
         const int nr = k_rx_nr[r], np = k_rx_np[r];
         for (int a = 0; a < MAXSIDE; ++a) {
           if (a < nr) {
-            double& e = Jc[k_rx_sp[r][a] * NS + m];
+            double& e = Jc(k_rx_sp[r][a], m);
             e = fma(pyro::slot_nu(r, a), d, e);
           }
           if (a < np) {
-            double& e = Jc[k_rx_sp[r][MAXSIDE + a] * NS + m];
+            double& e = Jc(k_rx_sp[r][MAXSIDE + a], m);
             e = fma(pyro::slot_nu(r, MAXSIDE + a), d, e);
           }
         }
@@ -371,11 +381,11 @@ __global__ void __launch_bounds__(JWARPS * 32)
         const int nr = k_rx_nr[r], np = k_rx_np[r];
         for (int a = 0; a < MAXSIDE; ++a) {
           if (a < nr) {
-            double& e = Jc[k_rx_sp[r][a] * NS + m];
+            double& e = Jc(k_rx_sp[r][a], m);
             e = fma(pyro::slot_nu(r, a), d, e);
           }
           if (a < np) {
-            double& e = Jc[k_rx_sp[r][MAXSIDE + a] * NS + m];
+            double& e = Jc(k_rx_sp[r][MAXSIDE + a], m);
             e = fma(pyro::slot_nu(r, MAXSIDE + a), d, e);
           }
         }
@@ -384,14 +394,18 @@ __global__ void __launch_bounds__(JWARPS * 32)
     __syncwarp();
     // u_k = sum_m dw_k/dc_m c_m (with the rank-1 part), column sums of H J
     const double RT = GAS_CONSTANT * T;
-    for (int k = lane; k < NS; k += 32) {
-      double u = sa[k] * s.ctot;
-      for (int mm = 0; mm < NS; ++mm) u = fma(Jc[k * NS + mm], sc[mm], u);
-      su[k] = u;
+    // the column-owned writes above are by other lanes: make them visible
+    __threadfence_block();
+    __syncwarp();
+    for (int k = 0; k < NS; ++k) {
+      double u = 0.0;
+      for (int mm = lane; mm < NS; mm += 32) u = fma(Jc(k, mm), sc[mm], u);
+      u = pyro::warp_sum(u);
+      if (lane == 0) su[k] = fma(sa[k], s.ctot, u);
     }
     for (int jj = lane; jj < NS; jj += 32) {
       double acc = 0.0;
-      for (int k = 0; k < NS; ++k) acc = fma(sh[k], Jc[k * NS + jj], acc);
+      for (int k = 0; k < NS; ++k) acc = fma(sh[k], Jc(k, jj), acc);
       shj[jj] = RT * acc;
     }
     __syncwarp();
@@ -410,7 +424,6 @@ __global__ void __launch_bounds__(JWARPS * 32)
     const double inv_rcp = 1.0 / rcp;
     const double qr2 = Q * inv_rcp * inv_rcp;
     const double inv_sig = 1.0 / sigma;
-    double* Ji = J + i * ldj;
     // row 0: d(dT/dt)/dx
     for (int col = lane; col < NC; col += 32) {
       double v;
@@ -436,12 +449,13 @@ __global__ void __launch_bounds__(JWARPS * 32)
         } else {
           const int jj = col - 1;
           const double iw = k_inv_mw[jj];
-          v = wk_rho * ((Jc[k * NS + jj] + ak) * rho * iw +
+          v = wk_rho * ((Jc(k, jj) + ak) * rho * iw +
                         (wk - uk) * inv_sig * iw);
         }
         Ji[(int64_t)(k + 1) * NC + col] = v;
       }
     }
+#undef Jc
     __syncwarp();
   }
 }

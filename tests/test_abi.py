@@ -47,7 +47,7 @@ def test_block_thomas_library_exports_header_symbols():
     for name in declared("pyro_block_thomas.h"):
         assert hasattr(so, name), name
     so.pyro_block_thomas_work_doubles.restype = ctypes.c_int64
-    assert so.pyro_block_thomas_work_doubles(10, 7) == 7 * 110
+    assert so.pyro_block_thomas_work_doubles(10, 7) == 7 * (100 + 20)
 
 
 def test_argument_errors_without_launch():

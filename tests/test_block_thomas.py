@@ -82,10 +82,13 @@ def _residual(L, C, U, b, x):
 @pytest.mark.gpu
 @pytest.mark.parametrize("nv", [10, 54])
 def test_cuda_block_thomas_uneven_batch(nv):
-    """Against the reference algorithm on long systems: the two recurrences
-    round differently (this one keeps S_i and t_i, the reference re-solves
-    with C'_i), so the comparison is at 1e-11 on x plus a componentwise
-    backward error at the level of the reference's own."""
+    """Against the reference algorithm on long systems.  Both are
+    backward-stable but round differently (partial pivoting inside each
+    block here, LAPACK's solve there), so x agrees only to about
+    cond(A)·eps: these random systems have cond(A) of 1e4 to 3e4, which puts
+    the forward difference near 1e-11 at nv=54.  The test therefore checks
+    x at 1e-10 and the componentwise backward error at the level of the
+    reference's own."""
     _cuda()
     lengths, L, C, U, b = make_systems(37 if nv == 54 else 300, nv, 1, 200,
                                        seed=nv)
@@ -95,7 +98,7 @@ def test_cuda_block_thomas_uneven_batch(nv):
     for n in lengths:
         n = int(n)
         sl = slice(r0, r0 + n)
-        assert _rel(got[sl], ref[sl]) < 1e-11
+        assert _rel(got[sl], ref[sl]) < 1e-10
         be_got = _residual(L[sl], C[sl], U[sl], b[sl], got[sl])
         be_ref = _residual(L[sl], C[sl], U[sl], b[sl], ref[sl])
         assert be_got <= max(4.0 * be_ref, 1e-15)
