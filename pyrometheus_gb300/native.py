@@ -37,7 +37,16 @@ def build_block_thomas() -> str:
     return _build("block_thomas.cu", "block_thomas")
 
 
-BUILDERS = [build_peaks, build_mathcheck, build_runtime, build_block_thomas]
+def build_batched_lu() -> str:
+    return _build("batched_lu.cu", "batched_lu")
+
+
+def build_reactor_step() -> str:
+    return _build("reactor_step.cu", "reactor_step")
+
+
+BUILDERS = [build_peaks, build_mathcheck, build_runtime, build_block_thomas,
+            build_batched_lu, build_reactor_step]
 
 
 @lru_cache(maxsize=None)
@@ -118,4 +127,25 @@ def block_thomas_lib() -> ctypes.CDLL:
     lib.pyro_block_thomas_work_doubles.argtypes = [I, I64]
     lib.pyro_block_thomas_smem_bytes.restype = I64
     lib.pyro_block_thomas_smem_bytes.argtypes = [I]
+    return lib
+
+
+@lru_cache(maxsize=None)
+def batched_lu_lib() -> ctypes.CDLL:
+    lib = ctypes.CDLL(build_batched_lu())
+    P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    lib.pyro_batched_lu_factor.restype = I
+    lib.pyro_batched_lu_factor.argtypes = [P, P, P, I, I, P, P]
+    lib.pyro_batched_lu_solve.restype = I
+    lib.pyro_batched_lu_solve.argtypes = [P, P, P, P, I64, I64, P, I64, I64,
+                                          I, I, P]
+    return lib
+
+
+@lru_cache(maxsize=None)
+def reactor_step_lib() -> ctypes.CDLL:
+    lib = ctypes.CDLL(build_reactor_step())
+    P, I64, I = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int
+    lib.pyro_wrms_columns.restype = I
+    lib.pyro_wrms_columns.argtypes = [P, I64, P, I64, I, I64, P, P]
     return lib

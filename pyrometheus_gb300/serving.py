@@ -4,22 +4,43 @@ A request is a batch of cells -- adiabatic constant-pressure reactors
 (``Thermochemistry.get_reactor_source``) with their own initial ``T``,
 ``Y``, pressure -- to integrate to ``t_end``.  The server keeps, per
 mechanism, a fixed-capacity pool of cell slots resident in HBM (state,
-history, step sizes, Jacobian and Newton workspaces); the capacity comes
-from an HBM budget.  Between engine steps it admits queued requests into free
-slots (first fit, arrival order), so requests that arrive while others are on
-the GPU join the running batch; each engine step advances every occupied slot
-by one implicit step, and finished requests are copied back and completed.
+history, step sizes, Jacobian and factored Newton matrices); the capacity
+comes from an HBM budget.  Between engine steps it admits queued requests
+into free slots (first fit, arrival order), so requests that arrive while
+others are on the GPU join the running batch; each engine step advances
+every occupied slot by one implicit step attempt, and finished requests are
+copied back and completed.
 
-Integrator (per cell, independent of the batch): variable-step BDF2 started
-with one backward-Euler step (the reference's implicit reactor stepping,
-``examples/free_flame/time_integ.py:72-106``, uses Crank-Nicolson with a
-Newton loop and ``jnp.linalg.solve``); Newton iterations use the analytic
-Jacobian kernel and a batched LU solve (the block-Thomas kernel on
-length-one systems); weighted RMS norms with ``rtol`` / ``atol``; local
-error from the predictor-corrector difference; per-cell step acceptance and
-step-size control.  Every quantity is computed per cell with the same
-arithmetic whatever else is in the batch, so a request's result is the same
-alone and in a mix.
+Integrator (per cell, independent of the batch): variable-step BDF2
+started with one backward-Euler step.  The reference steps its implicit
+reactor with Crank-Nicolson and a full Newton loop, re-forming the
+Jacobian and calling ``jnp.linalg.solve`` each iteration
+(``examples/free_flame/time_integ.py:70-106``); here
+
+* Newton is the modified (chord) iteration: the analytic Jacobian is
+  formed at the predictor when a cell's copy is stale (admission, a Newton
+  failure, 20 accepted steps), ``M = I - gamma J`` is factorised by the
+  batched LU kernel when J or gamma changed by more than 30 %, and each
+  iteration costs one source evaluation and one solve with the kept
+  factors;
+* convergence is judged in the weighted RMS norm ``w = rtol |y_n| + atol``
+  with the contraction-rate test of the chord iteration (converged when
+  ``|dz| min(1, rate) <= 0.1``; failed when it grows, after 4 iterations,
+  or on a non-finite iterate);
+* the local error is ``(1 + w) / (3 w + 2) |z - z_pred|`` for the
+  variable-step BDF2 corrector against the quadratic Hermite predictor
+  through ``y_{n-1}, y_n, f_n`` (``w = h_n / h_{n-1}``; 1/2 with the
+  explicit-Euler predictor on the first, backward-Euler step), with the
+  step-size factor ``0.9 err^(-1/3)`` clipped to [0.2, 2] after an accepted
+  step (the ratio stays below the 1 + sqrt(2) zero-stability bound of
+  variable-step BDF2) and [0.1, 0.9] after a rejected one;
+* the first step size follows Hairer, Norsett and Wanner's starting-step
+  algorithm (Solving ODEs I, II.4) from two source evaluations.
+
+Every quantity is computed per cell with the same arithmetic whatever else
+is in the batch (element-wise tensor operations, per-cell kernels and a
+per-cell fixed-order norm), so a request's result is the same alone and in
+a mix.
 """
 
 from __future__ import annotations
@@ -27,7 +48,7 @@ from __future__ import annotations
 import ctypes
 import heapq
 import time
-from dataclasses import dataclass, field
+from dataclasses import dataclass
 from typing import Dict, List, Optional
 
 import numpy as np
@@ -69,69 +90,143 @@ class Request:
         return self.finished - self.arrival
 
 
-class ReactorPool:
-    """Device-resident slots of one mechanism and its integrator state."""
+class CudaReactorBackend:
+    """Source, Jacobian, batched LU and per-cell norms of one mechanism on
+    the GPU (the drop-in Thermochemistry class plus the batched-LU and
+    reactor-step libraries), launched on torch's current stream."""
 
-    BYTES_PER_CELL_DOUBLES = 4   # J, M, LU workspace + vectors (x nv^2)
-
-    def __init__(self, thermo, capacity: int, rtol: float = 1e-8,
-                 atol: float = 1e-14, max_newton: int = 6,
-                 h0: float = 1e-10, stream=None):
+    def __init__(self, thermo):
         self.th = thermo
-        self.S = thermo.num_species
+        self.num_species = thermo.num_species
+        self.device = thermo.device
+        self._lu = native.batched_lu_lib()
+        self._rs = native.reactor_step_lib()
+
+    @staticmethod
+    def _stream():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def source(self, p, T, Y):
+        return self.th.get_reactor_source(p, T, Y)
+
+    def jacobian(self, p, T, Y, out):
+        self.th.get_reactor_jacobian(p, T, Y, out=out)
+
+    def lu_factor(self, M, piv, mask, status):
+        n, nv = M.shape[0], M.shape[1]
+        st = self._lu.pyro_batched_lu_factor(
+            M.data_ptr(), piv.data_ptr(), mask.data_ptr(), n, nv,
+            status.data_ptr(), self._stream())
+        if st != 0:
+            raise RuntimeError(f"batched LU factorisation failed ({st})")
+
+    def lu_solve(self, M, piv, mask, rhs, out):
+        """out[:, s] = M_s^-1 rhs[:, s] for masked s (species-major)."""
+        n, nv = M.shape[0], M.shape[1]
+        st = self._lu.pyro_batched_lu_solve(
+            M.data_ptr(), piv.data_ptr(), mask.data_ptr(), rhs.data_ptr(),
+            rhs.stride(1), rhs.stride(0), out.data_ptr(), out.stride(1),
+            out.stride(0), n, nv, self._stream())
+        if st != 0:
+            raise RuntimeError(f"batched LU solve failed ({st})")
+
+    def wrms(self, v, w, out):
+        nv, n = v.shape
+        st = self._rs.pyro_wrms_columns(
+            v.data_ptr(), v.stride(0), w.data_ptr(), w.stride(0), nv, n,
+            out.data_ptr(), self._stream())
+        if st != 0:
+            raise RuntimeError(f"per-cell norm failed ({st})")
+        return out
+
+
+class ReactorPool:
+    """Device-resident slots of one mechanism and its integrator state.
+
+    *backend* supplies ``source``, ``jacobian``, ``lu_factor``,
+    ``lu_solve`` and ``wrms`` (:class:`CudaReactorBackend` for a drop-in
+    Thermochemistry object, which may be passed directly)."""
+
+    NEWTON_ITERS = 4
+    NEWTON_TOL = 0.1
+    JAC_MAX_AGE = 20
+    REFACTOR_GAMMA = 0.3
+
+    def __init__(self, backend, capacity: int, rtol: float = 1e-8,
+                 atol: float = 1e-14, max_attempts: int = 200000,
+                 stream=None):
+        if not hasattr(backend, "lu_factor"):
+            backend = CudaReactorBackend(backend)
+        self.be = backend
+        self.S = backend.num_species
         self.nv = self.S + 1
         self.cap = int(capacity)
         self.rtol, self.atol = float(rtol), float(atol)
-        self.max_newton = int(max_newton)
-        self.h0 = float(h0)
-        self.h_min = 1e-14   # relative to t_end
-        dev = thermo.device
+        self.max_attempts = int(max_attempts)
+        dev = torch.device(backend.device)
         self.device = dev
-        self.stream = stream if stream is not None else torch.cuda.Stream(
-            dev)
+        self.cuda = dev.type == "cuda"
+        if self.cuda:
+            self.stream = stream if stream is not None else \
+                torch.cuda.Stream(dev)
+        else:
+            self.stream = None
         f64 = dict(dtype=torch.float64, device=dev)
         nv, cap = self.nv, self.cap
-        with torch.cuda.stream(self.stream):
+        with self._on_stream():
             self.y = torch.zeros((nv, cap), **f64)
             self.y_prev = torch.zeros((nv, cap), **f64)
+            self.f_n = torch.zeros((nv, cap), **f64)
             self.p = torch.ones(cap, **f64)
             self.t = torch.zeros(cap, **f64)
             self.t_end = torch.zeros(cap, **f64)
-            self.h = torch.full((cap,), self.h0, **f64)
+            self.h = torch.ones(cap, **f64)
             self.h_prev = torch.ones(cap, **f64)
-            self.f_prev = torch.zeros((nv, cap), **f64)
+            self.g_lu = torch.ones(cap, **f64)
+            self.crate = torch.ones(cap, **f64)
             self.nsteps = torch.zeros(cap, dtype=torch.int64, device=dev)
+            self.nattempts = torch.zeros(cap, dtype=torch.int64, device=dev)
+            self.jage = torch.zeros(cap, dtype=torch.int64, device=dev)
+            self.jstale = torch.ones(cap, dtype=torch.bool, device=dev)
             self.active = torch.zeros(cap, dtype=torch.bool, device=dev)
             self.failed = torch.zeros(cap, dtype=torch.bool, device=dev)
-            self.J = torch.empty((cap, nv, nv), **f64)
-            self.rhs = torch.empty((cap, nv), **f64)
-            self.dx = torch.empty((cap, nv), **f64)
+            self.J = torch.zeros((cap, nv, nv), **f64)
+            self.M = torch.zeros((cap, nv, nv), **f64)
+            self.piv = torch.zeros((cap, nv), dtype=torch.int32, device=dev)
             self.eye = torch.eye(nv, **f64)
-            self.row_off = torch.arange(cap + 1, dtype=torch.int64,
-                                        device=dev)
-            self.order = torch.arange(cap, dtype=torch.int32, device=dev)
-            lib = native.block_thomas_lib()
-            wd = int(lib.pyro_block_thomas_work_doubles(nv, cap))
-            self.work = torch.empty(wd, **f64)
-            self.counter = torch.zeros(1, dtype=torch.int32, device=dev)
             self.lu_status = torch.zeros(1, dtype=torch.int32, device=dev)
-        self.lu = lib
-        from .flamelet import default_threads
-        self.lu_threads = default_threads(nv)
+            self._norm = torch.empty(cap, **f64)
         self.free = list(range(cap))
         heapq.heapify(self.free)
         self.high_water = 0
         self.slot_req = np.full(cap, -1, dtype=np.int64)
         self.n_active = 0
+        self._done = None
+        self.engine_steps = 0
 
     @classmethod
     def bytes_per_cell(cls, n_species: int) -> int:
+        """Device bytes one slot holds (J and the factored M, state,
+        history and per-cell scalars)."""
         nv = n_species + 1
-        return 8 * (3 * nv * nv + 8 * nv + 12)
+        return 8 * (2 * nv * nv + 3 * nv + 8) + 4 * nv + 3 * 8 + 3
+
+    def _on_stream(self):
+        if self.cuda:
+            return torch.cuda.stream(self.stream)
+        import contextlib
+        return contextlib.nullcontext()
+
+    def synchronize(self):
+        if self.cuda:
+            self.stream.synchronize()
 
     # -- slots -----------------------------------------------------------
     def can_admit(self, n: int) -> bool:
         return len(self.free) >= n
+
+    def _norm_of(self, v, w):
+        return self.be.wrms(v, w, self._norm[:v.shape[1]]).clone()
 
     def admit(self, req: Request) -> np.ndarray:
         slots = np.array([heapq.heappop(self.free) for _ in range(req.n)],
@@ -139,24 +234,53 @@ class ReactorPool:
         self.high_water = max(self.high_water, int(slots.max()) + 1)
         self.slot_req[slots] = req.rid
         idx = torch.as_tensor(slots, device=self.device)
-        with torch.cuda.stream(self.stream):
+        with self._on_stream():
             y0 = torch.empty((self.nv, req.n), dtype=torch.float64)
             y0[0] = torch.from_numpy(np.asarray(req.T0, dtype=np.float64))
             y0[1:] = torch.from_numpy(np.asarray(req.Y0, dtype=np.float64))
-            y0 = y0.to(self.device, non_blocking=False)
+            y0 = y0.to(self.device)
+            p = torch.full((req.n,), float(req.pressure), dtype=torch.float64,
+                           device=self.device)
+            h0, f0 = self._initial_step(p, y0, float(req.t_end))
             self.y[:, idx] = y0
             self.y_prev[:, idx] = y0
-            self.p[idx] = float(req.pressure)
+            self.f_n[:, idx] = f0
+            self.p[idx] = p
             self.t[idx] = 0.0
             self.t_end[idx] = float(req.t_end)
-            self.h[idx] = min(self.h0, float(req.t_end))
-            self.h_prev[idx] = 1.0
+            self.h[idx] = h0
+            self.h_prev[idx] = h0
+            self.g_lu[idx] = 1.0
+            self.crate[idx] = 1.0
             self.nsteps[idx] = 0
-            self.f_prev[:, idx] = 0.0
+            self.nattempts[idx] = 0
+            self.jage[idx] = 0
+            self.jstale[idx] = True
             self.failed[idx] = False
             self.active[idx] = True
         self.n_active += req.n
         return slots
+
+    def _initial_step(self, p, y0, t_end):
+        """Starting step of Hairer, Norsett and Wanner (Solving ODEs I,
+        II.4) for a first-order start, per cell."""
+        w = self.rtol * y0.abs() + self.atol
+        f0 = self.be.source(p, y0[0], y0[1:])
+        d0 = self._norm_of(y0, w)
+        d1 = self._norm_of(f0, w)
+        h_a = torch.where((d0 < 1e-5) | (d1 < 1e-5),
+                          torch.full_like(d0, 1e-6), 0.01 * d0 / d1)
+        h_a = torch.clamp(h_a, max=t_end)
+        y1 = y0 + h_a * f0
+        f1 = self.be.source(p, y1[0], y1[1:])
+        d2 = self._norm_of(f1 - f0, w) / h_a
+        dm = torch.maximum(d1, d2)
+        h_b = torch.where(dm > 1e-15, torch.sqrt(0.01 / dm),
+                          torch.clamp(h_a * 1e-3, min=1e-6))
+        h0 = torch.minimum(100.0 * h_a, h_b)
+        h0 = torch.where(torch.isfinite(h0) & (h0 > 0), h0,
+                         torch.full_like(h0, 1e-12 * t_end))
+        return torch.clamp(h0, max=t_end), f0
 
     def release(self, slots: np.ndarray):
         for s in slots.tolist():
@@ -167,101 +291,137 @@ class ReactorPool:
         self.high_water = int(occupied.max()) + 1 if occupied.size else 0
 
     # -- numerics --------------------------------------------------------
-    def _wrms(self, v, ref):
-        w = self.rtol * ref.abs() + self.atol
-        return torch.sqrt(((v / w) ** 2).mean(dim=0))
-
-    def _lu_solve(self, n):
-        """rhs[:n] <- M[:n]^-1 rhs[:n] (M in self.J, factorised in place
-        in the workspace)."""
-        st = self.lu.pyro_block_thomas(
-            self.J.data_ptr(), self.J.data_ptr(), self.J.data_ptr(),
-            self.rhs.data_ptr(), self.dx.data_ptr(),
-            self.row_off.data_ptr(), self.order.data_ptr(), int(n), self.nv,
-            self.work.data_ptr(), self.counter.data_ptr(),
-            self.lu_status.data_ptr(), self.lu_threads, 0,
-            ctypes.c_void_p(self.stream.cuda_stream))
-        if st != 0:
-            raise RuntimeError(f"batched LU failed (status {st})")
-
     def step(self):
         """One implicit step attempt for every occupied slot (asynchronous
-        on the pool's stream)."""
+        on the pool's stream, apart from the host reading which cells need
+        a Jacobian or a factorisation and whether Newton is done)."""
         n = self.high_water
         if n == 0:
             return
-        th = self.th
-        with torch.cuda.stream(self.stream):
+        be = self.be
+        self.engine_steps += 1
+        with self._on_stream():
             act = self.active[:n]
-            y, yp = self.y[:, :n], self.y_prev[:, :n]
-            t, te = self.t[:n], self.t_end[:n]
-            h = torch.minimum(self.h[:n], te - t)
-            h = torch.where(act, h, torch.ones_like(h))
+            y, yp, fn = self.y[:, :n], self.y_prev[:, :n], self.f_n[:, :n]
+            t, te, hp = self.t[:n], self.t_end[:n], self.h_prev[:n]
+            h = torch.where(act, torch.minimum(self.h[:n], te - t),
+                            torch.ones_like(t))
             first = self.nsteps[:n] == 0
-            hp = self.h_prev[:n]
             om = torch.where(first, torch.zeros_like(h), h / hp)
             den = 1.0 + 2.0 * om
-            ca = (1.0 + om) ** 2 / den
-            cb = -(om * om) / den
-            gh = (1.0 + om) / den * h
-            base = ca * y + cb * yp
-            # predictor: quadratic through y_{n-1}, y_n with slope f_n
-            fp = self.f_prev[:, :n]
-            cq = (yp - y + fp * hp) / (hp * hp)
-            zp = torch.where(first, y, y + h * (fp + cq * h))
-            z = zp.clone()
+            gam = (1.0 + om) / den * h
+            base = ((1.0 + om) ** 2 / den) * y - (om * om / den) * yp
+            cq = torch.where(first, torch.zeros_like(h),
+                             (yp - y + fn * hp) / (hp * hp))
+            zp = y + h * (fn + cq * h)
+            w = self.rtol * y.abs() + self.atol
             p = self.p[:n]
+
+            # Jacobian at the predictor for stale cells, then M = I - gam J
+            need_j = act & self.jstale[:n]
+            jidx = torch.nonzero(need_j).flatten()
+            if jidx.numel():
+                zj = zp[:, jidx]
+                jt = torch.empty((jidx.numel(), self.nv, self.nv),
+                                 dtype=torch.float64, device=self.device)
+                be.jacobian(p[jidx], zj[0], zj[1:], jt)
+                self.J[jidx] = jt
+                self.jstale[jidx] = False
+                self.jage[jidx] = 0
+            refac = need_j | (act & ((gam / self.g_lu[:n] - 1.0).abs()
+                                     > self.REFACTOR_GAMMA))
+            ridx = torch.nonzero(refac).flatten()
+            if ridx.numel():
+                self.M[ridx] = self.eye - gam[ridx, None, None] * self.J[ridx]
+                self.g_lu[ridx] = gam[ridx]
+                be.lu_factor(self.M[:n], self.piv[:n],
+                             refac.to(torch.uint8), self.lu_status)
+
+            # chord Newton
+            z = zp.clone()
             conv = ~act
-            f = fp
-            for _ in range(self.max_newton):
-                f = th.get_reactor_source(p, z[0], z[1:])
-                J = self.J[:n]
-                th.get_reactor_jacobian(p, z[0], z[1:], out=J)
-                # M = I - gamma h J ; G = z - base - gamma h f ; frozen
-                # (converged / idle) cells solve I dx = 0
-                live = ~conv
-                J.mul_(-gh[:, None, None]).add_(self.eye)
-                J[~live] = self.eye
-                g = z - base - gh * f
-                g = torch.where(live, g, torch.zeros_like(g))
-                self.rhs[:n] = g.T
-                self._lu_solve(n)
-                dz = self.dx[:n].T
+            fail = torch.zeros_like(act)
+            crate = self.crate[:n].clone()
+            del_prev = torch.ones_like(h)
+            dz = torch.zeros_like(z)
+            for k in range(self.NEWTON_ITERS):
+                live = act & ~conv & ~fail
+                if k > 0 and not bool(live.any()):
+                    break
+                f = be.source(p, z[0], z[1:])
+                g = torch.where(live, z - base - gam * f,
+                                torch.zeros_like(z))
+                be.lu_solve(self.M[:n], self.piv[:n], live.to(torch.uint8),
+                            g, dz)
+                dz = torch.where(live, dz, torch.zeros_like(dz))
                 z = z - dz
-                conv = conv | (self._wrms(dz, z) < 1e-3)
-            # BDF2 local error ~ 2 (z - z_pred) for the Hermite predictor
-            # (constant-step error constants -2/9 and -1/3 of h^3 y^(3));
-            # the first (backward-Euler) step is accepted on convergence
-            err = 2.0 * self._wrms(z - zp, z)
-            err = torch.where(first, torch.zeros_like(err), err)
-            ok = act & conv & torch.isfinite(err) & (err <= 1.0)
-            self.f_prev[:, :n] = torch.where(ok, f, fp)
+                dl = self._norm_of(dz, w)
+                if k > 0:
+                    crate = torch.where(
+                        live, torch.maximum(0.3 * crate, dl / del_prev),
+                        crate)
+                ok_k = live & (dl * torch.clamp(crate, max=1.0)
+                               <= self.NEWTON_TOL)
+                bad = live & (~torch.isfinite(z).all(dim=0)
+                              | ~torch.isfinite(dl))
+                if k > 0:
+                    bad = bad | (live & (dl > 2.0 * del_prev))
+                fail = fail | bad
+                conv = conv | (ok_k & ~bad)
+                del_prev = torch.where(live, dl, del_prev)
+            fail = fail | (act & ~conv)
+            conv = conv & act & ~fail
+
+            # local error and acceptance
+            cerr = torch.where(first, torch.full_like(om, 0.5),
+                               (1.0 + om) / (3.0 * om + 2.0))
+            err = cerr * self._norm_of(z - zp, w)
+            ok = conv & torch.isfinite(err) & (err <= 1.0)
+            rej = conv & ~ok
+            f_new = (z - base) / gam
             self.y_prev[:, :n] = torch.where(ok, y, yp)
             self.y[:, :n] = torch.where(ok, z, y)
+            self.f_n[:, :n] = torch.where(ok, f_new, fn)
             self.t[:n] = torch.where(ok, t + h, t)
-            self.h_prev[:n] = torch.where(ok, h, self.h_prev[:n])
+            self.h_prev[:n] = torch.where(ok, h, hp)
             self.nsteps[:n] += ok.to(torch.int64)
-            fac = torch.clamp(0.9 * torch.pow(torch.clamp(err, min=1e-12),
-                                              -1.0 / 3.0), 0.2, 4.0)
-            fac = torch.where(conv, fac, torch.full_like(fac, 0.25))
+            self.nattempts[:n] += act.to(torch.int64)
+            self.crate[:n] = torch.where(ok, crate, torch.ones_like(crate))
+            jage = self.jage[:n] + ok.to(torch.int64)
+            self.jage[:n] = jage
+            # Newton failure: retry with a fresh Jacobian if it was old,
+            # otherwise with a quarter of the step
+            nfail = act & fail
+            self.jstale[:n] |= nfail | (ok & (jage >= self.JAC_MAX_AGE))
+            e = torch.clamp(err, min=1e-10)
+            fac = torch.where(
+                ok, torch.clamp(0.9 * e ** (-1.0 / 3.0), 0.2, 2.0),
+                torch.where(rej, torch.clamp(0.9 * e ** (-1.0 / 3.0), 0.1,
+                                             0.9),
+                            torch.where(nfail & ~need_j,
+                                        torch.ones_like(e),
+                                        torch.full_like(e, 0.25))))
             fac = torch.where(torch.isfinite(fac), fac,
                               torch.full_like(fac, 0.25))
             hn = torch.where(act, h * fac, self.h[:n])
             self.h[:n] = hn
-            # a cell whose step collapses (or whose state is not finite)
-            # fails instead of spinning: it leaves the batch with a flag
-            bad = act & ((hn < self.h_min * te) |
-                         ~torch.isfinite(self.y[:, :n]).all(dim=0))
+            # a cell whose step underflows its time, whose state is not
+            # finite, or that exceeds the attempt limit fails alone
+            tn = self.t[:n]
+            stuck = (tn + hn == tn) & (tn > 0)
+            bad = act & (stuck | (hn < 1e-30)
+                         | (self.nattempts[:n] > self.max_attempts)
+                         | ~torch.isfinite(self.y[:, :n]).all(dim=0))
             self.failed[:n] |= bad
-            done = act & ((self.t[:n] >= te * (1.0 - 1e-12)) | bad)
+            done = act & ((tn >= te * (1.0 - 1e-12)) | bad)
             self.active[:n] = act & ~done
             self._done = done
 
     def finished_slots(self) -> np.ndarray:
         """Slots that completed in the last step (synchronises)."""
-        if self.high_water == 0 or getattr(self, "_done", None) is None:
+        if self.high_water == 0 or self._done is None:
             return np.zeros(0, dtype=np.int64)
-        self.stream.synchronize()
+        self.synchronize()
         fin = np.nonzero(self._done.cpu().numpy())[0]
         self._done = None
         return fin
@@ -269,22 +429,22 @@ class ReactorPool:
     def results(self, slots: np.ndarray):
         """(T[n], Y[S, n], steps[n], failed[n]) of the given slots."""
         idx = torch.as_tensor(slots, device=self.device)
-        with torch.cuda.stream(self.stream):
+        with self._on_stream():
             yv = self.y[:, idx].cpu().numpy()
             ns = self.nsteps[idx].cpu().numpy()
             fl = self.failed[idx].cpu().numpy()
         return yv[0], yv[1:], ns, fl
 
     def deactivate(self, slots: np.ndarray):
-        with torch.cuda.stream(self.stream):
+        with self._on_stream():
             self.active[torch.as_tensor(slots, device=self.device)] = False
-        self.stream.synchronize()
+        self.synchronize()
 
     def reset(self):
         """Drop every cell (after a failed engine step)."""
-        with torch.cuda.stream(self.stream):
+        with self._on_stream():
             self.active.zero_()
-        self.stream.synchronize()
+        self.synchronize()
         self.free = list(range(self.cap))
         heapq.heapify(self.free)
         self.slot_req[:] = -1

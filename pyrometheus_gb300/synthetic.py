@@ -23,7 +23,15 @@ reactions), generated here from a seed:
   ``Ea ~ U[0, 60]`` kcal/mol.  One reaction in eight (and every falloff
   low-pressure limit with probability 1/2) gets ``Ea = 0`` so the
   ``A*T**b`` branch of the reference (``chem_expr.py:319-321``) is
-  exercised.
+  exercised;
+* orientation: with ``orient_temperature`` set (the benchmark mechanisms use
+  1500 K), each reaction is written in the direction whose standard Gibbs
+  energy change at that temperature is negative.  The random formation
+  enthalpies span about 1e5 R, so a reaction written uphill has an
+  equilibrium constant near e^-100 and a reverse rate coefficient
+  ``k_f / K_c`` tens of decades above any forward one; a 0-D reactor on
+  such a mechanism has time scales below 1e-30 s and cannot be integrated.
+  Written downhill, ``k_r`` stays within a few decades of ``k_f``.
 
 States: ``T ~ U[300, 3000]`` K, ``p`` log-uniform in [1e4, 1e6] Pa and
 ``Y = 0.6 e_N2 + 0.4 Dirichlet(0.5)`` (the "N2 floor of 0.6").
@@ -209,11 +217,22 @@ def _pick(rng, n_avail: int, n_want: int) -> np.ndarray:
     return np.concatenate(picks)
 
 
+def _gibbs_rt(thermo: NasaPoly2, t: float) -> float:
+    """g/RT of one species from its NASA-7 fit."""
+    a = thermo.high if t > thermo.t_mid else thermo.low
+    h_rt = (a[0] + a[1] * t / 2 + a[2] * t ** 2 / 3 + a[3] * t ** 3 / 4
+            + a[4] * t ** 4 / 5 + a[5] / t)
+    s_r = (a[0] * np.log(t) + a[1] * t + a[2] * t ** 2 / 2
+           + a[3] * t ** 3 / 3 + a[4] * t ** 4 / 4 + a[6])
+    return float(h_rt - s_r)
+
+
 def make_mechanism(species_names: Sequence[str], n_reactions: int,
                    n_three_body: int, n_troe: int, n_lindemann: int = 0,
                    seed: int = 0, irreversible_fraction: float = 0.0,
                    inert: Sequence[str] = ("AR",),
-                   name: str = "synthetic") -> Solution:
+                   name: str = "synthetic",
+                   orient_temperature: Optional[float] = None) -> Solution:
     """Seeded synthetic mechanism (see the module docstring)."""
     rng = np.random.default_rng(seed)
     names = list(species_names)
@@ -221,6 +240,17 @@ def make_mechanism(species_names: Sequence[str], n_reactions: int,
     species = []
     for n, c in zip(names, comps):
         species.append(Species(n, c, _nasa_fit(rng, int(sum(c.values())))))
+    g_rt = {sp.name: (_gibbs_rt(sp.thermo, orient_temperature)
+                      if orient_temperature else 0.0) for sp in species}
+
+    def downhill(reac, prod):
+        """(reac, prod) swapped if the reaction is uphill in g at the
+        orientation temperature."""
+        if orient_temperature is None:
+            return reac, prod
+        dg = (sum(v * g_rt[k] for k, v in prod.items())
+              - sum(v * g_rt[k] for k, v in reac.items()))
+        return (prod, reac) if dg > 0 else (reac, prod)
     elements = []
     for c in comps:
         for el in c:
@@ -259,6 +289,7 @@ def make_mechanism(species_names: Sequence[str], n_reactions: int,
             reac, prod = spec([a]), spec([b, c])
         else:
             reac, prod = spec([b, c]), spec([a])
+        reac, prod = downhill(reac, prod)
         order = sum(reac.values())
         eff = _efficiencies(rng, names)
         if kind == "three-body":
@@ -284,7 +315,7 @@ def make_mechanism(species_names: Sequence[str], n_reactions: int,
                                       ThirdBody(eff, 1.0)))
     for ei in e_pick:
         p, q = exch[ei]
-        reac, prod = spec(p), spec(q)
+        reac, prod = downhill(spec(p), spec(q))
         reversible = not (rng.random() < irreversible_fraction)
         arrow = "<=>" if reversible else "=>"
         eq = f"{_side(reac)} {arrow} {_side(prod)}"
@@ -308,16 +339,16 @@ def make_mechanism(species_names: Sequence[str], n_reactions: int,
 
 def config1_mechanism(seed: int = 1) -> Solution:
     """9 species (H, O, N, Ar) / 24 reversible reactions: 3 three-body,
-    2 Troe falloff, 19 elementary."""
+    2 Troe falloff, 19 elementary; written downhill at 1500 K."""
     return make_mechanism(SPECIES_9, 24, 3, 2, 0, seed=seed,
-                          name="synthetic9")
+                          name="synthetic9", orient_temperature=1500.0)
 
 
 def config2_mechanism(seed: int = 2) -> Solution:
     """53 species (C, H, O, N, Ar) / 325 reactions: 30 three-body, 25 Troe,
-    3 Lindemann, 267 elementary."""
+    3 Lindemann, 267 elementary; written downhill at 1500 K."""
     return make_mechanism(SPECIES_53, 325, 30, 25, 3, seed=seed,
-                          name="synthetic53")
+                          name="synthetic53", orient_temperature=1500.0)
 
 # }}}
 

@@ -50,6 +50,31 @@ def test_block_thomas_library_exports_header_symbols():
     assert so.pyro_block_thomas_work_doubles(10, 7) == 7 * (100 + 20)
 
 
+@pytest.mark.parametrize("header,builder", [
+    ("pyro_batched_lu.h", "build_batched_lu"),
+    ("pyro_reactor_step.h", "build_reactor_step")])
+def test_integrator_libraries_export_header_symbols(header, builder):
+    from pyrometheus_gb300 import native
+    so = ctypes.CDLL(getattr(native, builder)())
+    names = declared(header)
+    assert names
+    for name in names:
+        assert hasattr(so, name), name
+
+
+def test_batched_lu_argument_errors_without_launch():
+    from pyrometheus_gb300 import native
+    lib = native.batched_lu_lib()
+    assert lib.pyro_batched_lu_factor(None, None, None, -1, 4, None,
+                                      None) == 1
+    assert lib.pyro_batched_lu_factor(None, None, None, 3, 65, None,
+                                      None) == 1
+    assert lib.pyro_batched_lu_factor(None, None, None, 0, 4, None,
+                                      None) == 0
+    assert lib.pyro_batched_lu_solve(1, 1, None, None, 4, 1, 1, 4, 1, 2, 4,
+                                     None) == 1
+
+
 def test_argument_errors_without_launch():
     """Argument checks happen before any CUDA call, so they run without a
     GPU: a negative size or a short leading dimension is rejected."""
