@@ -42,6 +42,34 @@ int pyro_block_thomas(const double* L, const double* C, const double* U,
                       int* counter, int* status, int threads, int ctas,
                       cudaStream_t stream);
 
+/* No counterpart in the reference (its block_thomas allocates through JAX
+ * on every call).  For callers that cannot allocate device memory when they
+ * solve: host applications that hand all device memory to their own pool at
+ * start-up and forbid allocation inside a time step (a flow solver's
+ * implicit chemistry update), and real-time loops where the latency or a
+ * failure of an allocation in the middle of a step is not acceptable.  Same
+ * inputs and outputs as
+ * pyro_block_thomas, but the per-row workspace and the work counter live in
+ * a static device array of the library (16 MiB, held on every GPU that loads
+ * the library until the process exits), so the call allocates nothing.
+ * Limit: total_rows (= row_off[nsys], passed from the host) at most
+ * pyro_block_thomas_noalloc_max_rows(nv) = 2^21 / (nv*nv + 2*nv) rows
+ * (17,476 at nv = 10, 693 at nv = 54); larger requests return
+ * PYRO_ERR_CAPACITY (5) before anything is launched.  status: bit 0 zero
+ * pivot, bit 1 a system's rows outside [0, total_rows).  All calls share
+ * the array and it keeps the last call's contents (the counter is cleared
+ * by each call, the workspace is written before it is read): calls whose
+ * executions overlap on the GPU race and must not be issued.  The first
+ * call on a device looks up the array's address with that device current;
+ * make that first call before any stream capture. */
+int64_t pyro_block_thomas_noalloc_max_rows(int nv);
+int pyro_block_thomas_noalloc(const double* L, const double* C,
+                              const double* U, const double* b, double* x,
+                              const int64_t* row_off, const int* order,
+                              int nsys, int nv, int64_t total_rows,
+                              int* status, int threads, int ctas,
+                              cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

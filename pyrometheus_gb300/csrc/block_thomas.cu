@@ -322,3 +322,161 @@ PYRO_EXPORT int pyro_block_thomas(const double* L, const double* C,
   return PYRO_OK;
 }
 
+// ------------------------------------------------------------------------
+// No-allocation variant.
+//
+// Some callers cannot allocate device memory at the point where they need a
+// solve: host applications that hand all device memory to their own pool at
+// start-up and forbid allocation inside a time step (for example a flow
+// solver's implicit chemistry update), and real-time loops where the
+// latency or a failure of an allocation in the middle of a step is not
+// acceptable.  For them,
+// pyro_block_thomas_noalloc takes the same inputs and outputs as
+// pyro_block_thomas but keeps its scratch -- the per-row factor workspace
+// and the work counter -- in the file-scope array below, so the
+// call allocates nothing.
+//
+// Limits and sharing: the array holds PYRO_BT_STATIC_DOUBLES doubles
+// (16 MiB), i.e. pyro_block_thomas_noalloc_max_rows(nv) packed rows
+// (17,476 rows at nv = 10, 693 at nv = 54); every GPU that loads the
+// library holds it until the process exits.  All calls share it and it
+// keeps the last call's contents (the counter is cleared by every call;
+// the workspace is written before it is read), so calls whose executions
+// overlap on the GPU -- on different streams, or from different host
+// threads -- race and must not be issued.  The first call on a device
+// looks up the array's device address (cudaGetSymbolAddress, with that
+// device current); make that first call before any stream capture.
+// ------------------------------------------------------------------------
+
+#include <mutex>
+
+#define PYRO_BT_STATIC_DOUBLES (1 << 21)
+#define PYRO_BT_MAX_DEVICES 64
+
+// workspace, then 32 doubles (256 bytes) whose first int is the counter
+static __device__ __align__(256) double
+    pyro_bt_static_scratch[PYRO_BT_STATIC_DOUBLES + 32];
+
+namespace {
+
+std::mutex g_bt_static_mu;
+double* g_bt_static_ptr[PYRO_BT_MAX_DEVICES] = {nullptr};
+
+// Device address of the static scratch on the current device (looked up
+// once per device).
+int bt_static_scratch(double** out) {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 ||
+      dev >= PYRO_BT_MAX_DEVICES) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  std::lock_guard<std::mutex> lock(g_bt_static_mu);
+  if (g_bt_static_ptr[dev] == nullptr) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, pyro_bt_static_scratch) != cudaSuccess ||
+        p == nullptr) {
+      (void)cudaGetLastError();
+      return PYRO_ERR_LAUNCH;
+    }
+    g_bt_static_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_bt_static_ptr[dev];
+  return PYRO_OK;
+}
+
+// k_block_thomas with a bound on the rows it may touch in `work`: a system
+// whose rows fall outside [0, cap_rows) is skipped and flagged (status
+// bit 1) instead of writing past the static scratch.
+__global__ void k_block_thomas_capped(
+    const double* __restrict__ Lm, const double* __restrict__ Cm,
+    const double* __restrict__ Um, const double* __restrict__ B,
+    double* __restrict__ X, const int64_t* __restrict__ row_off,
+    const int* __restrict__ order, int nsys, int nv,
+    double* __restrict__ work, int64_t cap_rows, int* __restrict__ counter,
+    int* __restrict__ status) {
+  extern __shared__ double smem[];
+  __shared__ int s_sys;
+  __shared__ int s_sing;
+  for (;;) {
+    if (threadIdx.x == 0) {
+      s_sys = atomicAdd(counter, 1);
+      s_sing = 0;
+    }
+    __syncthreads();
+    const int q = s_sys;
+    if (q >= nsys) break;
+    const int s = order[q];
+    const int64_t r0 = row_off[s];
+    const int64_t r1 = row_off[s + 1];
+    if (r0 < 0 || r1 <= r0 || r1 > cap_rows) {
+      if (threadIdx.x == 0 && status) atomicOr(status, 2);
+      __syncthreads();
+      continue;
+    }
+    solve_system(Lm, Cm, Um, B, X, r0, (int)(r1 - r0), nv, work, smem,
+                 &s_sing);
+    if (threadIdx.x == 0 && s_sing && status) atomicOr(status, 1);
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+// Rows of the static scratch for blocks of size nv (0 for nv out of range).
+PYRO_EXPORT int64_t pyro_block_thomas_noalloc_max_rows(int nv) {
+  if (nv < 1 || nv > 64) return 0;
+  return (int64_t)PYRO_BT_STATIC_DOUBLES / ((int64_t)nv * nv + 2 * nv);
+}
+
+// pyro_block_thomas without a caller workspace or counter: scratch in the
+// library's static device array (see above).  total_rows: row_off[nsys]
+// (host value); more than pyro_block_thomas_noalloc_max_rows(nv) returns
+// PYRO_ERR_CAPACITY before anything is launched.  status: as for
+// pyro_block_thomas, plus bit 1 if a system's rows lie outside
+// [0, total_rows].  Allocates nothing; asynchronous on `stream`.
+PYRO_EXPORT int pyro_block_thomas_noalloc(
+    const double* L, const double* C, const double* U, const double* b,
+    double* x, const int64_t* row_off, const int* order, int nsys, int nv,
+    int64_t total_rows, int* status, int threads, int ctas,
+    cudaStream_t stream) {
+  if (nsys < 0 || nv < 1 || nv > 64 || threads < 32 || threads > 1024 ||
+      threads % 32 || total_rows < 0)
+    return PYRO_ERR_ARGUMENT;
+  if (total_rows > pyro_block_thomas_noalloc_max_rows(nv))
+    return PYRO_ERR_CAPACITY;
+  if (nsys == 0) return PYRO_OK;
+  if (!L || !C || !U || !b || !x || !row_off || !order)
+    return PYRO_ERR_ARGUMENT;
+  double* scratch = nullptr;
+  if (bt_static_scratch(&scratch) != PYRO_OK) return PYRO_ERR_LAUNCH;
+  int* counter = reinterpret_cast<int*>(scratch + PYRO_BT_STATIC_DOUBLES);
+  const size_t smem = (size_t)pyro_block_thomas_smem_bytes(nv);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute((const void*)k_block_thomas_capped,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  if (ctas <= 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_block_thomas_capped, threads, smem) != cudaSuccess ||
+        per_sm < 1) {
+      (void)cudaGetLastError();
+      per_sm = 1;
+    }
+    ctas = per_sm * pyro_sm_count();
+  }
+  if (ctas > nsys) ctas = nsys;
+  if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  k_block_thomas_capped<<<ctas, threads, smem, stream>>>(
+      L, C, U, b, x, row_off, order, nsys, nv, scratch, total_rows, counter,
+      status);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}

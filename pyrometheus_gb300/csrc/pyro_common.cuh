@@ -23,6 +23,7 @@ enum PyroStatus : int {
   PYRO_ERR_LAUNCH = 2,        // a CUDA launch or runtime call failed
   PYRO_ERR_NOT_CONVERGED = 3, // some states' Newton iteration failed
   PYRO_ERR_UNSUPPORTED = 4,   // option not supported for this mechanism
+  PYRO_ERR_CAPACITY = 5,      // request larger than a fixed static scratch
 };
 
 #define PYRO_CHECK_LAUNCH()                                   \
