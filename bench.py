@@ -347,7 +347,8 @@ def secondary_legs(sol, th, dev, dfma):
             "fp64_tflops": flops / ms / 1e9,
             "fp64_frac": flops / ms / 1e9 / (dfma / 1e12),
             "hbm_gbs": rows * (5 * nv * nv + 4 * nv) * 8 / ms / 1e6,
-            "threads_per_system": solver.threads, "cuda_graph": True}
+            "kernel": solver.kernel, "threads": solver.threads,
+            "cuda_graph": True}
         del C, L, U, b, solver
     out["block_thomas"] = bt
     torch.cuda.empty_cache()

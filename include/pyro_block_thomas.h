@@ -42,6 +42,19 @@ int pyro_block_thomas(const double* L, const double* C, const double* U,
                       int* counter, int* status, int threads, int ctas,
                       cudaStream_t stream);
 
+/* pyro_block_thomas for blocks of size nv <= 16 with one thread per system
+ * (the whole recurrence of a system runs in one thread, so every FP64
+ * instruction of a warp does 32 useful operations).  Same arguments and
+ * workspace as pyro_block_thomas without the counter and the grid size;
+ * threads: systems per CTA, 32 or 64 (64 needs 3*nv*(nv+1)*8*64 bytes of
+ * shared memory to fit in 227 KB).  Replaces the same reference function,
+ * pyrometheus/flamelets/linear_solver.py:6-103. */
+int pyro_block_thomas_small(const double* L, const double* C, const double* U,
+                            const double* b, double* x,
+                            const int64_t* row_off, const int* order,
+                            int nsys, int nv, double* work, int* status,
+                            int threads, cudaStream_t stream);
+
 /* No counterpart in the reference (its block_thomas allocates through JAX
  * on every call).  For callers that cannot allocate device memory when they
  * solve: host applications that hand all device memory to their own pool at

@@ -248,6 +248,173 @@ class _Emitter:
         self.block = int(opts.block_size) if opts.block_size else \
             _default_block(self.m.S)
 
+    def _jacobian_tables(self, perm, flags, rates, dnu, defeff, tb_start,
+                         tb_idx, tb_de, fo_slot, fo_form, fo_low,
+                         fo_troe) -> List[str]:
+        """Tables of the warp-per-state Jacobian kernel (jacobian.cuh).
+
+        The lanes of a warp index these with different reactions or
+        species, so they live in global memory (read through L1 with
+        ``__ldg``) rather than in constant memory, whose cache serialises
+        divergent indices.  Reactions are renumbered in ``perm`` order
+        (grouped by kind); every reaction's species occupy consecutive
+        "slots" (reactants, then products), and the S x S block of
+        dw/dc is built from an update list: entry (output offset, source,
+        coefficient) adds coefficient * D[source] into one element, where
+        D holds per slot the partial derivative of the rate of progress
+        with respect to that slot's concentration and, after the slots, the
+        third-body derivative of each reaction.  Entries are sorted by
+        output element and split into 32 contiguous, equally long runs, one
+        per lane, so each element is summed by one lane in a fixed order
+        and stored once (no atomics, no divergent trip counts); elements
+        without contributions get one entry from a zero source."""
+        m = self.m
+        S, R = m.S, m.R
+        nc = S + 1
+        qual = "__device__"
+        slot0, sp, ex, nu, srx, sanu = [0], [], [], [], [], []
+        q_nr = []
+        for qq, j in enumerate(perm):
+            r = m.rx[j]
+            q_nr.append(len(r.fwd))
+            for (k, e) in r.fwd:
+                sp.append(k)
+                ex.append(e)
+                nu.append(-r.nu_r.get(k, 0.0))
+            for (k, v) in r.rev:
+                sp.append(k)
+                ex.append(v)
+                nu.append(v)
+            for _ in range(len(r.fwd) + len(r.rev)):
+                srx.append(qq)
+                sanu.append(nu[len(srx) - 1] * defeff[j]
+                            if r.kind != "elementary" else 0.0)
+            slot0.append(len(sp))
+        nslot = len(sp)
+        zero_src = nslot + R
+        entries = []
+        for qq, j in enumerate(perm):
+            r = m.rx[j]
+            slots = range(slot0[qq], slot0[qq + 1])
+            for b in slots:
+                for a in slots:
+                    entries.append(((sp[b] + 1) * nc + sp[a] + 1, a, nu[b]))
+            if r.kind != "elementary":
+                for t in range(tb_start[j], tb_start[j + 1]):
+                    for b in slots:
+                        entries.append(((sp[b] + 1) * nc + tb_idx[t] + 1,
+                                        nslot + qq, nu[b] * tb_de[t]))
+        have = {e[0] for e in entries}
+        for k in range(S):
+            for mm in range(S):
+                off = (k + 1) * nc + mm + 1
+                if off not in have:
+                    entries.append((off, zero_src, 0.0))
+        entries.sort(key=lambda e: e[0])
+        groups: List[List[Tuple[int, int, float]]] = []
+        for e in entries:
+            if groups and groups[-1][0][0] == e[0]:
+                groups[-1].append(e)
+            else:
+                groups.append([e])
+        # contiguous split of the groups into 32 runs of nearly equal length
+        lanes: List[List[Tuple[int, int, float]]] = [[] for _ in range(32)]
+        total, done, lane = len(entries), 0, 0
+        for g in groups:
+            if lane < 31 and done >= (lane + 1) * total / 32.0:
+                lane += 1
+            lanes[lane].extend(g)
+            done += len(g)
+        iters = max(len(x) for x in lanes)
+        u_off, u_src, u_coef = [], [], []
+        for it in range(iters):
+            for ln in range(32):
+                if it < len(lanes[ln]):
+                    o, s, c = lanes[ln][it]
+                else:
+                    o, s, c = 0xFFFF, zero_src, 0.0
+                u_off.append(o)
+                u_src.append(s)
+                u_coef.append(c)
+        # third-body efficiency entries, in permuted reaction order
+        q_tb0, q_tbidx, q_tbde = [0], [], []
+        for j in perm:
+            for t in range(tb_start[j], tb_start[j + 1]):
+                q_tbidx.append(tb_idx[t])
+                q_tbde.append(tb_de[t])
+            q_tb0.append(len(q_tbidx))
+        # species -> slots
+        inc: List[List[int]] = [[] for _ in range(S)]
+        for s_, k in enumerate(sp):
+            inc[k].append(s_)
+        si0, si_slot = [0], []
+        for k in range(S):
+            si_slot.extend(inc[k])
+            si0.append(len(si_slot))
+        nf = max(1, len(fo_low))
+        nasa = [[m.tmid[k]] + list(m.hi[k]) + list(m.lo[k]) + [0.0]
+                for k in range(S)]
+        jw_doubles = 9 * S + 2 * R + nslot + R + 1
+        jwarps = max(1, min(16, (227 * 1024 - 16384) // (8 * jw_doubles)))
+
+        def arr(ctype, name, dims, vals):
+            return _table(qual, ctype, name, dims, vals)
+
+        L: List[str] = []
+        w = L.append
+        w("// Jacobian kernel tables (global memory; see jacobian.cuh)")
+        w(f"#define NSLOT {nslot}")
+        w(f"#define JU_ITERS {iters}")
+        w(f"#define JD_ZERO {zero_src}")
+        w(f"#define JW_DOUBLES {jw_doubles}")
+        w(f"#define JWARPS {jwarps}")
+        w(arr("int", "jq_flags", [R], [_cint(flags[j]) for j in perm]))
+        w(arr("int", "jq_slot0", [R + 1], [_cint(v) for v in slot0]))
+        w(arr("int", "jq_nr", [R], [_cint(v) for v in q_nr]))
+        w(arr("double", "jq_rate", [3, R],
+              ["{" + ", ".join(_dlit(rates[j][p]) for j in perm) + "}"
+               for p in range(3)]))
+        w(arr("double", "jq_dnu", [R], [_hexd(dnu[j]) for j in perm]))
+        w(arr("double", "jq_defeff", [R], [_hexd(defeff[j]) for j in perm]))
+        w(arr("int", "jq_tb0", [R + 1], [_cint(v) for v in q_tb0]))
+        w(arr("int", "jq_tbidx", [max(1, len(q_tbidx))],
+              [_cint(v) for v in (q_tbidx or [0])]))
+        w(arr("double", "jq_tbde", [max(1, len(q_tbde))],
+              [_hexd(v) for v in (q_tbde or [0.0])]))
+        w(arr("int", "jq_fo", [R], [_cint(fo_slot[j]) for j in perm]))
+        w(arr("int", "jf_lowform", [nf], [_cint(v) for v in
+                                          (fo_form or [0])]))
+        w(arr("double", "jf_low", [3, nf],
+              ["{" + ", ".join(_dlit(rec[p]) for rec in
+                               (fo_low or [[0.0] * 3])) + "}"
+               for p in range(3)]))
+        w(arr("double", "jf_troe", [5, nf],
+              ["{" + ", ".join(_dlit(rec[p]) for rec in
+                               (fo_troe or [[0.0] * 5])) + "}"
+               for p in range(5)]))
+        w(arr("int", "jq_sp", [nslot], [_cint(v) for v in sp]))
+        w(arr("double", "jq_e", [nslot], [_hexd(v) for v in ex]))
+        w(arr("double", "jq_nu", [nslot], [_hexd(v) for v in nu]))
+        w(arr("int", "jq_slot_rx", [nslot], [_cint(v) for v in srx]))
+        w(arr("double", "jq_slot_anu", [nslot], [_hexd(v) for v in sanu]))
+        w(arr("int", "jg_si0", [S + 1], [_cint(v) for v in si0]))
+        w(arr("int", "jg_si_slot", [nslot], [_cint(v) for v in si_slot]))
+        w(arr("double", "jg_nasa", [S, 16],
+              ["{" + ", ".join(_hexd(v) for v in row) + "}"
+               for row in nasa]))
+        w(arr("double", "jg_mw", [S], [_hexd(v) for v in m.W]))
+        w(arr("double", "jg_invmw", [S], [_hexd(v) for v in m.invW]))
+        w(arr("unsigned short", "ju_off", [32 * iters],
+              [_cint(v) for v in u_off]))
+        w(arr("unsigned short", "ju_src", [32 * iters],
+              [_cint(v) for v in u_src]))
+        w(arr("double", "ju_coef", [32 * iters],
+              [_hexd(v) for v in u_coef]))
+        if zero_src > 0xFFFE or (S + 1) * nc > 0xFFFE:
+            raise NotImplementedError("mechanism too large for the "
+                                      "Jacobian update list")
+        return L
+
     def render(self) -> str:
         m = self.m
         S, R = m.S, m.R
@@ -471,9 +638,9 @@ class _Emitter:
             return (rank, troe, flags[j] >> 3 & 3, j)
         perm = sorted(range(R), key=kind_key)
         w(_table(qual, "short", "k_rx_perm", [R], [_cint(v) for v in perm]))
-        jw = 5 * R + 10 * S
-        jwarps = max(1, min(16, (227 * 1024 - 16384) // (8 * jw)))
-        w(f"#define JWARPS {jwarps}")
+        L.extend(self._jacobian_tables(perm, flags, rates, dnu, defeff,
+                                       tb_start, tb_idx, tb_de, fo_slot,
+                                       fo_form, fo_low, fo_troe))
         vblock = max(32, min(128, (100 * 1024 // (5 * S * 8)) // 32 * 32))
         w(f"#define VBLOCK {vblock}")
         w("")

@@ -263,6 +263,219 @@ __global__ void k_block_thomas(const double* __restrict__ Lm,
   }
 }
 
+
+// ------------------------------------------------------------------------
+// Small blocks (nv <= 16): one thread per system.
+//
+// On GB300 a warp-wide FP64 instruction occupies the FP64 pipe for the same
+// time however few of its lanes are active, so the CTA-per-system kernel
+// above, whose 10 x 10 steps keep only a few lanes busy, is bound by
+// partially empty FP64 instructions.  Here each thread runs one system's
+// whole recurrence (same algorithm, same per-row workspace layout), so every
+// FP64 instruction does 32 useful operations; the thread's blocks live in
+// shared memory interleaved by thread ([element][thread]: a warp's accesses
+// to one element are 32 consecutive doubles, conflict-free).  Systems are
+// handed out in the caller's order (longest first), so the threads of a
+// warp get systems of similar length.
+template <int NV>
+__global__ void __launch_bounds__(64)
+    k_block_thomas_small(const double* __restrict__ Lm,
+                         const double* __restrict__ Cm,
+                         const double* __restrict__ Um,
+                         const double* __restrict__ B, double* __restrict__ X,
+                         const int64_t* __restrict__ row_off,
+                         const int* __restrict__ order, int nsys,
+                         double* __restrict__ work, int* __restrict__ status) {
+  extern __shared__ double smem[];
+  constexpr int LD = NV + 1;
+  constexpr int BLK = NV * LD;
+  const int T = blockDim.x;
+  const int q = blockIdx.x * T + threadIdx.x;
+  if (q >= nsys) return;  // no block-wide synchronisation below
+  double* A = smem + threadIdx.x;  // C'_i | b'_i, then LU | b'_i
+  double* R = A + (size_t)BLK * T;  // U_i | b'_i -> S_i | t_i
+  double* P = R + (size_t)BLK * T;  // S_{i-1} | t_{i-1}
+#define EA(i, j) A[((i) * LD + (j)) * T]
+#define ER(i, j) R[((i) * LD + (j)) * T]
+#define EP(i, j) P[((i) * LD + (j)) * T]
+  const int s = order[q];
+  const int64_t r0 = row_off[s];
+  const int N = (int)(row_off[s + 1] - r0);
+  constexpr int64_t WROW = (int64_t)NV * NV + 2 * NV;
+  bool singular = false;
+  for (int i = 0; i < N; ++i) {
+    const int64_t row = r0 + i;
+    const double* Ci = Cm + row * NV * NV;
+    double* w = work + row * WROW;
+    for (int r = 0; r < NV; ++r) {
+#pragma unroll
+      for (int c = 0; c < NV; ++c) EA(r, c) = __ldg(Ci + r * NV + c);
+      EA(r, NV) = __ldg(B + row * NV + r);
+    }
+    if (i > 0) {
+      // C' = C - L S_prev ; b' = b - L t_prev
+      const double* Li = Lm + (row - 1) * NV * NV;
+      for (int r = 0; r < NV; ++r) {
+        double l[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k) l[k] = __ldg(Li + r * NV + k);
+#pragma unroll
+        for (int c = 0; c < LD; ++c) {
+          double acc = EA(r, c);
+#pragma unroll
+          for (int k = 0; k < NV; ++k) acc = fma(-l[k], EP(k, c), acc);
+          EA(r, c) = acc;
+        }
+      }
+    }
+    // LU with partial pivoting of the NV x NV part (b' column untouched);
+    // the pivots go straight to the workspace row
+    for (int k = 0; k < NV; ++k) {
+      int p = k;
+      double best = fabs(EA(k, k));
+      for (int r = k + 1; r < NV; ++r) {
+        const double v = fabs(EA(r, k));
+        if (v > best) {
+          best = v;
+          p = r;
+        }
+      }
+      w[NV * NV + NV + k] = (double)p;
+      if (best == 0.0) singular = true;
+      if (p != k) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) {
+          const double t = EA(k, c);
+          EA(k, c) = EA(p, c);
+          EA(p, c) = t;
+        }
+      }
+      const double inv = 1.0 / EA(k, k);
+      for (int r = k + 1; r < NV; ++r) {
+        const double lrk = EA(r, k) * inv;
+        EA(r, k) = lrk;
+        for (int c = k + 1; c < NV; ++c)
+          EA(r, c) = fma(-lrk, EA(k, c), EA(r, c));
+      }
+    }
+    // keep the factors and b'_i for the backward solve
+    for (int r = 0; r < NV; ++r) {
+#pragma unroll
+      for (int c = 0; c < NV; ++c) w[r * NV + c] = EA(r, c);
+      w[NV * NV + r] = EA(r, NV);
+    }
+    // S_i | t_i = C'_i^-1 (U_i | b'_i)  (only t_i on the last row)
+    const bool has_u = i < N - 1;
+    const double* Ui = Um + row * NV * NV;
+    for (int r = 0; r < NV; ++r) {
+      if (has_u) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) ER(r, c) = __ldg(Ui + r * NV + c);
+      }
+      ER(r, NV) = EA(r, NV);
+    }
+    for (int k = 0; k < NV; ++k) {
+      const int p = (int)w[NV * NV + NV + k];
+      if (p != k) {
+        for (int c = has_u ? 0 : NV; c < LD; ++c) {
+          const double t = ER(k, c);
+          ER(k, c) = ER(p, c);
+          ER(p, c) = t;
+        }
+      }
+    }
+    for (int k = 0; k < NV - 1; ++k)
+      for (int r = k + 1; r < NV; ++r) {
+        const double l = EA(r, k);
+        for (int c = has_u ? 0 : NV; c < LD; ++c)
+          ER(r, c) = fma(-l, ER(k, c), ER(r, c));
+      }
+    for (int k = NV - 1; k >= 0; --k) {
+      const double inv = 1.0 / EA(k, k);
+      for (int c = has_u ? 0 : NV; c < LD; ++c) ER(k, c) *= inv;
+      for (int r = 0; r < k; ++r) {
+        const double u = EA(r, k);
+        for (int c = has_u ? 0 : NV; c < LD; ++c)
+          ER(r, c) = fma(-u, ER(k, c), ER(r, c));
+      }
+    }
+    double* tmp = P;
+    P = R;
+    R = tmp;
+  }
+  // backward: x_{N-1} = t_{N-1}; x_i = C'_i^-1 (b'_i - U_i x_{i+1}), with
+  // x_{i+1} kept in the R block's last column
+  {
+    const int64_t row = r0 + N - 1;
+    for (int r = 0; r < NV; ++r) {
+      const double v = EP(r, NV);
+      ER(r, NV) = v;
+      X[row * NV + r] = v;
+    }
+  }
+  for (int i = N - 2; i >= 0; --i) {
+    const int64_t row = r0 + i;
+    const double* w = work + row * WROW;
+    const double* Ui = Um + row * NV * NV;
+    // A's last column <- b'_i - U_i x_{i+1}
+    for (int r = 0; r < NV; ++r) {
+      double a = w[NV * NV + r];
+#pragma unroll
+      for (int k = 0; k < NV; ++k)
+        a = fma(-__ldg(Ui + r * NV + k), ER(k, NV), a);
+      EA(r, NV) = a;
+    }
+    for (int k = 0; k < NV; ++k) {
+      const int p = (int)w[NV * NV + NV + k];
+      if (p != k) {
+        const double t = EA(k, NV);
+        EA(k, NV) = EA(p, NV);
+        EA(p, NV) = t;
+      }
+    }
+    for (int k = 0; k < NV - 1; ++k) {
+      const double v = EA(k, NV);
+      for (int r = k + 1; r < NV; ++r)
+        EA(r, NV) = fma(-w[r * NV + k], v, EA(r, NV));
+    }
+    for (int k = NV - 1; k >= 0; --k) {
+      const double v = EA(k, NV) / w[k * NV + k];
+      EA(k, NV) = v;
+      for (int r = 0; r < k; ++r)
+        EA(r, NV) = fma(-w[r * NV + k], v, EA(r, NV));
+    }
+    for (int r = 0; r < NV; ++r) {
+      const double v = EA(r, NV);
+      ER(r, NV) = v;
+      X[row * NV + r] = v;
+    }
+  }
+  if (singular && status) atomicOr(status, 1);
+#undef EA
+#undef ER
+#undef EP
+}
+
+template <int NV>
+int launch_small(const double* L, const double* C, const double* U,
+                 const double* b, double* x, const int64_t* row_off,
+                 const int* order, int nsys, double* work, int* status,
+                 int threads, cudaStream_t stream) {
+  const size_t smem = (size_t)3 * NV * (NV + 1) * threads * sizeof(double);
+  if (smem > 48 * 1024 &&
+      cudaFuncSetAttribute((const void*)k_block_thomas_small<NV>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  const int grid = (nsys + threads - 1) / threads;
+  k_block_thomas_small<NV><<<grid, threads, smem, stream>>>(
+      L, C, U, b, x, row_off, order, nsys, work, status);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
 }  // namespace
 
 // Doubles of workspace pyro_block_thomas needs for `rows` packed rows.
@@ -320,6 +533,37 @@ PYRO_EXPORT int pyro_block_thomas(const double* L, const double* C,
                                                   counter, status);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
+}
+
+// pyro_block_thomas for blocks of size nv <= 16 with one thread per system
+// (same arguments minus the counter; threads = systems per CTA, 32 or 64).
+// The workspace layout is the same as pyro_block_thomas's.
+PYRO_EXPORT int pyro_block_thomas_small(const double* L, const double* C,
+                                        const double* U, const double* b,
+                                        double* x, const int64_t* row_off,
+                                        const int* order, int nsys, int nv,
+                                        double* work, int* status,
+                                        int threads, cudaStream_t stream) {
+  if (nsys < 0 || nv < 1 || nv > 16 || (threads != 32 && threads != 64))
+    return PYRO_ERR_ARGUMENT;
+  if (nsys == 0) return PYRO_OK;
+  if (!L || !C || !U || !b || !x || !row_off || !order || !work)
+    return PYRO_ERR_ARGUMENT;
+  if ((size_t)3 * nv * (nv + 1) * threads * sizeof(double) > 227 * 1024)
+    return PYRO_ERR_ARGUMENT;
+  switch (nv) {
+#define PYRO_BT_SMALL(NV)                                                    \
+  case NV:                                                                   \
+    return launch_small<NV>(L, C, U, b, x, row_off, order, nsys, work,       \
+                            status, threads, stream);
+    PYRO_BT_SMALL(1) PYRO_BT_SMALL(2) PYRO_BT_SMALL(3) PYRO_BT_SMALL(4)
+    PYRO_BT_SMALL(5) PYRO_BT_SMALL(6) PYRO_BT_SMALL(7) PYRO_BT_SMALL(8)
+    PYRO_BT_SMALL(9) PYRO_BT_SMALL(10) PYRO_BT_SMALL(11) PYRO_BT_SMALL(12)
+    PYRO_BT_SMALL(13) PYRO_BT_SMALL(14) PYRO_BT_SMALL(15) PYRO_BT_SMALL(16)
+#undef PYRO_BT_SMALL
+    default:
+      return PYRO_ERR_ARGUMENT;
+  }
 }
 
 // ------------------------------------------------------------------------

@@ -20,16 +20,21 @@
 //   chain rule through c(T, Y) and rho(T, Y), then the dT/dt row.
 //
 // k_reactor_jacobian: one warp per state.  Lanes take reactions in an
-// order sorted by kind (k_rx_perm), so a warp's lanes run the same code
-// path.  The S x S block dw/dc is accumulated in place in the state's own
-// output block (rows/columns 1..S of its (S+1)^2 slot: L1/L2-resident while
-// the warp works on it); each lane owns whole columns (species m), walking
-// the reactions that contain m, so no atomics are needed.  The third-body
-// default efficiency contributes a rank-1 term added in the assembly
-// instead of S entries per reaction.  Shared memory holds only per-reaction
-// and per-species vectors (about 17 KB per warp at 53 species / 325
-// reactions), so about a dozen warps fit per SM.  The output is written
-// row by row, 32 consecutive doubles per warp store.
+// order sorted by kind, so a warp's lanes run the same code path; the
+// tables they index with different reactions or species are global-memory
+// copies read through L1 (the constant cache would serialise the 32
+// different addresses).  Each lane writes, per slot of its reaction, the
+// partial derivative of the rate of progress with respect to that slot's
+// concentration (and dq/dM) into a per-warp shared-memory vector D.  The
+// S x S block dw/dc is then built in the interior of the state's own output
+// block from a generated update list: entries (element, source in D,
+// stoichiometric coefficient) sorted by element and split into 32 runs of
+// equal length, one per lane, so every element is summed by one lane in a
+// fixed order and stored once -- no atomics and no divergent trip counts.
+// The third-body default efficiency contributes a rank-1 term added in the
+// assembly instead of S entries per reaction.  Shared memory holds per-warp
+// vectors only (about 21 KB per warp at 53 species / 325 reactions).  The
+// output is written row by row, 32 consecutive doubles per warp store.
 //
 // k_reactor_vjp: one thread per state, reverse accumulation.  Each reaction
 // gets one scalar adjoint mu_r = sum_k lambda_k nu_kr, so the cost is a
@@ -254,12 +259,156 @@ __device__ __forceinline__ SpThermo species_thermo(int k, double T,
 
 }  // namespace pyro
 
-#ifndef JWARPS
-#define JWARPS 4
-#endif
-// doubles of shared memory per warp of the Jacobian kernel
-#define JW_DOUBLES (5 * NR + 10 * NS)
+namespace pyro {
 
+// Rate-of-progress derivatives of reaction qq (permuted numbering) from the
+// global Jacobian tables: q, dq/dT at fixed c, dq/dM, and per slot s of the
+// reaction dq/dc_{sp(s)} into D[s]; dq/dM goes to D[NSLOT + qq].
+template <class CT>
+__device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
+                                             CT c, CT g, CT h, double* D,
+                                             double* Dq, double* DdT) {
+  const double T = s.T, lnT = s.lnT, invT = s.invT;
+  const int f = __ldg(jq_flags + qq);
+  const int kind = f & RX_KIND_MASK;
+  const int form = (f >> RX_FORM_SHIFT) & 3;
+  const int s0 = __ldg(jq_slot0 + qq), s2 = __ldg(jq_slot0 + qq + 1);
+  const int s1 = s0 + __ldg(jq_nr + qq);
+  const double p0 = __ldg(&jq_rate[0][qq]), p1 = __ldg(&jq_rate[1][qq]),
+               p2 = __ldg(&jq_rate[2][qq]);
+  double m = 1.0;
+  if (kind != RX_ELEMENTARY) {
+    const double d = __ldg(jq_defeff + qq);
+    m = d == 0.0 ? 0.0 : (d == 1.0 ? s.ctot : d * s.ctot);
+    const int t1 = __ldg(jq_tb0 + qq + 1);
+    for (int t = __ldg(jq_tb0 + qq); t < t1; ++t)
+      m = fma(__ldg(jq_tbde + t), c[__ldg(jq_tbidx + t)], m);
+  }
+  double kf, x = 0.0, dlnkf, dkfdM = 0.0;
+  bool exp_form = false;
+  if (kind == RX_FALLOFF) {
+    const int sl = __ldg(jq_fo + qq);
+    const int lform = __ldg(jf_lowform + sl);
+    const double l0 = __ldg(&jf_low[0][sl]), l1 = __ldg(&jf_low[1][sl]),
+                 l2 = __ldg(&jf_low[2][sl]);
+    double xh, xl;
+    const double k_hi = arrhenius(form, p0, p1, p2, T, lnT, invT, xh);
+    const double k_lo = arrhenius(lform, l0, l1, l2, T, lnT, invT, xl);
+    const double dxh = darr_dT(form, p1, p2, invT);
+    const double dxl = darr_dT(lform, l1, l2, invT);
+    const double pr = m * k_lo / k_hi;
+    double blend = 1.0, dlnF_dT = 0.0, phi_x = 0.0;
+    if (f & RX_TROE) {
+      const double ln10 = 2.302585092994045684;
+      const double t0 = __ldg(&jf_troe[0][sl]), t1 = __ldg(&jf_troe[1][sl]);
+      const double t2 = __ldg(&jf_troe[2][sl]), t3 = __ldg(&jf_troe[3][sl]);
+      const double e3 = PEXP(T * t1);
+      const double e1 = PEXP(T * t3);
+      double fsum = t0 * e3 + t2 * e1;
+      double dfsum = t0 * t1 * e3 + t2 * t3 * e1;
+      if (f & RX_TROE_T2) {
+        const double t4 = __ldg(&jf_troe[4][sl]);
+        const double e2 = PEXP(t4 * invT);
+        fsum += e2;
+        dfsum -= t4 * invT * invT * e2;
+      }
+      const double L = log10(fsum);
+      const double dL = dfsum / (fsum * ln10);
+      double fac = -1.0 / 0.14, dfac = 0.0, fx = 0.0;
+      if (pr > 0.0) {
+        const double xx = log10(pr) + (-0.4 - 0.67 * L);
+        const double nn = 0.75 - 1.27 * L;
+        const double den = nn - 0.14 * xx;
+        fac = xx / den;
+        fx = nn / (den * den);
+        const double fn = -xx / (den * den);
+        const double dxx = (dxl - dxh) / ln10 - 0.67 * dL;
+        dfac = fx * dxx + fn * (-1.27 * dL);
+      }
+      const double opf = 1.0 + fac * fac;
+      blend = PEXP10(L / opf);
+      const double dphi = dL / opf - 2.0 * L * fac / (opf * opf) * dfac;
+      dlnF_dT = ln10 * dphi;
+      phi_x = -2.0 * L * fac * fx / (opf * opf);
+    }
+    kf = k_hi * (blend * pr / (1.0 + pr));
+    dlnkf = dxh + dlnF_dT + (dxl - dxh) / (1.0 + pr);
+    dkfdM = blend * k_lo / (1.0 + pr) * (phi_x + 1.0 / (1.0 + pr));
+  } else {
+    const double ek = arrhenius(form, p0, p1, p2, T, lnT, invT, x);
+    exp_form = form == FORM_EXP;
+    dlnkf = darr_dT(form, p1, p2, invT);
+    if (kind == RX_THREE_BODY) {
+      kf = ek * m;
+      dkfdM = ek;
+    } else {
+      kf = ek;
+    }
+  }
+  // side products and the log K sums (signed stoichiometry per slot)
+  double pf = 1.0, pv = 1.0, sg = 0.0, shh = 0.0;
+  for (int a = s0; a < s2; ++a) {
+    const int k = __ldg(jq_sp + a);
+    const double cv = c[k];
+    const double e = __ldg(jq_e + a), nu = __ldg(jq_nu + a);
+    if (a < s1)
+      pf *= ipow_or_pow(cv, e);
+    else
+      pv *= ipow_or_pow(cv, e);
+    sg = fma(nu, g[k], sg);
+    shh = fma(nu, h[k], shh);
+  }
+  double kr = 0.0, dlnkr = 0.0, dkrdM = 0.0;
+  if (f & RX_REVERSIBLE) {
+    const double dnu = __ldg(jq_dnu + qq);
+    double lk = sg;
+    if (dnu != 0.0) lk -= dnu * s.c0;
+    const double dlk = (dnu - shh) * invT;
+    if (exp_form) {
+      const double ekr = PEXP(x + lk);
+      kr = kind == RX_THREE_BODY ? ekr * m : ekr;
+      dkrdM = kind == RX_THREE_BODY ? ekr : 0.0;
+    } else {
+      const double eK = PEXP(lk);
+      kr = kf * eK;
+      dkrdM = dkfdM * eK;
+    }
+    dlnkr = dlnkf + dlk;
+  } else {
+    pv = 0.0;
+  }
+  Dq[qq] = kf * pf - kr * pv;
+  DdT[qq] = kf * dlnkf * pf - kr * dlnkr * pv;
+  D[NSLOT + qq] = dkfdM * pf - dkrdM * pv;
+  // dq/dc per slot: kf d(prod c^e)/dc (reactants), -kr d(prod c^nu'')/dc
+  for (int a = s0; a < s2; ++a) {
+    const bool rside = a < s1;
+    const int b0 = rside ? s0 : s1, b1 = rside ? s1 : s2;
+    double others = 1.0, ea = 1.0;
+    for (int b = b0; b < b1; ++b) {
+      const double e = __ldg(jq_e + b);
+      if (b == a)
+        ea = e;
+      else
+        others *= ipow_or_pow(c[__ldg(jq_sp + b)], e);
+    }
+    const double cm = c[__ldg(jq_sp + a)];
+    double d;
+    if (ea == 1.0)
+      d = 1.0;
+    else if (ea == 2.0)
+      d = 2.0 * cm;
+    else
+      d = ea * pow(cm, ea - 1.0);
+    D[a] = rside ? kf * (d * others) : -kr * (d * others);
+  }
+}
+
+}  // namespace pyro
+
+// doubles of shared memory per warp (JW_DOUBLES, from the tables):
+//   c, h, g, cp, w, jt, a, u, shj [NS each]; q, dq/dT [NR each];
+//   D = dq/dc per slot [NSLOT], dq/dM per reaction [NR], one zero.
 __global__ void __launch_bounds__(JWARPS * 32)
     k_reactor_jacobian(const double* __restrict__ Pp, int64_t p_inc,
                        const double* __restrict__ Tp, int64_t t_inc,
@@ -268,43 +417,59 @@ __global__ void __launch_bounds__(JWARPS * 32)
   extern __shared__ double smem[];
   PEXP_PRELOAD();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* rq = smem + (size_t)wid * JW_DOUBLES;
-  double* rdT = rq + NR;
-  double* rdM = rdT + NR;
-  double* rkf = rdM + NR;
-  double* rkr = rkf + NR;
-  double* sc = rkr + NR;
-  double* sg = sc + NS;
-  double* sh = sg + NS;
-  double* scp = sh + NS;
+  double* sc = smem + (size_t)wid * JW_DOUBLES;
+  double* sh = sc + NS;
+  double* sg = sh + NS;
+  double* scp = sg + NS;
   double* sw = scp + NS;
   double* sjt = sw + NS;
   double* sa = sjt + NS;
   double* su = sa + NS;
   double* shj = su + NS;
+  double* Dq = shj + NS;
+  double* DdT = Dq + NR;
+  double* D = DdT + NR;  // [NSLOT] dq/dc, [NR] dq/dM, [1] zero
   using LC = pyro::LocalCols;
   const LC c{sc}, g{sg}, h{sh};
   constexpr int NC = NS + 1;
+  if (lane == 0) D[JD_ZERO] = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * JWARPS + wid; i < n;
        i += (int64_t)gridDim.x * JWARPS) {
     double* Ji = J + i * ldj;
-    // Jc(k, m) = dw_k/dc_m, accumulated in the interior of this state's
-    // output block
-#define Jc(k, m) Ji[(int64_t)((k) + 1) * NC + (m) + 1]
     const double T = pyro_ld(Tp, t_inc, i);
     const double P = pyro_ld(Pp, p_inc, i);
     const double lnT = log(T), invT = 1.0 / T;
-    // species thermo, sigma, cp, dcp/dT
+    // species thermo, sigma, cp, dcp/dT (lanes over species)
     double sig = 0.0, cpp = 0.0, dcpp = 0.0;
     for (int k = lane; k < NS; k += 32) {
-      const double wk = __ldg(Y + (int64_t)k * ldy + i) * k_inv_mw[k];
-      const pyro::SpThermo th = pyro::species_thermo(k, T, lnT, invT);
-      scp[k] = th.cp;
-      sh[k] = th.h;
-      sg[k] = th.g;
+      const double* nk = &jg_nasa[k][0];
+      const bool up = T > __ldg(nk);
+      const double* a = nk + (up ? 1 : 8);
+      double q[7];
+#pragma unroll
+      for (int t = 0; t < 7; ++t) q[t] = __ldg(a + t);
+      const double cpk =
+          fma(T, fma(T, fma(T, fma(T, q[4], q[3]), q[2]), q[1]), q[0]);
+      const double hk =
+          fma(T, fma(T, fma(T, fma(T, q[4] * 0.2, q[3] * 0.25),
+                            q[2] * (1.0 / 3.0)),
+                    q[1] * 0.5),
+              q[0]) +
+          q[5] * invT;
+      const double gk =
+          fma(q[0], 1.0 - lnT, fma(q[5], invT, -q[6])) -
+          T * fma(T, fma(T, fma(T, q[4] * (1.0 / 20.0), q[3] * (1.0 / 12.0)),
+                         q[2] * (1.0 / 6.0)),
+                  q[1] * 0.5);
+      const double dcpk =
+          fma(T, fma(T, 4.0 * q[4], 3.0 * q[3]), 2.0 * q[2]) * T + q[1];
+      const double wk = __ldg(Y + (int64_t)k * ldy + i) * __ldg(jg_invmw + k);
+      scp[k] = cpk;
+      sh[k] = hk;
+      sg[k] = gk;
       sig += wk;
-      cpp = fma(wk, th.cp, cpp);
-      dcpp = fma(wk, th.dcp, dcpp);
+      cpp = fma(wk, cpk, cpp);
+      dcpp = fma(wk, dcpk, dcpp);
     }
     const double sigma = pyro::warp_sum(sig);
     const double cpm = GAS_CONSTANT * pyro::warp_sum(cpp);
@@ -312,7 +477,8 @@ __global__ void __launch_bounds__(JWARPS * 32)
     const double rho = P / (GAS_CONSTANT * T * sigma);
     double ct = 0.0;
     for (int k = lane; k < NS; k += 32) {
-      const double v = k_inv_mw[k] * rho * __ldg(Y + (int64_t)k * ldy + i);
+      const double v =
+          __ldg(jg_invmw + k) * rho * __ldg(Y + (int64_t)k * ldy + i);
       sc[k] = v;
       ct += v;
     }
@@ -323,80 +489,51 @@ __global__ void __launch_bounds__(JWARPS * 32)
     s.c0 = LOG_P0_OVER_R - lnT;
     s.ctot = pyro::warp_sum(ct);
     __syncwarp();
-    // per reaction: q, dq/dT|c, dq/dM, kf, kr
-    for (int qq = lane; qq < NR; qq += 32) {
-      const int r = k_rx_perm[qq];
-      const pyro::RxnDeriv d = pyro::reaction_deriv(r, s, c, g, h);
-      rq[r] = d.q;
-      rdT[r] = d.dqdT;
-      rdM[r] = d.dqdM;
-      rkf[r] = d.kf;
-      rkr[r] = d.kr;
-    }
-    for (int k = 0; k < NS; ++k)
-      for (int mm = lane; mm < NS; mm += 32) Jc(k, mm) = 0.0;
+    // per reaction (lanes over the kind-sorted numbering)
+    for (int qq = lane; qq < NR; qq += 32)
+      pyro::jac_reaction(qq, s, c, g, h, D, Dq, DdT);
     __syncwarp();
+    // dw/dc into the interior of this state's output block: each lane sums
+    // its run of the update list and stores every element it owns once
+    {
+      int cur = -1;
+      double acc = 0.0;
+      for (int it = 0; it < JU_ITERS; ++it) {
+        const int e = it * 32 + lane;
+        const int off = __ldg(ju_off + e);
+        const double cf = __ldg(ju_coef + e);
+        const double dv = D[__ldg(ju_src + e)];
+        if (off != cur) {
+          if (cur >= 0 && cur != 0xFFFF) Ji[cur] = acc;
+          cur = off;
+          acc = 0.0;
+        }
+        acc = fma(cf, dv, acc);
+      }
+      if (cur >= 0 && cur != 0xFFFF) Ji[cur] = acc;
+    }
     // per species: w_k, dw_k/dT|c, rank-1 third-body vector a_k
     for (int k = lane; k < NS; k += 32) {
       double w = 0.0, jt = 0.0, a = 0.0;
-      for (int t = k_si_start[k]; t < k_si_start[k + 1]; ++t) {
-        const int r = k_si_rx[t];
-        const double nu = pyro::slot_nu(r, k_si_pos[t]);
-        w = fma(nu, rq[r], w);
-        jt = fma(nu, rdT[r], jt);
-        if ((k_rx_flags[r] & RX_KIND_MASK) != RX_ELEMENTARY)
-          a = fma(nu * k_rx_defeff[r], rdM[r], a);
+      const int t1 = __ldg(jg_si0 + k + 1);
+      for (int t = __ldg(jg_si0 + k); t < t1; ++t) {
+        const int sl = __ldg(jg_si_slot + t);
+        const int qq = __ldg(jq_slot_rx + sl);
+        const double nu = __ldg(jq_nu + sl);
+        w = fma(nu, Dq[qq], w);
+        jt = fma(nu, DdT[qq], jt);
+        a = fma(__ldg(jq_slot_anu + sl), D[NSLOT + qq], a);
       }
       sw[k] = w;
       sjt[k] = jt;
       sa[k] = a;
     }
-    // columns m of dw/dc owned by lane
-    for (int m = lane; m < NS; m += 32) {
-      for (int t = k_si_start[m]; t < k_si_start[m + 1]; ++t) {
-        const int r = k_si_rx[t];
-        const int pos = k_si_pos[t];
-        const int f = k_rx_flags[r];
-        const bool frac = (f & RX_FRACTIONAL) != 0;
-        double d;
-        if (pos < MAXSIDE)
-          d = rkf[r] * pyro::dprod(r, 0, pos, k_rx_nr[r], frac, c);
-        else
-          d = -rkr[r] * pyro::dprod(r, 1, pos - MAXSIDE, k_rx_np[r], frac, c);
-        const int nr = k_rx_nr[r], np = k_rx_np[r];
-        for (int a = 0; a < MAXSIDE; ++a) {
-          if (a < nr) {
-            double& e = Jc(k_rx_sp[r][a], m);
-            e = fma(pyro::slot_nu(r, a), d, e);
-          }
-          if (a < np) {
-            double& e = Jc(k_rx_sp[r][MAXSIDE + a], m);
-            e = fma(pyro::slot_nu(r, MAXSIDE + a), d, e);
-          }
-        }
-      }
-      for (int t = k_st_start[m]; t < k_st_start[m + 1]; ++t) {
-        const int r = k_st_rx[t];
-        const double d = k_st_de[t] * rdM[r];
-        const int nr = k_rx_nr[r], np = k_rx_np[r];
-        for (int a = 0; a < MAXSIDE; ++a) {
-          if (a < nr) {
-            double& e = Jc(k_rx_sp[r][a], m);
-            e = fma(pyro::slot_nu(r, a), d, e);
-          }
-          if (a < np) {
-            double& e = Jc(k_rx_sp[r][MAXSIDE + a], m);
-            e = fma(pyro::slot_nu(r, MAXSIDE + a), d, e);
-          }
-        }
-      }
-    }
-    __syncwarp();
-    // u_k = sum_m dw_k/dc_m c_m (with the rank-1 part), column sums of H J
-    const double RT = GAS_CONSTANT * T;
-    // the column-owned writes above are by other lanes: make them visible
+    // the output-block writes above are by other lanes: make them visible
     __threadfence_block();
     __syncwarp();
+#define Jc(k, m) Ji[(int64_t)((k) + 1) * NC + (m) + 1]
+    const double RT = GAS_CONSTANT * T;
+    // u_k = sum_m dw_k/dc_m c_m (+ rank-1 part); shj_m = RT sum_k h_k Jc
     for (int k = 0; k < NS; ++k) {
       double u = 0.0;
       for (int mm = lane; mm < NS; mm += 32) u = fma(Jc(k, mm), sc[mm], u);
@@ -431,26 +568,28 @@ __global__ void __launch_bounds__(JWARPS * 32)
         v = -dQdT * inv_rcp + qr2 * (-rcp * invT + rho * dcpm);
       } else {
         const int jj = col - 1;
-        const double iw = k_inv_mw[jj];
+        const double iw = __ldg(jg_invmw + jj);
         const double dQdY = rho * iw * (shj[jj] + HA) - HU * inv_sig * iw;
-        const double drcp = -rcp * inv_sig * iw + rho * GAS_CONSTANT * scp[jj] * iw;
+        const double drcp =
+            -rcp * inv_sig * iw + rho * GAS_CONSTANT * scp[jj] * iw;
         v = -dQdY * inv_rcp + qr2 * drcp;
       }
       Ji[col] = v;
     }
-    // rows 1..S: d(dY_k/dt)/dx
+    // rows 1..S: d(dY_k/dt)/dx = W_k/rho ((Jc + a_k) rho / W_m
+    //                                     + (w_k - u_k) / (sigma W_m))
     for (int k = 0; k < NS; ++k) {
-      const double wk_rho = k_mw[k] / rho;
-      const double wk = sw[k], uk = su[k], ak = sa[k];
+      const double wk_rho = __ldg(jg_mw + k) / rho;
+      const double wk = sw[k], uk = su[k];
+      const double A = wk_rho * rho;
+      const double B = wk_rho * fma(sa[k], rho, (wk - uk) * inv_sig);
       for (int col = lane; col < NC; col += 32) {
         double v;
         if (col == 0) {
           v = wk_rho * (sjt[k] - uk * invT + wk * invT);
         } else {
           const int jj = col - 1;
-          const double iw = k_inv_mw[jj];
-          v = wk_rho * ((Jc(k, jj) + ak) * rho * iw +
-                        (wk - uk) * inv_sig * iw);
+          v = __ldg(jg_invmw + jj) * fma(A, Jc(k, jj), B);
         }
         Ji[(int64_t)(k + 1) * NC + col] = v;
       }

@@ -35,16 +35,18 @@ class BlockThomasSolver:
     """Plan for solving ``len(lengths)`` block-tridiagonal systems with
     ``nv x nv`` blocks.
 
-    ``threads``: CTA size (a multiple of 32; ``None`` picks from the
-    autotuner cache or a size rule); ``ctas``: persistent grid (0: all
-    resident CTAs); ``use_graph``: capture the counter reset and the launch
-    in a CUDA graph on the first :meth:`solve` with given buffers and replay
-    it afterwards.
+    ``kernel``: ``"cta"`` (one CTA per system, threads over matrix
+    elements; any nv <= 64) or ``"small"`` (one thread per system, nv <=
+    16); ``threads``: CTA size (``"cta"``: a multiple of 32; ``"small"``:
+    32 or 64 systems per CTA); both ``None`` pick from the autotuner cache
+    or a size rule.  ``ctas``: persistent grid of the ``"cta"`` kernel (0:
+    all resident CTAs); ``use_graph``: capture the launch in a CUDA graph on
+    the first :meth:`solve` with given buffers and replay it afterwards.
     """
 
     def __init__(self, nv: int, lengths: Sequence[int], device=None,
                  threads: Optional[int] = None, ctas: int = 0,
-                 use_graph: bool = False):
+                 use_graph: bool = False, kernel: Optional[str] = None):
         if torch is None or not torch.cuda.is_available():
             raise RuntimeError("BlockThomasSolver needs a CUDA device")
         self.nv = int(nv)
@@ -66,13 +68,31 @@ class BlockThomasSolver:
                                 device=self.device)
         self.counter = torch.zeros(1, dtype=torch.int32, device=self.device)
         self.status = torch.zeros(1, dtype=torch.int32, device=self.device)
-        self.threads = int(threads) if threads else default_threads(self.nv)
+        if kernel is None and threads is None:
+            kernel, threads = default_plan(self.nv)
+        self.kernel = kernel or "cta"
+        if self.kernel not in ("cta", "small"):
+            raise ValueError(f"unknown block-Thomas kernel {kernel!r}")
+        if self.kernel == "small" and self.nv > 16:
+            raise ValueError("the one-thread-per-system kernel takes nv <= 16")
+        self.threads = int(threads) if threads else (
+            _small_threads(self.nv) if self.kernel == "small"
+            else default_threads(self.nv))
         self.ctas = int(ctas)
         self.use_graph = bool(use_graph)
         self._graph = None
         self._graph_key = None
 
     def _launch(self, L, C, U, b, x, stream):
+        if self.kernel == "small":
+            _check(self.lib.pyro_block_thomas_small(
+                L.data_ptr(), C.data_ptr(), U.data_ptr(), b.data_ptr(),
+                x.data_ptr(), self.offsets.data_ptr(), self.order.data_ptr(),
+                self.nsys, self.nv, self.work.data_ptr(),
+                self.status.data_ptr(), self.threads,
+                ctypes.c_void_p(stream.cuda_stream)),
+                "pyro_block_thomas_small")
+            return
         _check(self.lib.pyro_block_thomas(
             L.data_ptr(), C.data_ptr(), U.data_ptr(), b.data_ptr(),
             x.data_ptr(), self.offsets.data_ptr(), self.order.data_ptr(),
@@ -121,16 +141,35 @@ class BlockThomasSolver:
 
 
 def default_threads(nv: int) -> int:
-    """CTA size: from the autotuner cache when present, else one warp for
-    small blocks and up to 128 threads for larger ones."""
+    """CTA size of the one-CTA-per-system kernel: from the autotuner cache
+    when it holds one, else one warp for small blocks and up to 128 threads
+    for larger ones."""
     best = _tuned().get(str(nv))
-    if best:
-        return int(best)
+    if best and not str(best).startswith("small"):
+        return int(str(best).split(":")[-1])
     if nv <= 12:
         return 32
     if nv <= 24:
         return 64
     return 128
+
+
+def _small_threads(nv: int) -> int:
+    """Systems per CTA of the one-thread-per-system kernel: 64 while three
+    blocks per thread fit the 227 KB of shared memory, else 32."""
+    return 64 if 3 * nv * (nv + 1) * 8 * 64 <= 227 * 1024 else 32
+
+
+def default_plan(nv: int):
+    """(kernel, threads): the autotuner's choice when cached, else the
+    one-thread-per-system kernel for nv <= 16 and the CTA kernel above."""
+    best = _tuned().get(str(nv))
+    if best:
+        kind, _, th = str(best).rpartition(":")
+        return (kind or "cta"), int(th)
+    if nv <= 16:
+        return "small", _small_threads(nv)
+    return "cta", default_threads(nv)
 
 
 def _tune_path():
@@ -149,9 +188,11 @@ def _tuned():
 def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
              n_max: int = 1024, candidates=(32, 64, 128, 256),
              seed: int = 0, device=None, repeats: int = 3):
-    """Time the solve for each CTA size on a seeded sample of systems of
-    the given shape; store the fastest in the build directory's tuning
-    file and return ``{threads: ms}``."""
+    """Time the solve for each kernel and CTA size (the CTA kernel at each
+    of *candidates*, and for nv <= 16 the one-thread-per-system kernel at 32
+    and 64 systems per CTA) on a seeded sample of systems of the given
+    shape; store the fastest in the build directory's tuning file and
+    return ``{"kernel:threads": ms}``."""
     rng = np.random.default_rng(seed)
     lengths = rng.integers(n_min, n_max + 1, size=n_systems)
     dev = torch.device(device if device is not None else "cuda")
@@ -166,11 +207,14 @@ def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
                     generator=gen)
     b = torch.randn((rows, nv), dtype=torch.float64, device=dev,
                     generator=gen)
+    plans = [("cta", th) for th in candidates if not (nv > th and th < 64)]
+    if nv <= 16:
+        plans += [("small", th) for th in (32, 64)
+                  if 3 * nv * (nv + 1) * 8 * th <= 227 * 1024]
     times = {}
-    for th in candidates:
-        if nv > th and th < 64:
-            continue
-        solver = BlockThomasSolver(nv, lengths, device=dev, threads=th)
+    for kind, th in plans:
+        solver = BlockThomasSolver(nv, lengths, device=dev, threads=th,
+                                   kernel=kind)
         solver.solve(L, C, U, b)
         torch.cuda.synchronize(dev)
         e0, e1 = torch.cuda.Event(True), torch.cuda.Event(True)
@@ -179,10 +223,10 @@ def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
             solver.solve(L, C, U, b)
         e1.record()
         torch.cuda.synchronize(dev)
-        times[th] = e0.elapsed_time(e1) / repeats
+        times[f"{kind}:{th}"] = e0.elapsed_time(e1) / repeats
     best = min(times, key=times.get)
     tuned = _tuned()
-    tuned[str(nv)] = int(best)
+    tuned[str(nv)] = best
     os.makedirs(os.path.dirname(_tune_path()), exist_ok=True)
     with open(_tune_path(), "w") as f:
         json.dump(tuned, f)

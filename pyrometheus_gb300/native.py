@@ -127,6 +127,9 @@ def block_thomas_lib() -> ctypes.CDLL:
     lib.pyro_block_thomas_work_doubles.argtypes = [I, I64]
     lib.pyro_block_thomas_smem_bytes.restype = I64
     lib.pyro_block_thomas_smem_bytes.argtypes = [I]
+    lib.pyro_block_thomas_small.restype = I
+    lib.pyro_block_thomas_small.argtypes = [P, P, P, P, P, P, P, I, I, P, P,
+                                            I, P]
     return lib
 
 

@@ -47,24 +47,33 @@ def _cuda():
         pytest.fail("CUDA device required for the gpu tests")
 
 
-def _solve_cuda(lengths, L, C, U, b, threads=None, use_graph=False):
+def _solve_cuda(lengths, L, C, U, b, threads=None, use_graph=False,
+                kernel=None):
     from pyrometheus_gb300.flamelet import BlockThomasSolver
     dev = torch.device("cuda")
     t = [torch.as_tensor(a, device=dev).contiguous() for a in (L, C, U, b)]
     solver = BlockThomasSolver(C.shape[1], lengths, threads=threads,
-                               use_graph=use_graph)
+                               use_graph=use_graph, kernel=kernel)
     x = solver.solve(*t)
     solver.check_status()
     return x.cpu().numpy(), solver, t
 
 
+PLANS = [("cta", 32), ("cta", 64), ("cta", 128), ("small", 32),
+         ("small", 64)]
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("tag", TAGS)
-@pytest.mark.parametrize("threads", [32, 64, 128])
-def test_cuda_block_thomas_golden(tag, threads):
+@pytest.mark.parametrize("plan", PLANS)
+def test_cuda_block_thomas_golden(tag, plan):
     _cuda()
     lengths, L, C, U, b, x = _golden(tag)
-    got, _, _ = _solve_cuda(lengths, L, C, U, b, threads=threads)
+    kernel, threads = plan
+    if kernel == "small" and C.shape[1] > 16:
+        pytest.skip("one thread per system takes nv <= 16")
+    got, _, _ = _solve_cuda(lengths, L, C, U, b, threads=threads,
+                            kernel=kernel)
     assert _rel(got, x) < 1e-12
 
 
@@ -82,8 +91,9 @@ def _residual(L, C, U, b, x):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("nv", [10, 54])
-def test_cuda_block_thomas_uneven_batch(nv):
+@pytest.mark.parametrize("nv,kernel", [(10, "cta"), (10, "small"),
+                                       (54, "cta")])
+def test_cuda_block_thomas_uneven_batch(nv, kernel):
     """Against the reference algorithm on long systems.  The two round
     differently (right-looking LU and sequential Schur updates here,
     LAPACK's recursive getrf and BLAS there), so x agrees only to about
@@ -96,7 +106,7 @@ def test_cuda_block_thomas_uneven_batch(nv):
     lengths, L, C, U, b = make_systems(37 if nv == 54 else 300, nv, 1, 200,
                                        seed=nv)
     ref = solve_packed(lengths, L, C, U, b)
-    got, solver, t = _solve_cuda(lengths, L, C, U, b)
+    got, solver, t = _solve_cuda(lengths, L, C, U, b, kernel=kernel)
     r0 = 0
     for n in lengths:
         n = int(n)
