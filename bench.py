@@ -35,6 +35,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 N_STATES = 4_194_304
+# DRAM bytes per state of k_fused_step_u measured by ncu on 262,144 states
+# of this workload (read 119,283,968 B + write 111,984,128 B); the traffic
+# grows with the states processed (one pass, no re-reads)
+NCU_DRAM_BYTES_PER_STATE = (119_283_968 + 111_984_128) / 262_144
 WORKLOAD = "synthetic53_325: density + net production rates + T(e) Newton"
 METRIC = ("FP64 states/s (density + net production rates + temperature "
           "Newton)")
@@ -565,7 +569,12 @@ def run_gb300(args):
         "roofline": {
             "bound": "fp64", "achieved": achieved / 1e12,
             "peak": dfma / 1e12, "unit": "TFLOP/s",
-            "frac": achieved / dfma, "traffic": None,
+            "frac": achieved / dfma,
+            "traffic": NCU_DRAM_BYTES_PER_STATE * n,
+            "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum "
+                              "of one ncu capture of k_fused_step_u on "
+                              "262,144 states (231.3 MB = 882.2 B/state), "
+                              "scaled to this launch's states",
             "peak_source": "DFMA throughput measured live by bench.py "
                            "(MEASURED_PEAKS.json has no FP64 figure)",
             "flops_per_state": flops_state,

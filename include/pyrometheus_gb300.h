@@ -129,6 +129,51 @@ int pyro_fused_step(const double* p, int64_t p_inc, const double* T,
                     double* T_out, int* fail_count, int64_t n,
                     cudaStream_t stream);
 
+/* Reactor right-hand side f = (dT/dt, dY_1/dt .. dY_S/dt) of the adiabatic
+ * constant-pressure 0-D reactor, [S+1][ldf]: the function the reference's
+ * reactors integrate and differentiate (examples/free_flame/reactors.py:
+ * 115-125; flamelets/equations.py:124-129 for the Jacobian). */
+int pyro_reactor_source(const double* p, int64_t p_inc, const double* T,
+                        int64_t t_inc, const double* Y, int64_t ldy,
+                        double* F, int64_t ldf, int64_t n,
+                        cudaStream_t stream);
+
+/* Its Jacobian d f / d (T, Y) per state, J[n][ldj] with the (S+1) x (S+1)
+ * block row-major at J + i * ldj (ldj >= (S+1)^2): replaces
+ * jax.jacfwd(rhs) of reactors.py:125 / equations.py:124-129. */
+int pyro_reactor_jacobian(const double* p, int64_t p_inc, const double* T,
+                          int64_t t_inc, const double* Y, int64_t ldy,
+                          double* J, int64_t ldj, int64_t n,
+                          cudaStream_t stream);
+
+/* Vector-Jacobian product v^T df/d(T, Y) and v^T df/dp for cotangents
+ * V[S+1][ldv]: gT[n], gY[S][ldg], gp[n] (gp may be NULL); the reverse-mode
+ * counterpart of jax.vjp over the same function. */
+int pyro_reactor_vjp(const double* p, int64_t p_inc, const double* T,
+                     int64_t t_inc, const double* Y, int64_t ldy,
+                     const double* V, int64_t ldv, double* gT, double* gY,
+                     int64_t ldg, double* gp, int64_t n, cudaStream_t stream);
+
+/* Integrate cells [0, n) of a reactor pool with the fused per-cell
+ * variable-step BDF2 / chord-Newton kernel, up to `attempts` step attempts
+ * per cell in this call (the reference steps one reactor at a time with
+ * Crank-Nicolson and a Newton loop around jnp.linalg.solve,
+ * examples/free_flame/time_integ.py:70-106).  Per cell (leading dimension
+ * ld >= n): y, y_prev, f_n [S+1][ld]; p, t, t_end, h, h_prev, g_lu, crate
+ * [ld] doubles; nsteps, nattempts, jage [ld] int64; active, failed, jstale,
+ * done [ld] bytes; J, M [(S+1)^2][ld] doubles; piv [S+1][ld] ints.  Cells
+ * with active == 0 are skipped; a cell that reaches t_end or fails gets
+ * active = 0 and done = 1 (failed = 1 on failure).  Allocates nothing. */
+int pyro_reactor_bdf2(double* y, double* y_prev, double* f_n, int64_t ld,
+                      const double* p, double* t, const double* t_end,
+                      double* h, double* h_prev, double* g_lu, double* crate,
+                      int64_t* nsteps, int64_t* nattempts, int64_t* jage,
+                      unsigned char* active, unsigned char* failed,
+                      unsigned char* jstale, unsigned char* done, double* J,
+                      double* M, int* piv, int64_t n, int attempts,
+                      double rtol, double atol, int64_t max_attempts,
+                      cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

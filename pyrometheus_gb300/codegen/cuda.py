@@ -650,6 +650,14 @@ class _Emitter:
             L.extend(_UnrolledEmitter(m, self.opts.accum_in_smem,
                                       self.opts.hot_block).render())
         w('#include "kinetics_abi.cuh"')
+        # fused per-cell reactor integrator: threads per CTA so that seven
+        # per-thread columns (3 NS + 4 (NS + 1) doubles) fit beside the exp
+        # table in 227 KB of shared memory
+        per_thread = (3 * S + 4 * (S + 1)) * 8
+        iblock = max(32, min(128, ((227 - 16) * 1024 // per_thread)
+                             // 32 * 32))
+        w(f"#define IBLOCK {iblock}")
+        w('#include "reactor_bdf2.cuh"')
         return "\n".join(L) + "\n"
 
 

@@ -139,13 +139,36 @@ class CudaReactorBackend:
             raise RuntimeError(f"per-cell norm failed ({st})")
         return out
 
+    def fused_step(self, pool, n: int, attempts: int):
+        """Up to *attempts* step attempts of cells [0, n) of *pool* inside
+        one launch of the mechanism library's ``pyro_reactor_bdf2``."""
+        ptr = lambda x: x.data_ptr()  # noqa: E731
+        st = self.th._lib.pyro_reactor_bdf2(
+            ptr(pool.y), ptr(pool.y_prev), ptr(pool.f_n), pool.cap,
+            ptr(pool.p), ptr(pool.t), ptr(pool.t_end), ptr(pool.h),
+            ptr(pool.h_prev), ptr(pool.g_lu), ptr(pool.crate),
+            ptr(pool.nsteps), ptr(pool.nattempts), ptr(pool.jage),
+            ptr(pool.active), ptr(pool.failed), ptr(pool.jstale),
+            ptr(pool.done), ptr(pool.J), ptr(pool.M), ptr(pool.piv), n,
+            int(attempts), pool.rtol, pool.atol, pool.max_attempts,
+            self._stream())
+        if st != 0:
+            raise RuntimeError(f"fused reactor integration failed ({st})")
+
 
 class ReactorPool:
     """Device-resident slots of one mechanism and its integrator state.
 
     *backend* supplies ``source``, ``jacobian``, ``lu_factor``,
     ``lu_solve`` and ``wrms`` (:class:`CudaReactorBackend` for a drop-in
-    Thermochemistry object, which may be passed directly)."""
+    Thermochemistry object, which may be passed directly).
+
+    ``fused`` (default: on for the CUDA backend) runs the step attempts in
+    the mechanism library's per-cell integrator kernel, *attempts* of them
+    per engine step, instead of one attempt of batched tensor operations;
+    the arithmetic is the same apart from the Jacobian, which the kernel
+    forms by forward differences of the source (the batched path uses the
+    analytic Jacobian kernel)."""
 
     NEWTON_ITERS = 4
     NEWTON_TOL = 0.1
@@ -154,10 +177,14 @@ class ReactorPool:
 
     def __init__(self, backend, capacity: int, rtol: float = 1e-8,
                  atol: float = 1e-12, max_attempts: int = 200000,
-                 stream=None):
+                 stream=None, fused: Optional[bool] = None,
+                 attempts: int = 64):
         if not hasattr(backend, "lu_factor"):
             backend = CudaReactorBackend(backend)
         self.be = backend
+        self.fused = hasattr(backend, "fused_step") if fused is None \
+            else bool(fused)
+        self.attempts = int(attempts)
         self.S = backend.num_species
         self.nv = self.S + 1
         self.cap = int(capacity)
@@ -190,9 +217,18 @@ class ReactorPool:
             self.jstale = torch.ones(cap, dtype=torch.bool, device=dev)
             self.active = torch.zeros(cap, dtype=torch.bool, device=dev)
             self.failed = torch.zeros(cap, dtype=torch.bool, device=dev)
-            self.J = torch.zeros((cap, nv, nv), **f64)
-            self.M = torch.zeros((cap, nv, nv), **f64)
-            self.piv = torch.zeros((cap, nv), dtype=torch.int32, device=dev)
+            if self.fused:
+                # element-major for the per-cell kernel
+                self.J = torch.zeros((nv * nv, cap), **f64)
+                self.M = torch.zeros((nv * nv, cap), **f64)
+                self.piv = torch.zeros((nv, cap), dtype=torch.int32,
+                                       device=dev)
+                self.done = torch.zeros(cap, dtype=torch.bool, device=dev)
+            else:
+                self.J = torch.zeros((cap, nv, nv), **f64)
+                self.M = torch.zeros((cap, nv, nv), **f64)
+                self.piv = torch.zeros((cap, nv), dtype=torch.int32,
+                                       device=dev)
             self.eye = torch.eye(nv, **f64)
             self.lu_status = torch.zeros(1, dtype=torch.int32, device=dev)
             self._norm = torch.empty(cap, **f64)
@@ -292,14 +328,22 @@ class ReactorPool:
 
     # -- numerics --------------------------------------------------------
     def step(self):
-        """One implicit step attempt for every occupied slot (asynchronous
-        on the pool's stream, apart from the host reading which cells need
-        a Jacobian or a factorisation and whether Newton is done)."""
+        """One engine step for every occupied slot: *attempts* step
+        attempts per cell in the fused kernel, or one attempt of batched
+        tensor operations (asynchronous on the pool's stream, apart from
+        the host reading which cells need a Jacobian or a factorisation and
+        whether Newton is done)."""
         n = self.high_water
         if n == 0:
             return
         be = self.be
         self.engine_steps += 1
+        if self.fused:
+            with self._on_stream():
+                self.done[:n].zero_()
+                be.fused_step(self, n, self.attempts)
+                self._done = self.done[:n]
+            return
         with self._on_stream():
             act = self.active[:n]
             y, yp, fn = self.y[:, :n], self.y_prev[:, :n], self.f_n[:, :n]
@@ -473,7 +517,8 @@ class ReactorServer:
     @classmethod
     def from_thermos(cls, thermos: Dict[str, object],
                      hbm_budget_bytes: float, rtol: float = 1e-8,
-                     atol: float = 1e-12) -> "ReactorServer":
+                     atol: float = 1e-12, fused: Optional[bool] = None,
+                     attempts: int = 64) -> "ReactorServer":
         """Equal cell counts per mechanism, as many as the budget holds
         (state, history, Jacobian/Newton matrices, LU workspace)."""
         total = sum(ReactorPool.bytes_per_cell(th.num_species)
@@ -481,7 +526,8 @@ class ReactorServer:
         cap = int(hbm_budget_bytes / total)
         if cap < 1:
             raise ValueError("HBM budget too small for one cell")
-        return cls({name: ReactorPool(th, cap, rtol=rtol, atol=atol)
+        return cls({name: ReactorPool(th, cap, rtol=rtol, atol=atol,
+                                      fused=fused, attempts=attempts)
                     for name, th in thermos.items()})
 
     def now(self) -> float:

@@ -1,7 +1,9 @@
-"""The reactor server on the GPU: a request's result is bit-identical alone
-and in a mix (per-cell integration), agrees with a tight CPU BDF
-integration of the oracle's source, and a non-finite cell fails on its own
-without disturbing the others."""
+"""The reactor server on the GPU, on both integrator paths (the fused
+per-cell kernel and the batched tensor path): a request's result is
+bit-identical alone and in a mix (per-cell integration), agrees with a
+tight CPU BDF integration of the oracle's source, the two paths agree with
+each other, and a non-finite cell fails on its own without disturbing the
+others."""
 
 import numpy as np
 import pytest
@@ -12,7 +14,7 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def _server(budget=2e8):
+def _server(budget=2e8, fused=True):
     if not torch.cuda.is_available():
         pytest.fail("CUDA device required for the gpu tests")
     from pyrometheus_gb300 import get_thermochem_class
@@ -20,7 +22,8 @@ def _server(budget=2e8):
     s9, _ = load_golden("synthetic9")
     s53, _ = load_golden("synthetic53")
     th = {"s9": get_thermochem_class(s9)(), "s53": get_thermochem_class(s53)()}
-    return ReactorServer.from_thermos(th, budget), {"s9": s9, "s53": s53}
+    return (ReactorServer.from_thermos(th, budget, fused=fused),
+            {"s9": s9, "s53": s53})
 
 
 def _reqs(mechs, seed, n_req, cells=(1, 40)):
@@ -30,8 +33,9 @@ def _reqs(mechs, seed, n_req, cells=(1, 40)):
     return reqs[:n_req]
 
 
-def test_alone_and_in_mix_are_identical():
-    server, mechs = _server()
+@pytest.mark.parametrize("fused", [True, False])
+def test_alone_and_in_mix_are_identical(fused):
+    server, mechs = _server(fused=fused)
     reqs = _reqs(mechs, seed=1, n_req=6)
     target = reqs[2]
     import copy
@@ -39,7 +43,7 @@ def test_alone_and_in_mix_are_identical():
     alone.arrival = 0.0
     server.run([alone], time_limit=120.0)
     assert alone.status == "done"
-    server2, _ = _server()
+    server2, _ = _server(fused=fused)
     mix = [copy.deepcopy(r) for r in reqs]
     for r in mix:
         r.arrival *= 1e-3
@@ -50,11 +54,11 @@ def test_alone_and_in_mix_are_identical():
     assert np.array_equal(got.steps, alone.steps)
 
 
-def test_accuracy_against_cpu_bdf():
+@pytest.mark.parametrize("fused", [True, False])
+def test_accuracy_against_cpu_bdf(fused):
     scipy_integrate = pytest.importorskip("scipy.integrate")
     from oracle.thermo_oracle import Thermochemistry as Oracle
-    from pyrometheus_gb300.serving import Request
-    server, mechs = _server()
+    server, mechs = _server(fused=fused)
     sol = mechs["s9"]
     orc = Oracle(sol)
     reqs = _reqs({"s9": sol}, seed=3, n_req=1, cells=(3, 3))
@@ -77,8 +81,27 @@ def test_accuracy_against_cpu_bdf():
         assert np.abs(r.Y[:, c] - xe[1:]).max() <= 1e-5 * np.abs(xe[1:]).max()
 
 
+def test_fused_and_batched_paths_agree():
+    """Same requests through both paths: the fused kernel forms its
+    Jacobian by differences, the batched path analytically, so the step
+    sequences differ; both must land within the integration tolerance."""
+    import copy
+    got = {}
+    for fused in (True, False):
+        server, mechs = _server(fused=fused)
+        reqs = _reqs(mechs, seed=7, n_req=3, cells=(2, 6))
+        for r in reqs:
+            r.arrival = 0.0
+        server.run([copy.deepcopy(r) for r in reqs], time_limit=300.0)
+        got[fused] = {r.rid: r for r in server.done}
+    for rid, a in got[True].items():
+        b = got[False][rid]
+        assert a.status == "done" and b.status == "done"
+        assert np.abs(a.T - b.T).max() <= 1e-5 * np.abs(b.T).max()
+        assert np.abs(a.Y - b.Y).max() <= 1e-6
+
+
 def test_nonfinite_cell_fails_alone():
-    from pyrometheus_gb300.serving import Request
     server, mechs = _server()
     reqs = _reqs(mechs, seed=5, n_req=3)
     bad = reqs[1]
