@@ -303,13 +303,13 @@ def secondary_legs(sol, th, dev, dfma):
     """The other rows of the workload set, each measured with CUDA events on
     device-resident seeded inputs: the 54x54 reactor Jacobian and the VJP
     over 1,048,576 states of the same mechanism, and the batched
-    block-Thomas solve (4,096 systems, N ~ U[64, 1024], nv = 10; and a
-    304-system sample at nv = 54)."""
+    block-Thomas solve (4,096 systems, N ~ U[64, 1024], at nv = 10 and
+    nv = 54; diagonally dominant random blocks, diagonal scale 10)."""
     import numpy as np
     import torch
 
     from pyrometheus_gb300 import synthetic
-    from pyrometheus_gb300.flamelet import BlockThomasSolver
+    from pyrometheus_gb300.flamelet import BlockThomasSolver, autotune
     out = {}
     n = 1 << 20
     t, p, y = synthetic.sample_states(sol, n, seed=77)
@@ -332,28 +332,37 @@ def secondary_legs(sol, th, dev, dfma):
     del V, T, P, Y
     rng = np.random.default_rng(0)
     bt = {}
-    for nv, nsys in ((10, 4096), (54, 304)):
-        lengths = rng.integers(64, 1025, size=nsys)
+    for nv in (10, 54):
+        lengths = rng.integers(64, 1025, size=4096)
         rows = int(lengths.sum())
+        # the autotuner picks kernel and CTA size: on the workload itself at
+        # nv = 10, on a 304-system sample of it at nv = 54 (the full set's
+        # blocks take 160 GB; a second copy would not fit beside them)
+        tune_lengths = lengths if nv == 10 else lengths[:304]
+        tuning = autotune(nv, lengths=tune_lengths, device=dev, repeats=2)
+        torch.cuda.empty_cache()
         g = torch.Generator(device=dev).manual_seed(nv)
         f64 = dict(dtype=torch.float64, device=dev)
-        C = torch.randn((rows, nv, nv), generator=g, **f64) + 10.0 * \
-            torch.eye(nv, **f64)
+        C = torch.randn((rows, nv, nv), generator=g, **f64)
+        C.diagonal(dim1=1, dim2=2).add_(10.0)
         L = torch.randn((rows, nv, nv), generator=g, **f64)
         U = torch.randn((rows, nv, nv), generator=g, **f64)
         b = torch.randn((rows, nv), generator=g, **f64)
         solver = BlockThomasSolver(nv, lengths, device=dev, use_graph=True)
         ms = _event_ms(lambda: solver.solve(L, C, U, b), 2)
+        solver.check_status()
         flops = rows * (14.0 / 3.0) * nv ** 3
         bt[f"nv{nv}"] = {
-            "systems": nsys, "rows": rows, "ms": ms,
-            "solves_per_s": nsys / ms * 1e3,
+            "systems": len(lengths), "rows": rows, "ms": ms,
+            "solves_per_s": len(lengths) / ms * 1e3,
             "fp64_tflops": flops / ms / 1e9,
             "fp64_frac": flops / ms / 1e9 / (dfma / 1e12),
             "hbm_gbs": rows * (5 * nv * nv + 4 * nv) * 8 / ms / 1e6,
             "kernel": solver.kernel, "threads": solver.threads,
-            "cuda_graph": True}
+            "cuda_graph": True, "autotune_ms": tuning,
+            "autotune_systems": len(tune_lengths)}
         del C, L, U, b, solver
+        torch.cuda.empty_cache()
     out["block_thomas"] = bt
     torch.cuda.empty_cache()
     return out

@@ -657,7 +657,10 @@ class _Emitter:
         iblock = max(32, min(128, ((227 - 16) * 1024 // per_thread)
                              // 32 * 32))
         w(f"#define IBLOCK {iblock}")
+        if self.opts.unrolled and S <= 16:
+            w("#define PYRO_BDF2_UNROLLED 1")
         w('#include "reactor_bdf2.cuh"')
+        w('#include "flamelet.cuh"')
         return "\n".join(L) + "\n"
 
 
@@ -845,16 +848,26 @@ class _UnrolledEmitter:
         w("}")
         w("")
         w("using HCols = pyro::ColsT<HOT_BLOCK>;")
-        w("__device__ __forceinline__ void net_rates(double T, double rho, "
-          "const double* __restrict__ Y, int64_t ldy, int64_t i, "
-          "HCols c, HCols g, HCols w, double (&wd)[NS]) {")
+        w("// mass fractions of state i in a species-major global array")
+        w("struct GlobalY {")
+        w("  const double* __restrict__ Y;")
+        w("  int64_t ldy, i;")
+        w("  __device__ __forceinline__ double operator()(int k) const {")
+        w("    return __ldg(Y + (int64_t)k * ldy + i);")
+        w("  }")
+        w("};")
+        w("// net production rates into wd (registers) or w (columns); Y is")
+        w("// any accessor k -> Y_k, CT a per-thread column type")
+        w("template <class YA, class CT>")
+        w("__device__ __forceinline__ void net_rates_y(double T, double rho, "
+          "const YA& Y, CT c, CT g, CT w, double (&wd)[NS]) {")
         w("  const double lnT = log(T);")
         w("  const double invT = 1.0 / T;")
         w("  const double c0 = LOG_P0_OVER_R - lnT;")
         w("  double ctot = 0.0;")
         for k in range(m.S):
             w(f"  {{ const double v = {_hexd(m.invW[k])} * rho * "
-              f"__ldg(Y + (int64_t){k} * ldy + i); c[{k}] = v; ctot += v; }}")
+              f"Y({k}); c[{k}] = v; ctot += v; }}")
         w("  pyro::gibbs_all(T, lnT, invT, g);")
         for k in range(m.S):
             w(f"  {self.W(k)} = 0.0;")
@@ -864,8 +877,18 @@ class _UnrolledEmitter:
         w("  if (bad) {  // exact recompute through the table-driven path")
         w("    double lc[NS], lg[NS], lw[NS];")
         w("    const pyro::LocalCols C{lc}, G{lg}, W{lw};")
-        w("    const pyro::StateScalars s = "
-          "pyro::state_from_mass(T, rho, Y, ldy, i, C);")
+        w("    pyro::StateScalars s;")
+        w("    s.T = T;")
+        w("    s.lnT = log(T);")
+        w("    s.invT = 1.0 / T;")
+        w("    s.c0 = LOG_P0_OVER_R - s.lnT;")
+        w("    double ct = 0.0;")
+        w("    for (int k = 0; k < NS; ++k) {")
+        w("      const double v = k_inv_mw[k] * rho * Y(k);")
+        w("      lc[k] = v;")
+        w("      ct += v;")
+        w("    }")
+        w("    s.ctot = ct;")
         w("    pyro::production_rates(s, C, G, W);")
         w("#pragma unroll")
         w("    for (int k = 0; k < NS; ++k) " +
@@ -874,6 +897,12 @@ class _UnrolledEmitter:
         if self.acc_smem:
             w("#pragma unroll")
             w("  for (int k = 0; k < NS; ++k) wd[k] = w[k];")
+        w("}")
+        w("")
+        w("__device__ __forceinline__ void net_rates(double T, double rho, "
+          "const double* __restrict__ Y, int64_t ldy, int64_t i, "
+          "HCols c, HCols g, HCols w, double (&wd)[NS]) {")
+        w("  net_rates_y(T, rho, GlobalY{Y, ldy, i}, c, g, w, wd);")
         w("}")
         w("")
         w("}  // namespace pyro_unrolled")

@@ -1,0 +1,230 @@
+// Steady-flamelet residual and block-tridiagonal Jacobian on the device
+// (FP64, sm_103a): the assembly of pyrometheus/flamelets/equations.py
+// (FlameletEquations.rhs :193-238, jac :240-298, source_terms :340-385)
+// with the Laplacian block form of onedim_laplacian.py:144-180, for many
+// flamelets at once.
+//
+// Unknowns per grid point: phi = (h, Y_1..Y_S) (mixture enthalpy per unit
+// mass and mass fractions).  Per point, with T from h by Newton (the
+// caller's get_temperature_from_enthalpy) and rho = p / (R T sigma),
+// sigma = sum_k Y_k / W_k:
+//   source   S = (v / rho, W_k w_k / rho)          (v: viscous heating)
+//   residual R_i = chi_i / 2 Lap(phi)_i + S_i m_i - BC_i,
+//            Lap(phi)_i = (phi_{i-1} - 2 phi_i + phi_{i+1}) / dx^2 inside,
+//            phi_i / dx^2 at the two boundary points; m_i = 0 there and
+//            BC_i = (h_ox, y_ox) first, (h_fu, y_fu) last, 0 inside
+//   blocks   C_i = chi_i / 2 Lap_c,i I + dS/dphi_i (0 at the boundaries),
+//            L_i = chi_{i+1} / 2 dx^-2 I when point i+1 is interior,
+//            U_i = chi_i / 2 dx^-2 I when point i is interior, else 0.
+// The dissipation rates of the boundary points are used as given, as the
+// reference does (its _enforce_dirichlet_bcs builds new arrays with
+// .at[].set and discards them).
+//
+// dS/dphi comes from the reactor Jacobian J = d(dT/dt, W w / rho)/d(T, Y)
+// at (T, Y, p) (k_reactor_jacobian, written into the C blocks first) by
+// the chain rule through T(h, Y): dT/dh = 1 / cp, dT/dY_m = -h_m / cp
+// (h_m, cp per unit mass); this is what the reference's jacfwd through its
+// Newton loop converges to.  The enthalpy row: d(v/rho) = (v/rho)
+// (dT / T + dY_m / (sigma W_m)).
+//
+// Layout: systems packed along rows as for the block-Thomas solver:
+// system s owns rows [row_off[s], row_off[s+1]) (at least 3), sys_of_row
+// gives s for every row; per-row arrays [rows], species-major [S][ld];
+// blocks [rows][nv][nv] row-major (nv = S + 1); the residual [nv][ldr].
+#pragma once
+
+#define FNV (NS + 1)
+
+// one warp per row: transform the reactor Jacobian held in C in place and
+// write L and U.
+__global__ void __launch_bounds__(128)
+    k_flamelet_blocks(const double* __restrict__ Pp, int64_t p_inc,
+                      const double* __restrict__ Tt,
+                      const double* __restrict__ Y, int64_t ldy,
+                      const double* __restrict__ chi,
+                      const double* __restrict__ visc,
+                      const int64_t* __restrict__ row_off,
+                      const int* __restrict__ sys_of_row,
+                      const double* __restrict__ inv_dx2,
+                      double* __restrict__ L, double* __restrict__ C,
+                      double* __restrict__ U, int64_t rows) {
+  const int lane = threadIdx.x & 31;
+  constexpr int NB = FNV * FNV;
+  __shared__ double s_hm[4][NS];  // species enthalpies per unit mass
+  double* hm_w = s_hm[threadIdx.x >> 5];
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       r < rows; r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int s = sys_of_row[r];
+    const int64_t r0 = row_off[s], r1 = row_off[s + 1];
+    const bool first = r == r0, last = r == r1 - 1;
+    const bool interior = !first && !last;
+    const double idx2 = inv_dx2[s];
+    const double T = Tt[r];
+    const double invT = 1.0 / T;
+    double* Cr = C + r * NB;
+    // cp (mass), sigma and the species enthalpies per unit mass
+    double sig = 0.0, cpp = 0.0;
+    for (int k = lane; k < NS; k += 32) {
+      const double wk = __ldg(Y + (int64_t)k * ldy + r) * k_inv_mw[k];
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      const double cpk =
+          fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
+      const double hrt =
+          fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
+                            a[2] * (1.0 / 3.0)),
+                    a[1] * 0.5),
+              a[0]) +
+          a[5] * invT;
+      hm_w[k] = GAS_CONSTANT * T * hrt * k_inv_mw[k];
+      sig += wk;
+      cpp = fma(wk, cpk, cpp);
+    }
+    const double sigma = pyro::warp_sum(sig);
+    const double cp = GAS_CONSTANT * pyro::warp_sum(cpp);
+    const double rho = pyro_ld(Pp, p_inc, r) / (GAS_CONSTANT * T * sigma);
+    const double vr = visc[r] / rho;
+    const double inv_cp = 1.0 / cp;
+    __syncwarp();
+    if (interior) {
+      // species rows: column 0 <- J[1+k][0] / cp, columns m <- J - J[.][0] h_m / cp
+      for (int k = 0; k < NS; ++k) {
+        double* row = Cr + (int64_t)(k + 1) * FNV;
+        const double jt = row[0];
+        __syncwarp();
+        for (int m = lane; m < NS; m += 32)
+          row[m + 1] = fma(-jt * inv_cp, hm_w[m], row[m + 1]);
+        if (lane == 0) row[0] = jt * inv_cp;
+        __syncwarp();
+      }
+      // enthalpy row
+      for (int m = lane; m < FNV; m += 32) {
+        double v;
+        if (m == 0) {
+          v = vr * invT * inv_cp;
+        } else {
+          v = vr * (k_inv_mw[m - 1] / sigma - hm_w[m - 1] * inv_cp * invT);
+        }
+        Cr[m] = v;
+      }
+    } else {
+      for (int e = lane; e < NB; e += 32) Cr[e] = 0.0;
+    }
+    __syncwarp();
+    // Laplacian diagonal, and the couplings
+    const double lap_c = interior ? -2.0 * idx2 : idx2;
+    for (int d = lane; d < FNV; d += 32) Cr[(int64_t)d * FNV + d] += 0.5 * chi[r] * lap_c;
+    const bool next_interior = !last && (r + 1 < r1 - 1);
+    const double lo = next_interior ? 0.5 * chi[r + 1] * idx2 : 0.0;
+    const double up = interior ? 0.5 * chi[r] * idx2 : 0.0;
+    double* Lr = L + r * NB;
+    double* Ur = U + r * NB;
+    for (int e = lane; e < NB; e += 32) {
+      const bool diag = (e % (FNV + 1)) == 0;
+      Lr[e] = diag ? lo : 0.0;
+      Ur[e] = diag ? up : 0.0;
+    }
+    __syncwarp();
+  }
+}
+
+// thread per row: the residual R [nv][ldr].
+__global__ void __launch_bounds__(128)
+    k_flamelet_residual(const double* __restrict__ Pp, int64_t p_inc,
+                        const double* __restrict__ Tt,
+                        const double* __restrict__ H,
+                        const double* __restrict__ Y, int64_t ldy,
+                        const double* __restrict__ F, int64_t ldf,
+                        const double* __restrict__ chi,
+                        const double* __restrict__ visc,
+                        const int64_t* __restrict__ row_off,
+                        const int* __restrict__ sys_of_row,
+                        const double* __restrict__ inv_dx2,
+                        const double* __restrict__ h_ox,
+                        const double* __restrict__ h_fu,
+                        const double* __restrict__ y_ox,
+                        const double* __restrict__ y_fu, int64_t ldb,
+                        double* __restrict__ R, int64_t ldr, int64_t rows) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int s = sys_of_row[r];
+    const int64_t r0 = row_off[s], r1 = row_off[s + 1];
+    const bool first = r == r0, last = r == r1 - 1;
+    const double idx2 = inv_dx2[s];
+    const double hc = 0.5 * chi[r];
+    const double T = Tt[r];
+    double sig = 0.0;
+    for (int k = 0; k < NS; ++k)
+      sig = fma(__ldg(Y + (int64_t)k * ldy + r), k_inv_mw[k], sig);
+    const double rho = pyro_ld(Pp, p_inc, r) / (GAS_CONSTANT * T * sig);
+    // enthalpy
+    {
+      double v;
+      if (first)
+        v = hc * (H[r] * idx2) - h_ox[s];
+      else if (last)
+        v = hc * (H[r] * idx2) - h_fu[s];
+      else
+        v = hc * ((H[r - 1] - 2.0 * H[r] + H[r + 1]) * idx2) + visc[r] / rho;
+      R[r] = v;
+    }
+    for (int k = 0; k < NS; ++k) {
+      const double* yk = Y + (int64_t)k * ldy;
+      double v;
+      if (first)
+        v = hc * (yk[r] * idx2) - y_ox[(int64_t)k * ldb + s];
+      else if (last)
+        v = hc * (yk[r] * idx2) - y_fu[(int64_t)k * ldb + s];
+      else
+        v = hc * ((yk[r - 1] - 2.0 * yk[r] + yk[r + 1]) * idx2) +
+            F[(int64_t)(k + 1) * ldf + r];
+      R[(int64_t)(k + 1) * ldr + r] = v;
+    }
+  }
+}
+
+PYRO_EXPORT int pyro_flamelet_blocks(const double* p, int64_t p_inc,
+                                     const double* T, const double* Y,
+                                     int64_t ldy, const double* chi,
+                                     const double* visc,
+                                     const int64_t* row_off,
+                                     const int* sys_of_row,
+                                     const double* inv_dx2, double* L,
+                                     double* C, double* U, int64_t rows,
+                                     cudaStream_t stream) {
+  if (rows < 0 || ldy < rows) return PYRO_ERR_ARGUMENT;
+  if (rows == 0) return PYRO_OK;
+  if (!p || !T || !Y || !chi || !visc || !row_off || !sys_of_row ||
+      !inv_dx2 || !L || !C || !U)
+    return PYRO_ERR_ARGUMENT;
+  int64_t blocks = (rows * 32 + 127) / 128;
+  const int64_t cap = (int64_t)pyro_sm_count() * 32;
+  if (blocks > cap) blocks = cap;
+  k_flamelet_blocks<<<(int)blocks, 128, 0, stream>>>(
+      p, p_inc, T, Y, ldy, chi, visc, row_off, sys_of_row, inv_dx2, L, C, U,
+      rows);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_flamelet_residual(
+    const double* p, int64_t p_inc, const double* T, const double* h,
+    const double* Y, int64_t ldy, const double* F, int64_t ldf,
+    const double* chi, const double* visc, const int64_t* row_off,
+    const int* sys_of_row, const double* inv_dx2, const double* h_ox,
+    const double* h_fu, const double* y_ox, const double* y_fu, int64_t ldb,
+    double* R, int64_t ldr, int64_t rows, cudaStream_t stream) {
+  if (rows < 0 || ldy < rows || ldf < rows || ldr < rows || ldb < 1)
+    return PYRO_ERR_ARGUMENT;
+  if (rows == 0) return PYRO_OK;
+  if (!p || !T || !h || !Y || !F || !chi || !visc || !row_off ||
+      !sys_of_row || !inv_dx2 || !h_ox || !h_fu || !y_ox || !y_fu || !R)
+    return PYRO_ERR_ARGUMENT;
+  int64_t blocks = (rows + 127) / 128;
+  const int64_t cap = (int64_t)pyro_sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  k_flamelet_residual<<<(int)blocks, 128, 0, stream>>>(
+      p, p_inc, T, h, Y, ldy, F, ldf, chi, visc, row_off, sys_of_row,
+      inv_dx2, h_ox, h_fu, y_ox, y_fu, ldb, R, ldr, rows);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}

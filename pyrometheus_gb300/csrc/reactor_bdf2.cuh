@@ -61,10 +61,24 @@ __device__ __forceinline__ void cell_rhs(double P, ICols X, ICols F, ICols c,
               cpp);
   }
   const double rho = P / (GAS_CONSTANT * T * sigma);
+  const double invT = 1.0 / T;
+#if defined(PYRO_UNROLLED) && defined(PYRO_BDF2_UNROLLED)
+  // straight-line rates (small mechanisms): accumulators in registers
+  struct ColY {
+    ICols X;
+    __device__ __forceinline__ double operator()(int k) const {
+      return X[k + 1];
+    }
+  };
+  double wd[NS];
+  pyro_unrolled::net_rates_y(T, rho, ColY{X}, c, g, w, wd);
+#pragma unroll
+  for (int k = 0; k < NS; ++k) w[k] = wd[k];
+#else
   StateScalars s;
   s.T = T;
   s.lnT = log(T);
-  s.invT = 1.0 / T;
+  s.invT = invT;
   s.c0 = LOG_P0_OVER_R - s.lnT;
   double ctot = 0.0;
   for (int k = 0; k < NS; ++k) {
@@ -74,6 +88,7 @@ __device__ __forceinline__ void cell_rhs(double P, ICols X, ICols F, ICols c,
   }
   s.ctot = ctot;
   production_rates(s, c, g, w);
+#endif
   double q = 0.0;
   for (int k = 0; k < NS; ++k) {
     const Nasa a(k, T > k_tmid[k]);
@@ -82,7 +97,7 @@ __device__ __forceinline__ void cell_rhs(double P, ICols X, ICols F, ICols c,
                           a[2] * (1.0 / 3.0)),
                   a[1] * 0.5),
             a[0]) +
-        a[5] * s.invT;
+        a[5] * invT;
     q = fma(GAS_CONSTANT * T * hrt, w[k], q);
     F[k + 1] = k_mw[k] * w[k] / rho;
   }

@@ -187,14 +187,16 @@ def _tuned():
 
 def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
              n_max: int = 1024, candidates=(32, 64, 128, 256),
-             seed: int = 0, device=None, repeats: int = 3):
+             seed: int = 0, device=None, repeats: int = 3, lengths=None):
     """Time the solve for each kernel and CTA size (the CTA kernel at each
     of *candidates*, and for nv <= 16 the one-thread-per-system kernel at 32
     and 64 systems per CTA) on a seeded sample of systems of the given
-    shape; store the fastest in the build directory's tuning file and
-    return ``{"kernel:threads": ms}``."""
+    shape (or on systems of the given *lengths*); store the fastest in the
+    build directory's tuning file and return ``{"kernel:threads": ms}``."""
     rng = np.random.default_rng(seed)
-    lengths = rng.integers(n_min, n_max + 1, size=n_systems)
+    if lengths is None:
+        lengths = rng.integers(n_min, n_max + 1, size=n_systems)
+    lengths = np.asarray(lengths, dtype=np.int64)
     dev = torch.device(device if device is not None else "cuda")
     rows = int(lengths.sum())
     gen = torch.Generator(device=dev).manual_seed(seed)
@@ -252,3 +254,157 @@ def block_thomas(lower, central, upper, rhs):
     x = solver.solve(L, C, U, b)
     solver.check_status()
     return x
+
+
+class FlameletEquations:
+    """Steady-flamelet residual and block-tridiagonal Jacobian for many
+    flamelets at once, on the GPU: the counterpart of
+    ``pyrometheus.flamelets.equations.FlameletEquations`` (``rhs``
+    ``equations.py:193-238``, ``jac`` :240-298, ``source_terms`` :340-385)
+    with the Laplacian of ``onedim_laplacian.py:144-180``.
+
+    Flamelets are packed along rows as for :class:`BlockThomasSolver`:
+    flamelet ``s`` owns ``lengths[s]`` (>= 3) consecutive grid points on a
+    uniform mixture-fraction grid of spacing ``dx[s]``.  The unknowns are
+    ``h[rows]`` and ``Y[S, rows]``; ``jac`` returns the packed ``(L, C,
+    U)`` blocks ``[rows, S+1, S+1]`` the solver takes (the last row of each
+    flamelet's ``L``/``U`` is zero and unused).  ``y_ox``/``y_fu``: ``[S]``
+    (shared) or ``[S, n_flamelets]``.
+    """
+
+    def __init__(self, thermo, lengths, dx, y_ox, y_fu, device=None):
+        self.th = thermo
+        self.S = thermo.num_species
+        self.nv = self.S + 1
+        self.device = torch.device(device if device is not None
+                                   else thermo.device)
+        lengths = np.asarray(lengths, dtype=np.int64)
+        if np.any(lengths < 3):
+            raise ValueError("every flamelet needs at least 3 grid points")
+        self.lengths = lengths
+        self.nsys = int(len(lengths))
+        offs = np.concatenate([[0], np.cumsum(lengths)])
+        self.rows = int(offs[-1])
+        dev = self.device
+        self.row_off = torch.as_tensor(offs, dtype=torch.int64, device=dev)
+        self.sys_of_row = torch.as_tensor(
+            np.repeat(np.arange(self.nsys, dtype=np.int32), lengths),
+            device=dev)
+        dx = np.broadcast_to(np.asarray(dx, dtype=np.float64), (self.nsys,))
+        self.inv_dx2 = torch.as_tensor(1.0 / dx ** 2, device=dev)
+        self.y_ox = self._bc_mat(y_ox)
+        self.y_fu = self._bc_mat(y_fu)
+
+    def _bc_mat(self, y):
+        y = torch.as_tensor(np.asarray(y, dtype=np.float64)
+                            if not torch.is_tensor(y) else y,
+                            dtype=torch.float64, device=self.device)
+        if y.dim() == 1:
+            y = y[:, None].expand(self.S, self.nsys)
+        return y.contiguous()
+
+    def _rowvec(self, x):
+        if torch.is_tensor(x):
+            x = x.to(device=self.device, dtype=torch.float64)
+        else:
+            x = torch.as_tensor(np.asarray(x, dtype=np.float64),
+                                device=self.device)
+        if x.dim() == 0:
+            x = x.expand(self.rows)
+        return x.contiguous()
+
+    def _sysvec(self, x):
+        if torch.is_tensor(x):
+            x = x.to(device=self.device, dtype=torch.float64)
+        else:
+            x = torch.as_tensor(np.asarray(x, dtype=np.float64),
+                                device=self.device)
+        if x.dim() == 0:
+            x = x.expand(self.nsys)
+        return x.contiguous()
+
+    def _state(self, h, Y):
+        h = self._rowvec(h)
+        Y = Y.to(device=self.device, dtype=torch.float64) if torch.is_tensor(
+            Y) else torch.as_tensor(np.asarray(Y, dtype=np.float64),
+                                    device=self.device)
+        if tuple(Y.shape) != (self.S, self.rows):
+            raise ValueError(f"Y must have shape {(self.S, self.rows)}")
+        return h, Y.contiguous()
+
+    def _pressure(self, pressure):
+        p = self._rowvec(pressure)
+        return p, (0 if p.stride(0) == 0 else 1)
+
+    @staticmethod
+    def _stream():
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def temperature(self, h, Y, temp_guess):
+        """T with h_mix(T, Y) = h (``equation_of_state``,
+        ``equations.py:320-338``)."""
+        return self.th.get_temperature_from_enthalpy(
+            h, Y, self._rowvec(temp_guess))
+
+    def rhs(self, h, Y, diss_rate, viscous_diss, temp_guess, pressure,
+            h_ox, h_fu, temperature=None):
+        """Residual ``[S+1, rows]`` (row 0 enthalpy, rows 1.. species)."""
+        h, Y = self._state(h, Y)
+        T = temperature if temperature is not None else \
+            self.temperature(h, Y, temp_guess)
+        p, p_inc = self._pressure(pressure)
+        F = self.th.get_reactor_source(p, T, Y)
+        chi, visc = self._rowvec(diss_rate), self._rowvec(viscous_diss)
+        hox, hfu = self._sysvec(h_ox), self._sysvec(h_fu)
+        R = torch.empty((self.nv, self.rows), dtype=torch.float64,
+                        device=self.device)
+        _check(self.th._lib.pyro_flamelet_residual(
+            p.data_ptr(), p_inc, T.data_ptr(), h.data_ptr(), Y.data_ptr(),
+            Y.stride(0), F.data_ptr(), F.stride(0), chi.data_ptr(),
+            visc.data_ptr(), self.row_off.data_ptr(),
+            self.sys_of_row.data_ptr(), self.inv_dx2.data_ptr(),
+            hox.data_ptr(), hfu.data_ptr(), self.y_ox.data_ptr(),
+            self.y_fu.data_ptr(), self.y_ox.stride(0), R.data_ptr(),
+            R.stride(0), self.rows, self._stream()), "flamelet residual")
+        return R
+
+    def jac(self, h, Y, diss_rate, viscous_diss, temp_guess, pressure,
+            temperature=None, out=None):
+        """Packed ``(L, C, U)`` blocks ``[rows, S+1, S+1]``."""
+        h, Y = self._state(h, Y)
+        T = temperature if temperature is not None else \
+            self.temperature(h, Y, temp_guess)
+        p, p_inc = self._pressure(pressure)
+        nv = self.nv
+        if out is None:
+            f64 = dict(dtype=torch.float64, device=self.device)
+            out = tuple(torch.empty((self.rows, nv, nv), **f64)
+                        for _ in range(3))
+        L, C, U = out
+        self.th.get_reactor_jacobian(p, T, Y, out=C)
+        chi, visc = self._rowvec(diss_rate), self._rowvec(viscous_diss)
+        _check(self.th._lib.pyro_flamelet_blocks(
+            p.data_ptr(), p_inc, T.data_ptr(), Y.data_ptr(), Y.stride(0),
+            chi.data_ptr(), visc.data_ptr(), self.row_off.data_ptr(),
+            self.sys_of_row.data_ptr(), self.inv_dx2.data_ptr(),
+            L.data_ptr(), C.data_ptr(), U.data_ptr(), self.rows,
+            self._stream()), "flamelet blocks")
+        return L, C, U
+
+    def newton_step(self, h, Y, diss_rate, viscous_diss, temp_guess,
+                    pressure, h_ox, h_fu, solver=None):
+        """One Newton correction for every flamelet: ``(dphi [S+1, rows],
+        R, T)`` with ``J dphi = -R``; *solver* is a
+        :class:`BlockThomasSolver` for these lengths (built on first use
+        when omitted)."""
+        h, Y = self._state(h, Y)
+        T = self.temperature(h, Y, temp_guess)
+        R = self.rhs(h, Y, diss_rate, viscous_diss, None, pressure, h_ox,
+                     h_fu, temperature=T)
+        L, C, U = self.jac(h, Y, diss_rate, viscous_diss, None, pressure,
+                           temperature=T)
+        if solver is None:
+            solver = BlockThomasSolver(self.nv, self.lengths,
+                                       device=self.device)
+        x = solver.solve(L, C, U, (-R).T.contiguous())
+        return x.T, R, T

@@ -198,6 +198,138 @@ def golden_block_thomas(fname="block_thomas.npz"):
     print(f"wrote {fname}")
 
 
+def _enthalpy_newton(th, h, y, t0, fixed_iters=None):
+    """T with h_mix(T, Y) = h: the Newton iteration of the reference's
+    ``get_temperature_from_enthalpy`` (``flamelets/make_pyro.py:255-299``:
+    T -= f / j with f = h - h_mix(T), j = -cp_mix(T), until
+    ||f / j||_2 <= 1e-10), on the reference's generated class ``th``.  With
+    *fixed_iters* it runs that many steps instead (forward-mode autodiff
+    cannot follow a data-dependent loop exit; past convergence the steps
+    change nothing)."""
+    t = t0
+    for it in range(fixed_iters or 500):
+        f = h - th.get_mixture_enthalpy_mass(t, y)
+        j = -th.get_mixture_specific_heat_cp_mass(t, y)
+        if fixed_iters is None and np.linalg.norm(f / j) <= 1e-10:
+            return t
+        t = t - f / j
+    if fixed_iters is None:
+        raise RuntimeError("enthalpy Newton did not converge")
+    return t
+
+
+def flamelet_case(sol, n_x, seed):
+    """A seeded flamelet on a uniform mixture-fraction grid: air-like
+    oxidizer, diluted-H2 fuel, a hot layer near Z = 0.3 and small radical
+    fractions, with random dissipation rates and viscous heating."""
+    rng = np.random.default_rng(seed)
+    cls = refgen.reference_class(sol)
+    ref = cls()
+    S = sol.n_species
+    idx = sol.species_index
+    z = np.linspace(0.0, 1.0, n_x)
+    dx = float(z[1] - z[0])
+    y_ox = np.zeros(S)
+    y_ox[idx("O2")], y_ox[idx("N2")] = 0.233, 0.767
+    y_fu = np.zeros(S)
+    y_fu[idx("H2")], y_fu[idx("N2")] = 0.1, 0.9
+    y = (1.0 - z)[None, :] * y_ox[:, None] + z[None, :] * y_fu[:, None]
+    noise = 1e-3 * rng.dirichlet(np.full(S, 0.5), size=n_x).T
+    y[:, 1:-1] += noise[:, 1:-1]
+    y /= y.sum(axis=0, keepdims=True)
+    t = 350.0 + 1650.0 * np.exp(-((z - 0.3) / 0.2) ** 2)
+    h = np.asarray(ref.get_mixture_enthalpy_mass(t, y), dtype=np.float64)
+    t_guess = t * (1.0 + 0.02 * rng.uniform(-1.0, 1.0, size=n_x))
+    chi = 5.0 + 20.0 * rng.random(n_x)
+    visc = 1e3 * rng.random(n_x)
+    return dict(z=z, dx=np.asarray(dx), y_ox=y_ox, y_fu=y_fu, Y=y, T=t,
+                h=h, T_guess=t_guess, chi=chi, visc=visc,
+                P=np.asarray(1e5), h_ox=np.asarray(h[0]),
+                h_fu=np.asarray(h[-1])), cls, ref
+
+
+def flamelet_residual_and_blocks(sol, case, cls, ref):
+    """The reference's ``FlameletEquations.rhs`` and ``jac``
+    (``flamelets/equations.py:167-318``) with its Laplacian block form
+    (``onedim_laplacian.py:144-180``) and source terms
+    (``equations.py:340-420``), evaluated with the reference's generated
+    class: numpy for the residual, torch + ``jacfwd`` (the stand-in for
+    the reference's ``jax.vmap(jax.jacfwd(local_source_terms))``) for the
+    per-point source Jacobian.  The assembly (masks, boundary rows,
+    dissipation scaling) is restated here because the reference's
+    ``equations.py`` imports JAX, which is not installed.  As in the
+    reference, the boundary dissipation rates are used as given
+    (``_enforce_dirichlet_bcs`` builds new arrays with ``.at[].set`` and
+    discards them)."""
+    import torch
+    from torch.func import jacfwd, vmap
+    S = sol.n_species
+    nv = S + 1
+    y, h, dx = case["Y"], case["h"], float(case["dx"])
+    n_x = y.shape[1]
+    p = float(case["P"])
+    chi, visc = case["chi"], case["visc"]
+    mw = np.asarray(ref.molecular_weights, dtype=np.float64)
+    # residual (numpy)
+    t = _enthalpy_newton(ref, h, y, case["T_guess"])
+    rho = np.asarray(ref.get_density(p, t, y))
+    w = np.array([np.broadcast_to(np.asarray(v, dtype=np.float64), (n_x,))
+                  for v in ref.get_net_production_rates(rho, t, y)])
+    src = np.vstack([visc / rho, mw[:, None] * w / rho])
+    phi = np.vstack([h, y])
+    lap = np.empty_like(phi)
+    lap[:, 0] = phi[:, 0] / dx ** 2
+    lap[:, -1] = phi[:, -1] / dx ** 2
+    lap[:, 1:-1] = (phi[:, :-2] - 2.0 * phi[:, 1:-1] + phi[:, 2:]) / dx ** 2
+    mask = np.ones(n_x)
+    mask[0] = mask[-1] = 0.0
+    bc = np.zeros_like(phi)
+    bc[0, 0], bc[0, -1] = float(case["h_ox"]), float(case["h_fu"])
+    bc[1:, 0], bc[1:, -1] = case["y_ox"], case["y_fu"]
+    resid = 0.5 * chi * lap + src * mask - bc
+    # per-point source Jacobian (torch, jacfwd)
+    th = torch_reference(cls)
+    mwt = torch.tensor(mw)
+
+    def local(x, vd, tg, pres):
+        hh, yy = x[0], x[1:]
+        tt = _enthalpy_newton(th, hh, yy, tg, fixed_iters=40)
+        rr = th.get_density(pres, tt, yy)
+        ww = th.get_net_production_rates(rr, tt, yy)
+        return torch.cat([(vd / rr)[None], mwt * ww / rr])
+
+    xs = torch.tensor(phi.T.copy())
+    sj = vmap(jacfwd(local), in_dims=(0, 0, 0, None))(
+        xs, torch.tensor(visc), torch.tensor(case["T_guess"]),
+        torch.tensor(p)).numpy()
+    eye = np.eye(nv)
+    sj[0] = 0.0
+    sj[-1] = 0.0
+    lap_c = np.stack([eye / dx ** 2] + [-2.0 * eye / dx ** 2] * (n_x - 2)
+                     + [eye / dx ** 2])
+    lap_l = np.stack([eye / dx ** 2] * (n_x - 2) + [0.0 * eye])
+    lap_u = np.stack([0.0 * eye] + [eye / dx ** 2] * (n_x - 2))
+    central = 0.5 * chi[:, None, None] * lap_c + sj
+    lower = 0.5 * chi[1:, None, None] * lap_l
+    upper = 0.5 * chi[:-1, None, None] * lap_u
+    return dict(T_solved=t, resid=resid, src=src, L=lower, C=central,
+                U=upper)
+
+
+def golden_flamelet(fname="flamelet.npz"):
+    out = {}
+    for tag, sol, n_x, seed in (
+            ("s9", synthetic.config1_mechanism(), 12, 41),
+            ("s53", synthetic.config2_mechanism(), 5, 42)):
+        case, cls, ref = flamelet_case(sol, n_x, seed)
+        case.update(flamelet_residual_and_blocks(sol, case, cls, ref))
+        case["mech_yaml"] = np.array(dump_mechanism(sol))
+        for k, v in case.items():
+            out[f"{tag}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+    print(f"wrote {fname}")
+
+
 def main():
     if not refgen.reference_available():
         raise SystemExit("reference checkout not found")
@@ -205,6 +337,7 @@ def main():
     golden(synthetic.config2_mechanism(), 48, 12, 6, "synthetic53.npz")
     golden(quirks_mechanism(), 128, 13, 12, "quirks9.npz")
     golden_block_thomas()
+    golden_flamelet()
 
 
 if __name__ == "__main__":
