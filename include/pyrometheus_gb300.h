@@ -174,6 +174,41 @@ int pyro_reactor_bdf2(double* y, double* y_prev, double* f_n, int64_t ld,
                       double rtol, double atol, int64_t max_attempts,
                       cudaStream_t stream);
 
+/* Steady-flamelet residual, R[nv][ldr] = chi/2 Lap(phi) + S(phi) m - BC,
+ * for flamelets packed along rows (system s owns rows [row_off[s],
+ * row_off[s+1]), at least 3; sys_of_row[rows] gives s; uniform grid with
+ * inv_dx2[s] = 1/dx^2): FlameletEquations.rhs,
+ * pyrometheus/flamelets/equations.py:193-238, with the Laplacian of
+ * onedim_laplacian.py:182-212 and source_terms equations.py:340-385.
+ * Inputs: T[rows] (from get_temperature_from_enthalpy), h[rows],
+ * Y[S][ldy], F[S+1][ldf] the reactor source at (p, T, Y) (rows 1.. are
+ * W_k w_k / rho), chi and visc [rows], h_ox/h_fu [nsys], y_ox/y_fu
+ * [S][ldb] (ldb >= nsys). */
+int pyro_flamelet_residual(const double* p, int64_t p_inc, const double* T,
+                           const double* h, const double* Y, int64_t ldy,
+                           const double* F, int64_t ldf, const double* chi,
+                           const double* visc, const int64_t* row_off,
+                           const int* sys_of_row, const double* inv_dx2,
+                           const double* h_ox, const double* h_fu,
+                           const double* y_ox, const double* y_fu,
+                           int64_t ldb, double* R, int64_t ldr, int64_t rows,
+                           cudaStream_t stream);
+
+/* Block-tridiagonal Jacobian of that residual w.r.t. (h, Y):
+ * FlameletEquations.jac, equations.py:240-298, and
+ * Laplacian.assemble_block_form, onedim_laplacian.py:144-180.  On entry
+ * C[rows][nv][nv] holds pyro_reactor_jacobian at (p, T, Y); it is turned in
+ * place into the central blocks (chain rule through T(h, Y), viscous
+ * enthalpy row, zero source blocks at the boundary points, chi/2 times the
+ * Laplacian diagonal); L and U receive the packed sub/super-diagonal blocks
+ * pyro_block_thomas takes (the last row of each flamelet zero). */
+int pyro_flamelet_blocks(const double* p, int64_t p_inc, const double* T,
+                         const double* Y, int64_t ldy, const double* chi,
+                         const double* visc, const int64_t* row_off,
+                         const int* sys_of_row, const double* inv_dx2,
+                         double* L, double* C, double* U, int64_t rows,
+                         cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -142,16 +142,13 @@ class BlockThomasSolver:
 
 def default_threads(nv: int) -> int:
     """CTA size of the one-CTA-per-system kernel: from the autotuner cache
-    when it holds one, else one warp for small blocks and up to 128 threads
-    for larger ones."""
+    when it holds one, else the sizes the autotuner picks on GB300."""
     best = _tuned().get(str(nv))
     if best and not str(best).startswith("small"):
         return int(str(best).split(":")[-1])
-    if nv <= 12:
-        return 32
-    if nv <= 24:
-        return 64
-    return 128
+    # the autotuner's choices on GB300 for 4,096 systems of 64..1024 rows:
+    # 128 threads at nv = 10, 256 at nv = 54
+    return 128 if nv <= 24 else 256
 
 
 def _small_threads(nv: int) -> int:
@@ -162,13 +159,12 @@ def _small_threads(nv: int) -> int:
 
 def default_plan(nv: int):
     """(kernel, threads): the autotuner's choice when cached, else the
-    one-thread-per-system kernel for nv <= 16 and the CTA kernel above."""
+    one-CTA-per-system kernel (the one-thread-per-system kernel only pays
+    off with tens of thousands of systems)."""
     best = _tuned().get(str(nv))
     if best:
         kind, _, th = str(best).rpartition(":")
         return (kind or "cta"), int(th)
-    if nv <= 16:
-        return "small", _small_threads(nv)
     return "cta", default_threads(nv)
 
 

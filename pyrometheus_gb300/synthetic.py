@@ -377,3 +377,44 @@ def density(sol: Solution, p, t, y):
 # }}}
 
 # vim: foldmethod=marker
+
+
+# {{{ flamelets
+
+def flamelet_profiles(sol: Solution, lengths, seed: int = 0,
+                      chi_max: float = 10.0, t_peak: float = 2000.0):
+    """Seeded steady-flamelet initial states on uniform mixture-fraction
+    grids, packed along rows: oxidizer Y = (O2 0.233, N2 0.767), fuel
+    Y = (H2 0.1, N2 0.9), linear mixing plus 1e-3 of seeded radical
+    fractions inside, a hot layer T = 300 + (t_peak - 300)
+    exp(-((Z - Z_p) / 0.15)^2) around a seeded Z_p in [0.2, 0.4], and a
+    dissipation rate chi = chi_max exp(-((Z - 0.5) / 0.3)^2).
+
+    Returns a dict with ``Y`` [S, rows], ``T`` [rows] (temperature profile;
+    the caller turns it into the enthalpy unknown), ``chi`` [rows],
+    ``dx`` [n_flamelets], ``y_ox``, ``y_fu`` [S]."""
+    rng = np.random.default_rng(seed)
+    S = sol.n_species
+    idx = sol.species_index
+    y_ox = np.zeros(S)
+    y_ox[idx("O2")], y_ox[idx("N2")] = 0.233, 0.767
+    y_fu = np.zeros(S)
+    y_fu[idx("H2")], y_fu[idx("N2")] = 0.1, 0.9
+    ys, ts, chis, dxs = [], [], [], []
+    for n in np.asarray(lengths, dtype=np.int64):
+        n = int(n)
+        z = np.linspace(0.0, 1.0, n)
+        y = (1.0 - z)[None, :] * y_ox[:, None] + z[None, :] * y_fu[:, None]
+        noise = 1e-3 * rng.dirichlet(np.full(S, 0.5), size=n).T
+        y[:, 1:-1] += noise[:, 1:-1]
+        y /= y.sum(axis=0, keepdims=True)
+        zp = rng.uniform(0.2, 0.4)
+        ts.append(300.0 + (t_peak - 300.0) * np.exp(-((z - zp) / 0.15) ** 2))
+        chis.append(chi_max * np.exp(-((z - 0.5) / 0.3) ** 2))
+        ys.append(y)
+        dxs.append(1.0 / (n - 1))
+    return dict(Y=np.hstack(ys), T=np.concatenate(ts),
+                chi=np.concatenate(chis), dx=np.asarray(dxs), y_ox=y_ox,
+                y_fu=y_fu)
+
+# }}}
