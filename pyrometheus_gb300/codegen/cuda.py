@@ -267,7 +267,9 @@ class _Emitter:
         output element and split into 32 contiguous, equally long runs, one
         per lane, so each element is summed by one lane in a fixed order
         and stored once (no atomics, no divergent trip counts); elements
-        without contributions get one entry from a zero source."""
+        without contributions are listed separately and zeroed with plain
+        stores.  Species -> third-body entries give the column sums the
+        assembly needs without reading the block back."""
         m = self.m
         S, R = m.S, m.R
         nc = S + 1
@@ -305,11 +307,9 @@ class _Emitter:
                         entries.append(((sp[b] + 1) * nc + tb_idx[t] + 1,
                                         nslot + qq, nu[b] * tb_de[t]))
         have = {e[0] for e in entries}
-        for k in range(S):
-            for mm in range(S):
-                off = (k + 1) * nc + mm + 1
-                if off not in have:
-                    entries.append((off, zero_src, 0.0))
+        zero_offs = [(k + 1) * nc + mm + 1 for k in range(S)
+                     for mm in range(S)
+                     if (k + 1) * nc + mm + 1 not in have]
         entries.sort(key=lambda e: e[0])
         groups: List[List[Tuple[int, int, float]]] = []
         for e in entries:
@@ -336,6 +336,21 @@ class _Emitter:
                 u_off.append(o)
                 u_src.append(s)
                 u_coef.append(c)
+        # elements of dw/dc without contributions: plain zero stores
+        ziters = max(1, -(-len(zero_offs) // 32))
+        z_off = [zero_offs[it * 32 + ln] if it * 32 + ln < len(zero_offs)
+                 else 0xFFFF for it in range(ziters) for ln in range(32)]
+        # species -> third-body entries (permuted reaction, e - default)
+        stinc: List[List[Tuple[int, float]]] = [[] for _ in range(S)]
+        for qq, j in enumerate(perm):
+            for t in range(tb_start[j], tb_start[j + 1]):
+                stinc[tb_idx[t]].append((qq, tb_de[t]))
+        st0, st_q, st_de = [0], [], []
+        for k in range(S):
+            for qq, de in stinc[k]:
+                st_q.append(qq)
+                st_de.append(de)
+            st0.append(len(st_q))
         # third-body efficiency entries, in permuted reaction order
         q_tb0, q_tbidx, q_tbde = [0], [], []
         for j in perm:
@@ -354,7 +369,7 @@ class _Emitter:
         nf = max(1, len(fo_low))
         nasa = [[m.tmid[k]] + list(m.hi[k]) + list(m.lo[k]) + [0.0]
                 for k in range(S)]
-        jw_doubles = 9 * S + 2 * R + nslot + R + 1
+        jw_doubles = 9 * S + 4 * R + nslot + R + 1
         jwarps = max(1, min(16, (227 * 1024 - 16384) // (8 * jw_doubles)))
 
         def arr(ctype, name, dims, vals):
@@ -365,6 +380,7 @@ class _Emitter:
         w("// Jacobian kernel tables (global memory; see jacobian.cuh)")
         w(f"#define NSLOT {nslot}")
         w(f"#define JU_ITERS {iters}")
+        w(f"#define JZ_ITERS {ziters}")
         w(f"#define JD_ZERO {zero_src}")
         w(f"#define JW_DOUBLES {jw_doubles}")
         w(f"#define JWARPS {jwarps}")
@@ -404,6 +420,13 @@ class _Emitter:
                for row in nasa]))
         w(arr("double", "jg_mw", [S], [_hexd(v) for v in m.W]))
         w(arr("double", "jg_invmw", [S], [_hexd(v) for v in m.invW]))
+        w(arr("int", "jg_st0", [S + 1], [_cint(v) for v in st0]))
+        w(arr("int", "jg_st_q", [max(1, len(st_q))],
+              [_cint(v) for v in (st_q or [0])]))
+        w(arr("double", "jg_st_de", [max(1, len(st_de))],
+              [_hexd(v) for v in (st_de or [0.0])]))
+        w(arr("unsigned short", "jz_off", [32 * ziters],
+              [_cint(v) for v in z_off]))
         w(arr("unsigned short", "ju_off", [32 * iters],
               [_cint(v) for v in u_off]))
         w(arr("unsigned short", "ju_src", [32 * iters],

@@ -263,11 +263,15 @@ namespace pyro {
 
 // Rate-of-progress derivatives of reaction qq (permuted numbering) from the
 // global Jacobian tables: q, dq/dT at fixed c, dq/dM, and per slot s of the
-// reaction dq/dc_{sp(s)} into D[s]; dq/dM goes to D[NSLOT + qq].
+// reaction dq/dc_{sp(s)} into D[s]; dq/dM goes to D[NSLOT + qq].  Also
+// Hq = sum over slots of nu h/RT, and Qc = sum_m dq/dc_m c_m over the
+// explicit (non-default) concentration dependences, from which the
+// assembly forms the column sums of the block without reading it back.
 template <class CT>
 __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
                                              CT c, CT g, CT h, double* D,
-                                             double* Dq, double* DdT) {
+                                             double* Dq, double* DdT,
+                                             double* Hq, double* Qc) {
   const double T = s.T, lnT = s.lnT, invT = s.invT;
   const int f = __ldg(jq_flags + qq);
   const int kind = f & RX_KIND_MASK;
@@ -276,13 +280,16 @@ __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
   const int s1 = s0 + __ldg(jq_nr + qq);
   const double p0 = __ldg(&jq_rate[0][qq]), p1 = __ldg(&jq_rate[1][qq]),
                p2 = __ldg(&jq_rate[2][qq]);
-  double m = 1.0;
+  double m = 1.0, mt = 0.0;
   if (kind != RX_ELEMENTARY) {
     const double d = __ldg(jq_defeff + qq);
     m = d == 0.0 ? 0.0 : (d == 1.0 ? s.ctot : d * s.ctot);
     const int t1 = __ldg(jq_tb0 + qq + 1);
-    for (int t = __ldg(jq_tb0 + qq); t < t1; ++t)
-      m = fma(__ldg(jq_tbde + t), c[__ldg(jq_tbidx + t)], m);
+    for (int t = __ldg(jq_tb0 + qq); t < t1; ++t) {
+      const double v = __ldg(jq_tbde + t) * c[__ldg(jq_tbidx + t)];
+      m += v;
+      mt += v;
+    }
   }
   double kf, x = 0.0, dlnkf, dkfdM = 0.0;
   bool exp_form = false;
@@ -379,7 +386,10 @@ __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
   }
   Dq[qq] = kf * pf - kr * pv;
   DdT[qq] = kf * dlnkf * pf - kr * dlnkr * pv;
-  D[NSLOT + qq] = dkfdM * pf - dkrdM * pv;
+  const double dqdm = dkfdM * pf - dkrdM * pv;
+  D[NSLOT + qq] = dqdm;
+  Hq[qq] = shh;
+  double qc = dqdm * mt;
   // dq/dc per slot: kf d(prod c^e)/dc (reactants), -kr d(prod c^nu'')/dc
   for (int a = s0; a < s2; ++a) {
     const bool rside = a < s1;
@@ -400,14 +410,17 @@ __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
       d = 2.0 * cm;
     else
       d = ea * pow(cm, ea - 1.0);
-    D[a] = rside ? kf * (d * others) : -kr * (d * others);
+    const double da = rside ? kf * (d * others) : -kr * (d * others);
+    D[a] = da;
+    qc = fma(da, cm, qc);
   }
+  Qc[qq] = qc;
 }
 
 }  // namespace pyro
 
 // doubles of shared memory per warp (JW_DOUBLES, from the tables):
-//   c, h, g, cp, w, jt, a, u, shj [NS each]; q, dq/dT [NR each];
+//   c, h, g, cp, w, jt, a, u, shj [NS each]; q, dq/dT, Hq, Qc [NR each];
 //   D = dq/dc per slot [NSLOT], dq/dM per reaction [NR], one zero.
 __global__ void __launch_bounds__(JWARPS * 32)
     k_reactor_jacobian(const double* __restrict__ Pp, int64_t p_inc,
@@ -419,16 +432,18 @@ __global__ void __launch_bounds__(JWARPS * 32)
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double* sc = smem + (size_t)wid * JW_DOUBLES;
   double* sh = sc + NS;
-  double* sg = sh + NS;
+  double* sg = sh + NS;   // g/RT, later the row constants B_k
   double* scp = sg + NS;
   double* sw = scp + NS;
-  double* sjt = sw + NS;
+  double* sjt = sw + NS;  // later the column-0 values
   double* sa = sjt + NS;
   double* su = sa + NS;
   double* shj = su + NS;
   double* Dq = shj + NS;
   double* DdT = Dq + NR;
-  double* D = DdT + NR;  // [NSLOT] dq/dc, [NR] dq/dM, [1] zero
+  double* Hq = DdT + NR;
+  double* Qc = Hq + NR;
+  double* D = Qc + NR;  // [NSLOT] dq/dc, [NR] dq/dM, [1] zero
   using LC = pyro::LocalCols;
   const LC c{sc}, g{sg}, h{sh};
   constexpr int NC = NS + 1;
@@ -491,10 +506,15 @@ __global__ void __launch_bounds__(JWARPS * 32)
     __syncwarp();
     // per reaction (lanes over the kind-sorted numbering)
     for (int qq = lane; qq < NR; qq += 32)
-      pyro::jac_reaction(qq, s, c, g, h, D, Dq, DdT);
+      pyro::jac_reaction(qq, s, c, g, h, D, Dq, DdT, Hq, Qc);
     __syncwarp();
-    // dw/dc into the interior of this state's output block: each lane sums
-    // its run of the update list and stores every element it owns once
+    // dw/dc into the interior of this state's output block: elements
+    // without contributions are zeroed, the others summed by the lane that
+    // owns them (its run of the update list) and stored once
+    for (int it = 0; it < JZ_ITERS; ++it) {
+      const int off = __ldg(jz_off + it * 32 + lane);
+      if (off != 0xFFFF) Ji[off] = 0.0;
+    }
     {
       int cur = -1;
       double acc = 0.0;
@@ -512,9 +532,15 @@ __global__ void __launch_bounds__(JWARPS * 32)
       }
       if (cur >= 0 && cur != 0xFFFF) Ji[cur] = acc;
     }
-    // per species: w_k, dw_k/dT|c, rank-1 third-body vector a_k
+    // per species k: w_k, dw_k/dT|c, the rank-1 third-body vector a_k,
+    // u_k = sum_m dw_k/dc_m c_m and the column sum
+    // shj_k = RT sum_j h_j dw_j/dc_k, from per-reaction sums; then the
+    // row constants of the assembly
+    const double RT = GAS_CONSTANT * T;
+    const double inv_sig = 1.0 / sigma;
+    double pQ = 0.0, pHA = 0.0, pHU = 0.0, pdQ = 0.0;
     for (int k = lane; k < NS; k += 32) {
-      double w = 0.0, jt = 0.0, a = 0.0;
+      double w = 0.0, jt = 0.0, a = 0.0, u = 0.0, hj = 0.0;
       const int t1 = __ldg(jg_si0 + k + 1);
       for (int t = __ldg(jg_si0 + k); t < t1; ++t) {
         const int sl = __ldg(jg_si_slot + t);
@@ -523,44 +549,38 @@ __global__ void __launch_bounds__(JWARPS * 32)
         w = fma(nu, Dq[qq], w);
         jt = fma(nu, DdT[qq], jt);
         a = fma(__ldg(jq_slot_anu + sl), D[NSLOT + qq], a);
+        u = fma(nu, Qc[qq], u);
+        hj = fma(Hq[qq], D[sl], hj);
       }
+      const int e1 = __ldg(jg_st0 + k + 1);
+      for (int t = __ldg(jg_st0 + k); t < e1; ++t) {
+        const int qq = __ldg(jg_st_q + t);
+        hj = fma(Hq[qq] * __ldg(jg_st_de + t), D[NSLOT + qq], hj);
+      }
+      u = fma(a, s.ctot, u);
       sw[k] = w;
-      sjt[k] = jt;
       sa[k] = a;
-    }
-    // the output-block writes above are by other lanes: make them visible
-    __threadfence_block();
-    __syncwarp();
-#define Jc(k, m) Ji[(int64_t)((k) + 1) * NC + (m) + 1]
-    const double RT = GAS_CONSTANT * T;
-    // u_k = sum_m dw_k/dc_m c_m (+ rank-1 part); shj_m = RT sum_k h_k Jc
-    for (int k = 0; k < NS; ++k) {
-      double u = 0.0;
-      for (int mm = lane; mm < NS; mm += 32) u = fma(Jc(k, mm), sc[mm], u);
-      u = pyro::warp_sum(u);
-      if (lane == 0) su[k] = fma(sa[k], s.ctot, u);
-    }
-    for (int jj = lane; jj < NS; jj += 32) {
-      double acc = 0.0;
-      for (int k = 0; k < NS; ++k) acc = fma(sh[k], Jc(k, jj), acc);
-      shj[jj] = RT * acc;
-    }
-    __syncwarp();
-    double pQ = 0.0, pHA = 0.0, pHU = 0.0, pdQ = 0.0;
-    for (int k = lane; k < NS; k += 32) {
+      su[k] = u;
+      shj[k] = RT * hj;
       const double Hk = RT * sh[k];
-      pQ = fma(Hk, sw[k], pQ);
-      pHA = fma(Hk, sa[k], pHA);
-      pHU = fma(Hk, su[k], pHU);
+      pQ = fma(Hk, w, pQ);
+      pHA = fma(Hk, a, pHA);
+      pHU = fma(Hk, u, pHU);
       // dQ/dT = sum_k (R cp_k w_k + H_k (dw_k/dT|c - u_k / T))
-      pdQ += GAS_CONSTANT * scp[k] * sw[k] + Hk * (sjt[k] - su[k] * invT);
+      pdQ += GAS_CONSTANT * scp[k] * w + Hk * (jt - u * invT);
+      const double wk_rho = __ldg(jg_mw + k) / rho;
+      sg[k] = wk_rho * fma(a, rho, (w - u) * inv_sig);  // B_k
+      sjt[k] = wk_rho * (jt - u * invT + w * invT);     // column 0
     }
     const double Q = pyro::warp_sum(pQ), HA = pyro::warp_sum(pHA);
     const double HU = pyro::warp_sum(pHU), dQdT = pyro::warp_sum(pdQ);
     const double rcp = rho * cpm;
     const double inv_rcp = 1.0 / rcp;
     const double qr2 = Q * inv_rcp * inv_rcp;
-    const double inv_sig = 1.0 / sigma;
+    // the output-block writes above are by other lanes: make them visible
+    __threadfence_block();
+    __syncwarp();
+#define Jc(k, m) Ji[(int64_t)((k) + 1) * NC + (m) + 1]
     // row 0: d(dT/dt)/dx
     for (int col = lane; col < NC; col += 32) {
       double v;
@@ -578,18 +598,17 @@ __global__ void __launch_bounds__(JWARPS * 32)
     }
     // rows 1..S: d(dY_k/dt)/dx = W_k/rho ((Jc + a_k) rho / W_m
     //                                     + (w_k - u_k) / (sigma W_m))
+    //          = (W_k Jc + B_k) / W_m
     for (int k = 0; k < NS; ++k) {
-      const double wk_rho = __ldg(jg_mw + k) / rho;
-      const double wk = sw[k], uk = su[k];
-      const double A = wk_rho * rho;
-      const double B = wk_rho * fma(sa[k], rho, (wk - uk) * inv_sig);
+      const double A = __ldg(jg_mw + k);
+      const double Bk = sg[k];
       for (int col = lane; col < NC; col += 32) {
         double v;
         if (col == 0) {
-          v = wk_rho * (sjt[k] - uk * invT + wk * invT);
+          v = sjt[k];
         } else {
           const int jj = col - 1;
-          v = __ldg(jg_invmw + jj) * fma(A, Jc(k, jj), B);
+          v = __ldg(jg_invmw + jj) * fma(A, Jc(k, jj), Bk);
         }
         Ji[(int64_t)(k + 1) * NC + col] = v;
       }
