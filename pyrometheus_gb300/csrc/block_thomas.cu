@@ -69,6 +69,10 @@ __device__ void lu_factor(double* A, int ld, int nv, int* piv,
       }
       if (threadIdx.x == 0) {
         red_v[0] = best;
+        // the pivot's reciprocal, once for the CTA (the FP64 pipe is
+        // narrow: a division repeated by every thread costs more than the
+        // whole elimination step of a small block)
+        red_v[1] = 1.0 / A[bi * ld + k];
         red_i[0] = bi;
         piv[k] = bi;
         if (best == 0.0) *singular = 1;
@@ -76,6 +80,7 @@ __device__ void lu_factor(double* A, int ld, int nv, int* piv,
     }
     __syncthreads();
     const int p = red_i[0];
+    const double inv = red_v[1];
     if (p != k) {
       for (int j = threadIdx.x; j < nv; j += blockDim.x) {
         const double t = A[k * ld + j];
@@ -84,7 +89,6 @@ __device__ void lu_factor(double* A, int ld, int nv, int* piv,
       }
       __syncthreads();
     }
-    const double inv = 1.0 / A[k * ld + k];
     for (int i = k + 1 + threadIdx.x; i < nv; i += blockDim.x)
       A[i * ld + k] *= inv;
     __syncthreads();
@@ -124,9 +128,13 @@ __device__ void lu_solve(const double* A, double* R, int ld, int nv,
     }
     __syncthreads();
   }
-  // backward, upper
+  // backward, upper (the diagonal reciprocals once, in parallel)
+  __shared__ double s_invd[64];
+  for (int k = threadIdx.x; k < nv; k += blockDim.x)
+    s_invd[k] = 1.0 / A[k * ld + k];
+  __syncthreads();
   for (int k = nv - 1; k >= 0; --k) {
-    const double inv = 1.0 / A[k * ld + k];
+    const double inv = s_invd[k];
     for (int c = col0 + threadIdx.x; c < col0 + ncol; c += blockDim.x)
       R[k * ld + c] *= inv;
     __syncthreads();
