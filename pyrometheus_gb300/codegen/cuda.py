@@ -675,9 +675,9 @@ class _Emitter:
         w('#include "kinetics_abi.cuh"')
         # fused per-cell reactor integrator: threads per CTA so that seven
         # per-thread columns (3 NS + 4 (NS + 1) doubles) fit beside the exp
-        # table in 227 KB of shared memory
+        # and log tables (19,480 bytes) in 227 KB of shared memory
         per_thread = (3 * S + 4 * (S + 1)) * 8
-        iblock = max(32, min(128, ((227 - 16) * 1024 // per_thread)
+        iblock = max(32, min(128, ((227 * 1024 - 19480) // per_thread)
                              // 32 * 32))
         w(f"#define IBLOCK {iblock}")
         if self.opts.unrolled and S <= 16:
@@ -810,10 +810,11 @@ class _UnrolledEmitter:
                 if len(r.fc) == 4:
                     terms.append(self.troe_term(-r.fc[3], "invT", 1.0))
                 terms = [t for t in terms if t is not None] or ["0.0"]
-                w(f"    const double log_fc = log10({' + '.join(terms)});")
+                w(f"    const double log_fc = pyro_log10({' + '.join(terms)});")
                 w("    double fac = -1.0 / 0.14;")
                 w("    if (pr > 0.0) {")
-                w("      const double xx = log10(pr) + (-0.4 - 0.67 * log_fc);")
+                w("      const double xx = pyro_log10(pr) + (-0.4 - 0.67 * "
+                  "log_fc);")
                 w("      fac = xx / ((0.75 - 1.27 * log_fc) - 0.14 * xx);")
                 w("    }")
                 w("    const double blend = fx(log_fc / (1.0 + fac * fac) * "
@@ -884,7 +885,7 @@ class _UnrolledEmitter:
         w("template <class YA, class CT>")
         w("__device__ __forceinline__ void net_rates_y(double T, double rho, "
           "const YA& Y, CT c, CT g, CT w, double (&wd)[NS]) {")
-        w("  const double lnT = log(T);")
+        w("  const double lnT = pyro_log(T);")
         w("  const double invT = 1.0 / T;")
         w("  const double c0 = LOG_P0_OVER_R - lnT;")
         w("  double ctot = 0.0;")

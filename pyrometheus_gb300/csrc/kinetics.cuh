@@ -37,7 +37,7 @@
 #define PEXP(x) pyro_exp(x)
 #define PEXP10(x) pyro_exp10(x)
 #define PEXP_PRELOAD() PYRO_EXP_PRELOAD()
-#define PYRO_STATIC_SMEM (PYRO_EXP_N * sizeof(double))
+#define PYRO_STATIC_SMEM PYRO_TABLES_SMEM
 #else
 #define PYRO_STATIC_SMEM 0
 #define PEXP(x) exp(x)

@@ -27,6 +27,7 @@ __global__ void __launch_bounds__(HOT_BLOCK)
                              int64_t ldw, int64_t n) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
+  PYRO_LOG_PRELOAD();
   const auto c = hcol(smem, 0), g = hcol(smem, 1),
              w = hcol(smem, PYRO_HOT_COLS - 1);
   PYRO_HLOOP(i) {
@@ -50,6 +51,7 @@ __global__ void __launch_bounds__(HOT_BLOCK)
                    int64_t n) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
+  PYRO_LOG_PRELOAD();
   const auto c = hcol(smem, 0), g = hcol(smem, 1),
              w = hcol(smem, PYRO_HOT_COLS - 1);
   PYRO_HLOOP(i) {

@@ -32,3 +32,30 @@ PYRO_EXPORT int pyro_exp_check(const double* x, double* mine, double* ref,
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
+
+namespace {
+
+__global__ void k_logcheck(const double* __restrict__ x, double* mine,
+                           double* ref, int ten, int64_t n) {
+  PYRO_LOG_PRELOAD();
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    mine[i] = ten ? pyro_log10(v) : pyro_log(v);
+    ref[i] = ten ? log10(v) : log(v);
+  }
+}
+
+}  // namespace
+
+// mine[i] = pyro_log(x[i]) (pyro_log10 when ten != 0), ref[i] = CUDA's
+// log (log10).  Device pointers; asynchronous on stream.
+PYRO_EXPORT int pyro_log_check(const double* x, double* mine, double* ref,
+                               int ten, int64_t n, cudaStream_t stream) {
+  if (n < 0 || (n > 0 && (!x || !mine || !ref))) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  k_logcheck<<<pyro_grid(n, 256, pyro_sm_count() * 4), 256, 0, stream>>>(
+      x, mine, ref, ten, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}

@@ -54,3 +54,63 @@ __device__ __forceinline__ double pyro_exp(double x) {
 __device__ __forceinline__ double pyro_exp10(double x) {
   return pyro_exp(x * 2.302585092994045684);
 }
+
+// Table-driven double-precision logarithm (the logarithm counterpart of the
+// method above: P. T. P. Tang, "Table-driven implementation of the
+// logarithm function in IEEE floating-point arithmetic", ACM TOMS 16(4),
+// 1990), for the Troe blending of the straight-line rate kernels:
+//
+//   x = 2^m y, y in [1, 2);  F = 1 + j/128 nearest to y, f = y - F (exact),
+//   |f| <= 1/256 + 2^-20,  u = f * (1/F),
+//   ln x = m ln2 + ln F + ln(1 + u),
+//   ln(1 + u) ~= u - u^2/2 + ... - u^6/6 + u^7/7  (truncation < 2e-18 u).
+//
+// 1/F and ln F (as hi + lo) are correctly rounded (log_table.cuh) and
+// staged in shared memory; ln 2 is split so m * LN2_HI is exact.  About 14
+// FP64 instructions per call.  Zero, negative, subnormal, infinite and nan
+// arguments go to CUDA's log.
+#include "log_table.cuh"
+
+__shared__ double pyro_log_smem[3 * (PYRO_LOG_N + 1)];
+
+// Every kernel that calls pyro_log / pyro_log10 stages the table first.
+#define PYRO_LOG_PRELOAD()                                                 \
+  do {                                                                     \
+    for (int q_ = threadIdx.x; q_ < 3 * (PYRO_LOG_N + 1); q_ += blockDim.x) \
+      pyro_log_smem[q_] = pyro_log_table[q_];                              \
+    __syncthreads();                                                       \
+  } while (0)
+
+// shared memory the two tables take per block
+#define PYRO_TABLES_SMEM \
+  ((PYRO_EXP_N + 3 * (PYRO_LOG_N + 1)) * sizeof(double))
+
+__device__ __forceinline__ double pyro_log(double x) {
+  const int hx = __double2hiint(x);
+  if (hx < 0x00100000 || hx >= 0x7ff00000) return log(x);
+  const int mant = hx & 0x000fffff;
+  const int m = (hx >> 20) - 1023;
+  const double y = __hiloint2double(mant | 0x3ff00000, __double2loint(x));
+  const int j = (mant + (1 << 12)) >> 13;  // nearest j/128, 0..128
+  const double F = (double)(PYRO_LOG_N + j) * (1.0 / PYRO_LOG_N);
+  const double f = y - F;
+  const double* t = pyro_log_smem + 3 * j;
+  const double u = f * t[0];
+  // ln(1 + u) = u + u^2 (-1/2 + u (1/3 + u (-1/4 + u (1/5 + u (-1/6 +
+  // u / 7)))))
+  const double lp = fma(u * u, fma(u, fma(u, fma(u, fma(u, fma(u, 1.0 / 7.0,
+                                                               -1.0 / 6.0),
+                                                        1.0 / 5.0),
+                                                 -1.0 / 4.0),
+                                          1.0 / 3.0),
+                                   -0.5),
+                        u);
+  const double md = (double)m;
+  const double hi = fma(md, PYRO_LOG_LN2_HI, t[1]);
+  const double lo = fma(md, PYRO_LOG_LN2_LO, t[2]) + lp;
+  return hi + lo;
+}
+
+__device__ __forceinline__ double pyro_log10(double x) {
+  return pyro_log(x) * PYRO_LOG_INV_LN10;
+}

@@ -126,6 +126,9 @@ __global__ void __launch_bounds__(IBLOCK)
                    int64_t max_attempts) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
+#if defined(PYRO_UNROLLED) && defined(PYRO_BDF2_UNROLLED)
+  PYRO_LOG_PRELOAD();
+#endif
   using pyro::ICols;
   const ICols c = pyro::icol(smem, 0), g = pyro::icol(smem, NS),
               w = pyro::icol(smem, 2 * NS);

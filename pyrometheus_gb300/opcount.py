@@ -8,9 +8,9 @@ arithmetic as 1 flop, FMA as 2, division as 1 -- and, separately, the
 transcendental calls (``exp``, ``log``, ``log10``, ``exp10``, ``pow``).
 
 A transcendental is charged the FP64 flops of the implementation the
-kernels use: the table-driven exponential (14 flops per call, see
-``csrc/pyro_math.cuh``) and, for ``log``/``log10``, CUDA's libm at the
-FP64-pipe cost the benchmark measures (``DFMA FLOP/s / log/s``).  Then
+kernels use: the table-driven exponential and logarithm (14 and 22 flops
+per call, see ``csrc/pyro_math.cuh``) and, for ``pow``, CUDA's libm log at
+the FP64-pipe cost the benchmark measures (``DFMA FLOP/s / log/s``).  Then
 ``algorithmic flops / kernel time / DFMA peak`` is the fraction of the FP64
 pipe's FMA throughput doing the algorithm's work (additions and
 multiplications count one flop for a full pipe slot, so a perfectly busy
@@ -146,15 +146,20 @@ def libm_weights(dfma_flops: float, exp_rate: float, log_rate: float
 #: (csrc/pyro_math.cuh): 6 FMAs, one add, one multiply.
 TANG_EXP_FLOPS = 14.0
 
+#: FP64 flops of one call of the table-driven logarithm
+#: (csrc/pyro_math.cuh): 8 FMAs, three multiplies, three adds (the two
+#: int-to-double conversions are not counted).
+TANG_LOG_FLOPS = 22.0
+
 
 def kernel_weights(dfma_flops: float, log_rate: float) -> Dict[str, float]:
-    """Flops charged per transcendental as the kernels evaluate them:
-    ``exp`` and ``10^x`` by the table method (14 flops, +1 for the ln 10
-    scaling), ``log``/``log10``/``pow`` by CUDA's libm at its measured
-    FP64-pipe cost."""
+    """Flops charged per transcendental as the straight-line kernels
+    evaluate them: ``exp``, ``10^x``, ``log`` and ``log10`` by the table
+    methods (+1 flop for the ln 10 scalings), ``pow`` by CUDA's libm log
+    at its measured FP64-pipe cost plus the table exponential."""
     w_log = dfma_flops / log_rate
     return {"exp": TANG_EXP_FLOPS, "exp10": TANG_EXP_FLOPS + 1.0,
-            "log": w_log, "log10": w_log + 1.0,
+            "log": TANG_LOG_FLOPS, "log10": TANG_LOG_FLOPS + 1.0,
             "pow": w_log + TANG_EXP_FLOPS}
 
 

@@ -1,5 +1,6 @@
-"""The table-driven exponential (Tang 1989, csrc/pyro_math.cuh) against
-CUDA's double-precision exp/exp10 on the device."""
+"""The table-driven exponential (Tang 1989) and logarithm (Tang 1990) of
+csrc/pyro_math.cuh against CUDA's double-precision exp/exp10/log/log10 on
+the device."""
 
 import numpy as np
 import pytest
@@ -8,14 +9,14 @@ torch = pytest.importorskip("torch")
 pytestmark = pytest.mark.gpu
 
 
-def _run(x, ten):
+def _run(x, ten, fn="pyro_exp_check"):
     from pyrometheus_gb300 import native
     if not torch.cuda.is_available():
         pytest.fail("CUDA device required for the gpu tests")
     xd = torch.as_tensor(x, dtype=torch.float64, device="cuda")
     mine = torch.empty_like(xd)
     ref = torch.empty_like(xd)
-    st = native.mathcheck_lib().pyro_exp_check(
+    st = getattr(native.mathcheck_lib(), fn)(
         xd.data_ptr(), mine.data_ptr(), ref.data_ptr(), int(ten), xd.numel(),
         torch.cuda.current_stream().cuda_stream)
     assert st == 0
@@ -52,3 +53,25 @@ def test_exp10_against_cuda():
     rel = np.abs(mine - ref) / ref
     # exp(x ln10) carries the rounding of x ln10: |x| ln10 ulp-relative
     assert rel.max() < 1e-14, rel.max()
+
+
+def test_log_against_cuda():
+    rng = np.random.default_rng(2)
+    x = np.concatenate([
+        10.0 ** rng.uniform(-307.0, 308.0, 2_000_000),
+        rng.uniform(0.5, 2.0, 1_000_000),
+        1.0 + rng.uniform(-1e-6, 1e-6, 100_000),
+        1.0 + np.arange(-300, 300) / 2 ** 20,
+        1.0 + np.arange(0, 129) / 128.0,                 # table knots
+        [1.0, 2.0, 0.5, np.nextafter(1.0, 0.0), np.nextafter(1.0, 2.0),
+         2.2250738585072014e-308, 1.7976931348623157e308, 5e-324, 0.0,
+         -0.0, -1.0, np.inf, -np.inf, np.nan]])
+    for ten in (False, True):
+        mine, ref = _run(x, ten, "pyro_log_check")
+        both_nan = np.isnan(mine) & np.isnan(ref)
+        same = (mine == ref) | both_nan
+        finite = np.isfinite(ref) & (ref != 0.0)
+        rel = np.abs(mine[finite] - ref[finite]) / np.abs(ref[finite])
+        # both within about 1 ulp of the logarithm: a few ulps apart
+        assert rel.max() < 1e-15, (ten, rel.max())
+        assert np.all(same[~finite])
