@@ -329,7 +329,9 @@ def secondary_legs(sol, th, dev, dfma):
         "output_gbs": n * nc * nc * 8 / ms_j / 1e6}
     out["vjp"] = {"states": n, "ms": ms_v, "states_per_s": n / ms_v * 1e3,
                   "cotangents": "N(0,1), seeded"}
-    del V, T, P, Y
+    del V
+    out["transport"] = transport_leg(sol, th, dev, dfma, t, p, y, T, P, Y)
+    del T, P, Y
     rng = np.random.default_rng(0)
     bt = {}
     for nv in (10, 54):
@@ -367,6 +369,52 @@ def secondary_legs(sol, th, dev, dfma):
     torch.cuda.empty_cache()
     out["flamelet_newton"] = flamelet_newton_legs(dev, dfma)
     return out
+
+
+def transport_leg(sol, th, dev, dfma, t, p, y, T, P, Y):
+    """Mixture-averaged viscosity, conductivity and species diffusivities
+    (one ``k_transport_mixavg`` pass) over the Jacobian leg's 1,048,576
+    states, with a roofline against the live DFMA peak (divisions charged
+    their measured cost) and the oracle timed on a bounded sample."""
+    import torch
+
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    from pyrometheus_gb300 import native, opcount
+    n = T.shape[0]
+    ms = _event_ms(lambda: th.get_transport_mixavg(P, T, Y), 3)
+    scratch = torch.empty(int(native.peaks_scratch_doubles()),
+                          dtype=torch.float64, device=dev)
+    rcp = native.measure_fp64_rcp(scratch)
+    _, _, log_rate = native.measure_fp64(scratch)
+    counts = opcount.transport_counts(sol.n_species,
+                                      sol.transport.symmetric)
+    flops = opcount.transport_weighted_flops(counts, dfma, rcp, log_rate)
+    # oracle on a bounded sample, one core
+    m = 4096
+    o = Oracle(sol)
+    t0 = time.perf_counter()
+    o.get_mixture_viscosity_mixavg(t[:m], y[:, :m])
+    o.get_mixture_thermal_conductivity_mixavg(t[:m], y[:, :m])
+    o.get_species_mass_diffusivities_mixavg(p[:m], t[:m], y[:, :m])
+    cpu_s = time.perf_counter() - t0
+    S = sol.n_species
+    return {
+        "states": n, "ms": ms, "states_per_s": n / ms * 1e3,
+        "outputs": "viscosity, conductivity, S species diffusivities",
+        "roofline": {
+            "bound": "fp64", "flops_per_state": flops,
+            "achieved_tflops": flops * n / ms / 1e9,
+            "peak_tflops": dfma / 1e12,
+            "frac": flops * n / ms / 1e9 / (dfma / 1e12),
+            "flop_model": {"arith_flops": counts["flops"],
+                           "divisions": counts["div"],
+                           "flops_per_division": dfma / rcp,
+                           "logs": counts["log"]}},
+        "hbm_bytes_per_state": (3 + 2 * S + 2) * 8,
+        "cpu_baseline": {"value": m / cpu_s, "unit": "states/s",
+                         "cores": 1, "kind": "port",
+                         "sample": f"{m} states of the workload (oracle "
+                                   "numpy restatement)"}}
 
 
 def flamelet_newton_legs(dev, dfma):

@@ -209,6 +209,38 @@ int pyro_flamelet_blocks(const double* p, int64_t p_inc, const double* T,
                          double* L, double* C, double* U, int64_t rows,
                          cudaStream_t stream);
 
+/* ---- mixture-averaged transport (python.py:564-641) ---------------------
+ * Present in every mechanism library; for a mechanism generated without
+ * transport fits the three compute entry points return
+ * PYRO_ERR_UNSUPPORTED. */
+
+/* available = 1 when the library carries transport fits; symmetric = 1
+ * when the binary-diffusivity fits satisfy D_ij = D_ji. */
+int pyro_transport_info(int* available, int* symmetric);
+
+/* Species transport at T, out[S][ldo]; which:
+ *   0 viscosities            get_species_viscosities            python.py:564
+ *   1 thermal conductivities get_species_thermal_conductivities python.py:573 */
+int pyro_species_transport(int which, const double* T, int64_t t_inc,
+                           double* out, int64_t ldo, int64_t n,
+                           cudaStream_t stream);
+
+/* Binary diffusivities D_ij at T, out[(i S + j) ldo + state]:
+ * get_species_binary_mass_diffusivities, python.py:582-593. */
+int pyro_binary_diffusivities(const double* T, int64_t t_inc, double* out,
+                              int64_t ldo, int64_t n, cudaStream_t stream);
+
+/* Mixture-averaged viscosity mu[n] (get_mixture_viscosity_mixavg,
+ * python.py:595-605), thermal conductivity lam[n]
+ * (get_mixture_thermal_conductivity_mixavg, python.py:607-613) and species
+ * diffusivities D[S][ldd] (get_species_mass_diffusivities_mixavg,
+ * python.py:615-641) in one pass; a NULL output is skipped, and P may be
+ * NULL when D is. */
+int pyro_transport_mixavg(const double* P, int64_t p_inc, const double* T,
+                          int64_t t_inc, const double* Y, int64_t ldy,
+                          double* mu, double* lam, double* D, int64_t ldd,
+                          int64_t n, cudaStream_t stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -522,9 +522,9 @@ def reference_generator():
 
 class _TransportPlaceholder:
     """The reference template also emits mixture-averaged transport methods
-    (``python.py:564-641``), which read Cantera transport fits.  Transport
-    is not part of the kinetics path and its methods are never called here,
-    so unit fits are supplied only to let the template render."""
+    (``python.py:564-641``), which read Cantera transport fits.  For a
+    mechanism without fits, unit fits are supplied only to let the template
+    render (its transport methods are then never called)."""
 
     def __init__(self, sol):
         self._sol = sol
@@ -544,7 +544,9 @@ class _TransportPlaceholder:
 
 
 def reference_source(sol, name: str = "Thermochemistry") -> str:
-    return reference_generator().generate(name, _TransportPlaceholder(sol))
+    if getattr(sol, "transport", None) is None:
+        sol = _TransportPlaceholder(sol)
+    return reference_generator().generate(name, sol)
 
 
 def reference_class(sol, name: str = "Thermochemistry"):

@@ -392,6 +392,97 @@ class Thermochemistry:
 
     # }}}
 
+    # {{{ mixture-averaged transport (python.py:564-641, chem_expr.py:190-267)
+
+    def _transport(self):
+        tr = getattr(self.tab.sol, "transport", None)
+        if tr is None:
+            raise ValueError("mechanism has no transport fits")
+        return tr
+
+    @staticmethod
+    def _fit_poly(c, t):
+        """``c0 + c1 ln T + c2 (ln T)^2 + c3 (ln T)^3 + c4 (ln T)^4``,
+        summed left to right with the powers formed by ``**``, as the
+        generated expressions of ``chem_expr.py:190-244`` evaluate."""
+        lt = np.log(t)
+        return (c[0] + c[1] * lt + c[2] * (lt ** 2) + c[3] * (lt ** 3)
+                + c[4] * (lt ** 4))
+
+    def get_species_viscosities(self, t):
+        """``sqrt(T) * poly(ln T)^2`` -- chem_expr.py:190-205."""
+        t = np.asarray(t, dtype=np.float64)
+        v = self._transport().viscosity
+        return np.stack([np.sqrt(t) * self._fit_poly(v[k], t) ** 2
+                         for k in range(self.tab.S)])
+
+    def get_species_thermal_conductivities(self, t):
+        """``sqrt(T) * poly(ln T)`` -- chem_expr.py:208-223."""
+        t = np.asarray(t, dtype=np.float64)
+        c = self._transport().conductivity
+        return np.stack([np.sqrt(t) * self._fit_poly(c[k], t)
+                         for k in range(self.tab.S)])
+
+    def get_species_binary_mass_diffusivities(self, t):
+        """``sqrt(T) * T * poly(ln T)``, shape (S, S, N) -- chem_expr.py:
+        226-244, python.py:582-593."""
+        t = np.asarray(t, dtype=np.float64)
+        d = self._transport().diffusivity
+        S = self.tab.S
+        return np.stack([np.stack([np.sqrt(t) * t * self._fit_poly(d[i, j], t)
+                                   for j in range(S)]) for i in range(S)])
+
+    def get_mixture_viscosity_mixavg(self, t, y):
+        """Wilke's rule -- python.py:595-605, chem_expr.py:247-259:
+        ``f_k = sum_j x_j (1 + sqrt(mu_k/mu_j sqrt(W_j/W_k)))^2 /
+        sqrt(8 (1 + W_k/W_j))``, ``mu = sum_k x_k mu_k / f_k``."""
+        y = np.asarray(y, dtype=np.float64).reshape(self.tab.S, -1)
+        mmw = self.get_mixture_molecular_weight(y)
+        x = self.get_mole_fractions(mmw, y)
+        mu = self.get_species_viscosities(t)
+        W = self.tab.W
+        S = self.tab.S
+        f = []
+        for k in range(S):
+            acc = 0
+            for j in range(S):
+                acc = acc + (x[j] * (1 + np.sqrt(
+                    (mu[k] / mu[j]) * np.sqrt(W[j] / W[k]))) ** 2
+                    / np.sqrt(8 * (1 + (W[k] / W[j]))))
+            f.append(acc)
+        return sum(x * mu / np.stack(f))
+
+    def get_mixture_thermal_conductivity_mixavg(self, t, y):
+        """``(sum x lam + 1 / sum x/lam) / 2`` -- python.py:607-613."""
+        y = np.asarray(y, dtype=np.float64).reshape(self.tab.S, -1)
+        mmw = self.get_mixture_molecular_weight(y)
+        x = self.get_mole_fractions(mmw, y)
+        lam = self.get_species_thermal_conductivities(t)
+        return 0.5 * (sum(x * lam) + 1 / sum(x / lam))
+
+    def get_species_mass_diffusivities_mixavg(self, p, t, y):
+        """``(mmw - x_k W_k) / (p mmw (sum_i x_i/D_ik - x_k/D_kk))``, or
+        ``D_kk / p`` where that denominator is not positive --
+        python.py:615-641, chem_expr.py:262-271."""
+        y = np.asarray(y, dtype=np.float64).reshape(self.tab.S, -1)
+        mmw = self.get_mixture_molecular_weight(y)
+        x = self.get_mole_fractions(mmw, y)
+        bd = self.get_species_binary_mass_diffusivities(t)
+        S = self.tab.S
+        out = []
+        for k in range(S):
+            xs = 0
+            for i in range(S):
+                xs = xs + x[i] / bd[i][k]
+            denom = xs - x[k] / bd[k][k]
+            with np.errstate(divide="ignore", invalid="ignore"):
+                out.append(np.where(np.greater(denom, 0 * t),
+                                    (mmw - x[k] * self.tab.W[k])
+                                    / (p * mmw * denom), bd[k][k] / p))
+        return np.stack(out)
+
+    # }}}
+
     # {{{ constant-pressure reactor source and its Jacobian
 
     def reactor_source(self, p, t, y):

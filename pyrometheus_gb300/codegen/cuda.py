@@ -215,6 +215,28 @@ def _table(qual: str, ctype: str, name: str, dims: List[int],
     return f"{qual} {ctype} {name}{shape} = {{{', '.join(values)}}};"
 
 
+def _transport_fits(sol) -> Optional[Tuple[np.ndarray, np.ndarray,
+                                            np.ndarray]]:
+    """``(viscosity (S,5), conductivity (S,5), diffusivity (S,S,5))`` fits
+    read through the Cantera surface the reference's template uses
+    (``python.py:564-593``), or None for a mechanism without them."""
+    S = int(sol.n_species)
+    try:
+        visc = np.array([sol.get_viscosity_polynomial(k) for k in range(S)],
+                        dtype=np.float64)
+        cond = np.array([sol.get_thermal_conductivity_polynomial(k)
+                         for k in range(S)], dtype=np.float64)
+        diff = np.array([[sol.get_binary_diff_coeffs_polynomial(i, j)
+                          for j in range(S)] for i in range(S)],
+                        dtype=np.float64)
+    except (AttributeError, ValueError, RuntimeError, NotImplementedError):
+        return None
+    if visc.shape != (S, 5) or cond.shape != (S, 5) or \
+            diff.shape != (S, S, 5):
+        return None
+    return visc, cond, diff
+
+
 def _rate_record(rate: _Rate) -> Tuple[int, List[float]]:
     """(form, [p0, p1, p2]) of an Arrhenius record (kinetics.cuh FORM_*)."""
     if rate.Ta == 0.0 and rate.b == 0.0:
@@ -244,6 +266,7 @@ class _Emitter:
     def __init__(self, name: str, sol, opts: CudaGenerationOptions):
         self.name = name
         self.m = _Model(sol)
+        self.transport = _transport_fits(sol)
         self.opts = opts
         self.block = int(opts.block_size) if opts.block_size else \
             _default_block(self.m.S)
@@ -684,7 +707,58 @@ class _Emitter:
             w("#define PYRO_BDF2_UNROLLED 1")
         w('#include "reactor_bdf2.cuh"')
         w('#include "flamelet.cuh"')
+        L.extend(self._transport_tables())
+        w('#include "transport.cuh"')
         return "\n".join(L) + "\n"
+
+    def _transport_tables(self) -> List[str]:
+        """Fits and mixture-rule constants of ``csrc/transport.cuh`` (none
+        when the mechanism carries no transport fits).  Threads read them
+        with uniform indices, through L1 (``__ldg``)."""
+        if self.transport is None:
+            return ["// no transport fits: the transport entry points "
+                    "return PYRO_ERR_UNSUPPORTED"]
+        visc, cond, diff = self.transport
+        m = self.m
+        S = m.S
+        W = np.asarray(m.W, dtype=np.float64)
+        sym = bool(np.array_equal(diff, diff.transpose(1, 0, 2)))
+        if sym:
+            pairs = [diff[i, j] for j in range(S) for i in range(j + 1)]
+        else:
+            pairs = [diff[i, j] for i in range(S) for j in range(S)]
+        # Wilke: C_kj = 1 / sqrt(8 (1 + W_k/W_j)), a_k = |P_k| W_k^(-1/4)
+        wilke = [1.0 / np.sqrt(8.0 * (1.0 + W[k] / W[j]))
+                 for k in range(S) for j in range(S)]
+        wq = [float(v) for v in W ** -0.25]
+        # four per-thread columns of S doubles in the mixture kernel
+        per_thread = 4 * S * 8
+        tblock = max(32, min(128, (227 * 1024 - 1024) // per_thread
+                             // 32 * 32))
+        per_cta = per_thread * tblock + 1024
+        tbps = max(1, min(8, (228 * 1024) // per_cta))
+
+        def flat(a):
+            return [_hexd(v) for r in a for v in r]
+        out = [
+            "// mixture-averaged transport fits (chem_expr.py:190-244), five"
+            " coefficients per fit",
+            "#define PYRO_HAS_TRANSPORT 1",
+            f"#define PYRO_TR_SYM {1 if sym else 0}",
+            f"#define TBLOCK {tblock}",
+            f"#define TBLOCKS_PER_SM {tbps}",
+            _table("__device__ const", "double", "k_tr_visc", [S * 5],
+                   flat(visc)),
+            _table("__device__ const", "double", "k_tr_cond", [S * 5],
+                   flat(cond)),
+            _table("__device__ const", "double", "k_tr_diff",
+                   [len(pairs) * 5], flat(pairs)),
+            _table("__device__ const", "double", "k_tr_wilke", [S * S],
+                   [_hexd(v) for v in wilke]),
+            _table("__device__ const", "double", "k_tr_wq", [S],
+                   [_hexd(v) for v in wq]),
+        ]
+        return out
 
 
 class _UnrolledEmitter:

@@ -43,7 +43,44 @@ __global__ void k_log(double* out, int iters) {
   out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+__global__ void k_rcp(double* out, int iters) {
+  double x0 = 1.0 + threadIdx.x * 1e-6, x1 = x0 + 0.1, x2 = x0 + 0.2,
+         x3 = x0 + 0.3, s = 0.0;
+  for (int i = 0; i < iters; ++i) {
+    s += 1.0 / x0 + 1.0 / x1 + 1.0 / x2 + 1.0 / x3;
+    x0 += 1e-7; x1 += 1e-7; x2 += 1e-7; x3 += 1e-7;
+  }
+  out[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
 }  // namespace
+
+// *result = double-precision reciprocals (1.0 / x, IEEE-rounded) per second.
+// scratch: pyro_peaks_scratch_doubles() doubles.  Synchronous.
+PYRO_EXPORT int pyro_measure_fp64_rcp(double* scratch, double* result,
+                                      int repeats) {
+  if (!scratch || !result || repeats < 1) return PYRO_ERR_ARGUMENT;
+  const int blocks = pyro_sm_count() * 8, threads = 256, iters = 256;
+  const double n = (double)blocks * threads;
+  cudaEvent_t e0, e1;
+  if (cudaEventCreate(&e0) != cudaSuccess) return PYRO_ERR_LAUNCH;
+  if (cudaEventCreate(&e1) != cudaSuccess) return PYRO_ERR_LAUNCH;
+  double best = 0.0;
+  for (int r = 0; r < repeats + 1; ++r) {
+    float ms = 0.f;
+    cudaEventRecord(e0);
+    k_rcp<<<blocks, threads>>>(scratch, iters);
+    cudaEventRecord(e1);
+    cudaEventSynchronize(e1);
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (r && ms > 0) best = fmax(best, 4.0 * iters * n / (ms * 1e-3));
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (cudaGetLastError() != cudaSuccess) return PYRO_ERR_LAUNCH;
+  *result = best;
+  return PYRO_OK;
+}
 
 // Number of doubles the scratch buffer of pyro_measure_fp64 must hold.
 PYRO_EXPORT int64_t pyro_peaks_scratch_doubles() {

@@ -191,8 +191,10 @@ class Solution:
 
     def __init__(self, species: List[Species], reactions: List[Reaction],
                  elements: Optional[List[str]] = None, source: str = "",
-                 name: str = "gas"):
+                 name: str = "gas", transport=None):
         self._species = list(species)
+        #: :class:`pyrometheus_gb300.transport_fits.TransportFits` or None
+        self.transport = transport
         self._reactions = list(reactions)
         self.species_names = [sp.name for sp in self._species]
         if len(set(self.species_names)) != len(self.species_names):
@@ -260,6 +262,27 @@ class Solution:
 
     def product_stoich_coeff(self, k, i: int) -> float:
         return float(self._reactions[i].products.get(self._name(k), 0.0))
+
+    # -- transport fits (Cantera's MixTransport surface) -------------------
+    @property
+    def transport_model(self) -> str:
+        return "mixture-averaged" if self.transport is not None else "none"
+
+    def _fits(self):
+        if self.transport is None:
+            raise ValueError(f"mechanism '{self.source or self.name}' has no "
+                             "transport fits")
+        return self.transport
+
+    def get_viscosity_polynomial(self, k: int) -> np.ndarray:
+        return np.array(self._fits().viscosity[k], dtype=np.float64)
+
+    def get_thermal_conductivity_polynomial(self, k: int) -> np.ndarray:
+        return np.array(self._fits().conductivity[k], dtype=np.float64)
+
+    def get_binary_diff_coeffs_polynomial(self, i: int, j: int
+                                          ) -> np.ndarray:
+        return np.array(self._fits().diffusivity[i, j], dtype=np.float64)
 
     # -- convenience (not part of the Cantera surface) ---------------------
     def element_matrix(self) -> np.ndarray:

@@ -54,6 +54,9 @@ def peaks_lib() -> ctypes.CDLL:
     lib = ctypes.CDLL(build_peaks())
     lib.pyro_peaks_scratch_doubles.restype = ctypes.c_int64
     lib.pyro_peaks_scratch_doubles.argtypes = []
+    lib.pyro_measure_fp64_rcp.restype = ctypes.c_int
+    lib.pyro_measure_fp64_rcp.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_int]
     lib.pyro_measure_fp64.restype = ctypes.c_int
     lib.pyro_measure_fp64.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_int]
@@ -74,6 +77,17 @@ def measure_fp64(scratch, repeats: int = 3):
     if st != 0:
         raise RuntimeError(f"pyro_measure_fp64 failed (status {st})")
     return res[0], res[1], res[2]
+
+
+def measure_fp64_rcp(scratch, repeats: int = 3) -> float:
+    """Double-precision reciprocals (``1.0 / x``) per second on the current
+    device; *scratch* as for :func:`measure_fp64`."""
+    res = ctypes.c_double()
+    st = peaks_lib().pyro_measure_fp64_rcp(
+        ctypes.c_void_p(scratch.data_ptr()), ctypes.byref(res), int(repeats))
+    if st != 0:
+        raise RuntimeError(f"pyro_measure_fp64_rcp failed (status {st})")
+    return res.value
 
 
 @lru_cache(maxsize=None)

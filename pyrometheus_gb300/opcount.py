@@ -163,6 +163,49 @@ def kernel_weights(dfma_flops: float, log_rate: float) -> Dict[str, float]:
             "pow": w_log + TANG_EXP_FLOPS}
 
 
+def transport_counts(n_species: int, symmetric: bool = True) -> Counter:
+    """Per-state FP64 work of ``k_transport_mixavg`` (``csrc/transport.cuh``)
+    computing all three mixture quantities: ``flops`` (FMA = 2) and the
+    divisions/reciprocals (``div``, square roots counted with them), plus
+    one ``log``.  Pairs are formed once each with symmetric diffusivity
+    fits, S^2 times otherwise."""
+    S = n_species
+    c = Counter()
+    c["log"] += 1
+    c["div"] += 1                       # sqrt(T)
+    c["flops"] += 3                     # powers of ln T
+    c["flops"] += 2 * S + 2 * S         # sum Y/W (FMA), x = Y/W * mmw
+    c["div"] += 1                       # mmw
+    # viscosity: fit, a_k and 1/a_k, x/a, x/a^2; Wilke's three FMAs per
+    # pair; per species f_k and x mu / f
+    c["flops"] += S * (8 + 1 + 2) + S * S * 6 + S * 10
+    c["div"] += 2 * S
+    # conductivity
+    c["flops"] += S * 12 + 2
+    c["div"] += S + 1
+    # diffusivities
+    if symmetric:
+        off = S * (S - 1) // 2
+        c["flops"] += off * 12 + S * 10
+        c["div"] += off + S
+    else:
+        c["flops"] += S * S * 10 + S * 8
+        c["div"] += S * S + S
+    c["flops"] += 1 + S * 7             # sqrt(T) T, denominators, D_k
+    c["div"] += 1 + S
+    return c
+
+
+def transport_weighted_flops(counts: Dict[str, float], dfma_flops: float,
+                             rcp_rate: float, log_rate: float) -> float:
+    """Flops of :func:`transport_counts` with each division charged its
+    measured FP64-pipe cost (``DFMA FLOP/s / reciprocals/s``) and the log
+    CUDA's."""
+    return (float(counts["flops"])
+            + counts["div"] * dfma_flops / rcp_rate
+            + counts["log"] * dfma_flops / log_rate)
+
+
 def bytes_per_state(sol) -> int:
     """HBM bytes per state of the fused step: p, T, Y, e in; wdot, T out."""
     S = sol.n_species

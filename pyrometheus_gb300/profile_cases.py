@@ -4,6 +4,7 @@
     python -m pyrometheus_gb300.profile_cases vjp [states]
     python -m pyrometheus_gb300.profile_cases block_thomas [nv] [systems]
     python -m pyrometheus_gb300.profile_cases batched_lu [nv] [cells]
+    python -m pyrometheus_gb300.profile_cases transport [states]
 
 Each case builds its inputs on the current CUDA device (inputs larger than
 the 129 MB L2 at the default sizes, a few GB at most), runs the kernel three
@@ -102,6 +103,32 @@ def batched_lu(nv: int = 54, cells: int = 1 << 16):
     torch.cuda.synchronize()
 
 
+def transport(states: int = 1 << 18):
+    """Mixture viscosity, conductivity and species diffusivities
+    (``k_transport_mixavg``); prints the mean of the timed launches."""
+    import torch
+
+    from . import get_thermochem_class, synthetic
+    dev = _dev()
+    sol = synthetic.config2_mechanism()
+    th = get_thermochem_class(sol)(device=dev)
+    t, p, y = synthetic.sample_states(sol, states, seed=1)
+    T = torch.as_tensor(t, device=dev)
+    P = torch.as_tensor(p, device=dev)
+    Y = torch.as_tensor(y, device=dev)
+    th.get_transport_mixavg(P, T, Y)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(2):
+        th.get_transport_mixavg(P, T, Y)
+    e1.record()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / 2
+    print(f"transport: {states} states in {ms:.3f} ms "
+          f"({states / ms * 1e3:.4g} states/s)")
+
+
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     if not argv:
@@ -115,6 +142,8 @@ def main(argv=None):
         block_thomas(*rest)
     elif case == "batched_lu":
         batched_lu(*rest)
+    elif case == "transport":
+        transport(*rest)
     else:
         raise SystemExit(f"unknown case {case!r}")
     print("ok")

@@ -47,6 +47,7 @@ import numpy as np
 
 from .mechanism import (Arrhenius, LindemannRate, NasaPoly2, Reaction,
                         Solution, Species, ThirdBody, TroeRate, gas_constant)
+from .transport_fits import kinetic_theory_fits
 
 #: H/O/N/Ar set with the sandiego shape (9 species).
 SPECIES_9 = ["H2", "H", "O2", "O", "OH", "HO2", "H2O", "N2", "AR"]
@@ -333,8 +334,12 @@ def make_mechanism(species_names: Sequence[str], n_reactions: int,
         if len(group) > 1:
             for r in group:
                 r.duplicate = True
-    return Solution(species, reactions, elements,
-                    source=f"{name}.yaml", name="gas")
+    sol = Solution(species, reactions, elements, source=f"{name}.yaml",
+                   name="gas")
+    # transport fits from their own generator, so the kinetics above do not
+    # depend on whether fits are made
+    sol.transport = kinetic_theory_fits(sol, seed=seed + 7919)
+    return sol
 
 
 def config1_mechanism(seed: int = 1) -> Solution:

@@ -74,6 +74,11 @@ _SIGNATURES = {
                                                           _D, _I64, _P],
     "pyro_flamelet_blocks": [_P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P,
                              _P, _P, _I64, _P],
+    "pyro_transport_info": [_P, _P],
+    "pyro_species_transport": [_INT, _P, _I64, _P, _I64, _I64, _P],
+    "pyro_binary_diffusivities": [_P, _I64, _P, _I64, _I64, _P],
+    "pyro_transport_mixavg": [_P, _I64, _P, _I64, _P, _I64, _P, _P, _P, _I64,
+                              _I64, _P],
     "pyro_flamelet_residual": [_P, _I64, _P, _P, _P, _I64, _P, _I64, _P, _P,
                                _P, _P, _P, _P, _P, _P, _P, _I64, _P, _I64,
                                _I64, _P],
@@ -153,6 +158,10 @@ class CudaThermochemistryBase:
         if ns.value != self.num_species or nr.value != self.num_reactions:
             raise RuntimeError("generated library does not match mechanism")
         self._fail = torch.zeros(1, dtype=torch.int32, device=self.device)
+        avail = ctypes.c_int()
+        _check(self._lib.pyro_transport_info(ctypes.byref(avail), None),
+               "transport_info")
+        self.has_transport = bool(avail.value)
 
     # {{{ argument plumbing
 
@@ -558,6 +567,93 @@ class CudaThermochemistryBase:
         if check and int(self._fail.item()) > 0:
             raise RuntimeError("Temperature iteration failed to converge")
         return out_w, out_t
+
+    # }}}
+
+    # {{{ mixture-averaged transport (python.py:564-641)
+
+    def _need_transport(self):
+        if not self.has_transport:
+            raise ValueError(f"mechanism '{self.model_name}' has no transport"
+                             " fits")
+
+    def _species_transport(self, which, temperature):
+        self._need_transport()
+        tv = self._scalar_vec(temperature)
+        out = self._out(self.num_species, tv.n)
+        _check(self._lib.pyro_species_transport(
+            which, tv.ptr, tv.inc, out.data_ptr(), out.stride(0), tv.n,
+            self._stream), "species transport")
+        return self._shape_rows(out, _is_scalar(temperature))
+
+    def get_species_viscosities(self, temperature):
+        """``sqrt(T) P_k(ln T)^2`` ([S, N]) -- python.py:564-571."""
+        return self._species_transport(0, temperature)
+
+    def get_species_thermal_conductivities(self, temperature):
+        """``sqrt(T) Q_k(ln T)`` ([S, N]) -- python.py:573-580."""
+        return self._species_transport(1, temperature)
+
+    def get_species_binary_mass_diffusivities(self, temperature):
+        """``sqrt(T) T R_ij(ln T)`` ([S, S, N]) -- python.py:582-593."""
+        self._need_transport()
+        tv = self._scalar_vec(temperature)
+        S = self.num_species
+        out = torch.empty((S, S, tv.n), dtype=torch.float64,
+                          device=self.device)
+        _check(self._lib.pyro_binary_diffusivities(
+            tv.ptr, tv.inc, out.data_ptr(), tv.n, tv.n, self._stream),
+            "binary diffusivities")
+        return out[:, :, 0] if _is_scalar(temperature) else out
+
+    def _mixavg(self, pressure, temperature, mass_fractions, want_mu,
+                want_lam, want_d):
+        self._need_transport()
+        ym, ny, single = self._species_mat(mass_fractions, self.num_species)
+        tv = self._scalar_vec(temperature)
+        pv = self._scalar_vec(pressure) if want_d else None
+        n = self._n(ny, tv, *((pv,) if pv is not None else ()))
+        ym = self._expand_mat(ym, n)
+        mu = torch.empty(n, dtype=torch.float64, device=self.device) \
+            if want_mu else None
+        lam = torch.empty(n, dtype=torch.float64, device=self.device) \
+            if want_lam else None
+        d = self._out(self.num_species, n) if want_d else None
+        _check(self._lib.pyro_transport_mixavg(
+            pv.ptr if pv else None, pv.inc if pv else 0, tv.ptr, tv.inc,
+            ym.data_ptr(), ym.stride(0),
+            mu.data_ptr() if mu is not None else None,
+            lam.data_ptr() if lam is not None else None,
+            d.data_ptr() if d is not None else None,
+            d.stride(0) if d is not None else n, n, self._stream),
+            "mixture-averaged transport")
+        single = single and n == 1
+        return (None if mu is None else self._shape_vec(mu, single),
+                None if lam is None else self._shape_vec(lam, single),
+                None if d is None else self._shape_rows(d, single))
+
+    def get_mixture_viscosity_mixavg(self, temperature, mass_fractions):
+        """Wilke's mixture rule ([N]) -- python.py:595-605."""
+        return self._mixavg(None, temperature, mass_fractions, True, False,
+                            False)[0]
+
+    def get_mixture_thermal_conductivity_mixavg(self, temperature,
+                                                mass_fractions):
+        """``(sum x lam + 1 / sum x/lam) / 2`` ([N]) -- python.py:607-613."""
+        return self._mixavg(None, temperature, mass_fractions, False, True,
+                            False)[1]
+
+    def get_species_mass_diffusivities_mixavg(self, pressure, temperature,
+                                              mass_fractions):
+        """Mixture-averaged diffusivities ([S, N]) -- python.py:615-641."""
+        return self._mixavg(pressure, temperature, mass_fractions, False,
+                            False, True)[2]
+
+    def get_transport_mixavg(self, pressure, temperature, mass_fractions):
+        """``(viscosity [N], conductivity [N], diffusivities [S, N])`` in
+        one pass over the states (the three mixture methods above)."""
+        return self._mixavg(pressure, temperature, mass_fractions, True,
+                            True, True)
 
     # }}}
 

@@ -330,6 +330,46 @@ def golden_flamelet(fname="flamelet.npz"):
     print(f"wrote {fname}")
 
 
+def golden_transport(fname="transport.npz"):
+    """The reference's generated transport methods (``python.py:564-641``)
+    on the synthetic mechanisms' kinetic-theory fits.  The last two states
+    are pure N2 and pure H2 (the ``denom > 0`` branch of
+    ``get_species_mass_diffusivities_mixavg`` goes to ``D_kk / p``)."""
+    def dense(a):
+        a = np.asarray(a)
+        if a.dtype == object:
+            return np.array([dense(v) for v in a])
+        return a.astype(np.float64)
+
+    out = {}
+    for tag, sol, n, n_bd, seed in (
+            ("s9", synthetic.config1_mechanism(), 64, 16, 51),
+            ("s53", synthetic.config2_mechanism(), 32, 3, 52)):
+        ref = refgen.reference_class(sol)()
+        t, p, y = edge_states(sol, n, seed)
+        for col, sp in ((-1, "N2"), (-2, "H2")):
+            y[:, col] = 0.0
+            y[sol.species_index(sp), col] = 1.0
+        tr = sol.transport
+        case = dict(
+            T=t, P=p, Y=y,
+            fit_visc=tr.viscosity, fit_cond=tr.conductivity,
+            fit_diff=tr.diffusivity,
+            visc=dense(ref.get_species_viscosities(t)),
+            cond=dense(ref.get_species_thermal_conductivities(t)),
+            bdiff=dense(ref.get_species_binary_mass_diffusivities(
+                t[:n_bd])),
+            mu_mix=dense(ref.get_mixture_viscosity_mixavg(t, y)),
+            lam_mix=dense(ref.get_mixture_thermal_conductivity_mixavg(t,
+                                                                      y)),
+            d_mix=dense(ref.get_species_mass_diffusivities_mixavg(p, t, y)),
+            mech_yaml=np.array(dump_mechanism(sol)))
+        for k, v in case.items():
+            out[f"{tag}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+    print(f"wrote {fname}")
+
+
 def main():
     if not refgen.reference_available():
         raise SystemExit("reference checkout not found")
@@ -338,6 +378,7 @@ def main():
     golden(quirks_mechanism(), 128, 13, 12, "quirks9.npz")
     golden_block_thomas()
     golden_flamelet()
+    golden_transport()
 
 
 if __name__ == "__main__":
