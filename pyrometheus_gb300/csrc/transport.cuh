@@ -24,7 +24,8 @@
 //   * the powers of L are formed once per state and every fit is summed in
 //     the reference's order c0 + c1 L + c2 L^2 + c3 L^3 + c4 L^4;
 //   * with symmetric diffusivity fits (Cantera's are) each pair's 1/R_ij is
-//     formed once and added to both x_sum_i and x_sum_j, and the common
+//     formed once and added to both x_sum_i and x_sum_j, the reciprocals
+//     are formed four at a time by one division (rcp4), and the common
 //     1/(sqrt(T) T) is applied once per species.
 // Thread-private vectors (mole fractions and the Wilke / x_sum work
 // vectors) are shared-memory columns interleaved by thread.
@@ -68,6 +69,66 @@ __device__ __forceinline__ const double* diff_fit(int i, int j) {
 #else
   return k_tr_diff + 5 * (i * NS + j);
 #endif
+}
+
+// |v| in [2^-200, 2^200] (and finite, nonzero)
+__device__ __forceinline__ bool rcp_range(double v) {
+  const unsigned e = ((unsigned)__double2hiint(v) >> 20) & 0x7ffu;
+  return e - (1023u - 200u) <= 400u;
+}
+
+// r = 1/R for four values by one division (Montgomery's simultaneous
+// inversion, Math. Comp. 48 (1987) 243-264): three products forward, one
+// reciprocal, six products back -- 10 FP64 instructions instead of four
+// divisions.  Taken only when every value lies in [2^-200, 2^200], so no
+// partial product overflows or underflows; otherwise (and for zeros,
+// infinities and NaNs) each value is divided on its own, as the reference
+// divides every pair.
+__device__ __forceinline__ void rcp4(const double R[4], double r[4]) {
+  if (rcp_range(R[0]) & rcp_range(R[1]) & rcp_range(R[2]) &
+      rcp_range(R[3])) {
+    const double p01 = R[0] * R[1], p012 = p01 * R[2];
+    double inv = 1.0 / (p012 * R[3]);
+    r[3] = inv * p012;
+    inv *= R[3];
+    r[2] = inv * p01;
+    inv *= R[2];
+    r[1] = inv * R[0];
+    r[0] = inv * R[1];
+  } else {
+#pragma unroll
+    for (int u = 0; u < 4; ++u) r[u] = 1.0 / R[u];
+  }
+}
+
+// Adds x_k mu_k / f_k for k = k0 .. k0+K-1 (in that order) to acc: the
+// K species' Wilke sums run as 3K independent FMA chains over j, which
+// keeps the FP64 pipe fed from one warp per scheduler.
+template <int K>
+__device__ __forceinline__ void wilke_block(int k0, TCols X, TCols V,
+                                            TCols Q, TCols A, double sq,
+                                            double& acc) {
+  double s0[K], s1[K], s2[K];
+#pragma unroll
+  for (int u = 0; u < K; ++u) s0[u] = s1[u] = s2[u] = 0.0;
+  const double* __restrict__ c = k_tr_wilke + k0 * NS;
+  for (int j = 0; j < NS; ++j) {
+    const double xj = X[j], vj = V[j], qj = Q[j];
+#pragma unroll
+    for (int u = 0; u < K; ++u) {
+      const double ckj = __ldg(c + u * NS + j);
+      s0[u] = fma(ckj, xj, s0[u]);
+      s1[u] = fma(ckj, vj, s1[u]);
+      s2[u] = fma(ckj, qj, s2[u]);
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < K; ++u) {
+    const double pk = A[k0 + u];
+    const double a = fabs(pk) * k_tr_wq[k0 + u];
+    const double f = fma(a, fma(a, s2[u], 2.0 * s1[u]), s0[u]);
+    acc += X[k0 + u] * (sq * (pk * pk)) / f;
+  }
 }
 
 }  // namespace pyro_tr
@@ -144,21 +205,10 @@ __global__ void __launch_bounds__(TBLOCK)
         Q[k] = v * b;
       }
       double acc = 0.0;
-      for (int k = 0; k < NS; ++k) {
-        const double* __restrict__ c = k_tr_wilke + k * NS;
-        double s0 = 0.0, s1 = 0.0, s2 = 0.0;
-#pragma unroll 4
-        for (int j = 0; j < NS; ++j) {
-          const double ckj = __ldg(c + j);
-          s0 = fma(ckj, X[j], s0);
-          s1 = fma(ckj, V[j], s1);
-          s2 = fma(ckj, Q[j], s2);
-        }
-        const double pk = A[k];
-        const double a = fabs(pk) * k_tr_wq[k];
-        const double f = fma(a, fma(a, s2, 2.0 * s1), s0);
-        acc += X[k] * (sq * (pk * pk)) / f;
-      }
+      int k = 0;
+      for (; k + 4 <= NS; k += 4)
+        pyro_tr::wilke_block<4>(k, X, V, Q, A, sq, acc);
+      for (; k < NS; ++k) pyro_tr::wilke_block<1>(k, X, V, Q, A, sq, acc);
       mu_out[i] = acc;
     }
 
@@ -181,7 +231,19 @@ __global__ void __launch_bounds__(TBLOCK)
         const double xj = X[j];
         const double* __restrict__ c = k_tr_diff + 5 * (j * (j + 1) / 2);
         double acc = 0.0;
-        for (int m = 0; m < j; ++m) {
+        int m = 0;
+        for (; m + 4 <= j; m += 4) {
+          double R[4], r[4];
+#pragma unroll
+          for (int u = 0; u < 4; ++u) R[u] = fit(c + 5 * (m + u), pw);
+          pyro_tr::rcp4(R, r);
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            acc = fma(X[m + u], r[u], acc);
+            V[m + u] = fma(xj, r[u], V[m + u]);
+          }
+        }
+        for (; m < j; ++m) {
           const double r = 1.0 / fit(c + 5 * m, pw);
           acc = fma(X[m], r, acc);
           V[m] = fma(xj, r, V[m]);

@@ -140,6 +140,29 @@ def test_non_symmetric_fits():
                    o.get_species_mass_diffusivities_mixavg(p, t, y))
 
 
+def test_extreme_fit_values_take_the_exact_division_path():
+    """Pair values outside [2^-200, 2^200] make the grouped reciprocal
+    (one division for four pairs) fall back to one division per pair; the
+    result still matches the reference's per-pair division."""
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.transport_fits import TransportFits
+    sol = synthetic.config1_mechanism()
+    tr = sol.transport
+    diff = tr.diffusivity.copy()
+    for i, j, f in ((2, 5, 1e230), (1, 7, 1e-230)):
+        diff[i, j] *= f
+        diff[j, i] *= f
+    sol.transport = TransportFits(tr.viscosity, tr.conductivity, diff)
+    th = _cuda_class(sol)()
+    o = Oracle(sol)
+    t, p, y = synthetic.sample_states(sol, 300, seed=79)
+    got = _np(th.get_species_mass_diffusivities_mixavg(p, t, y))
+    ref = o.get_species_mass_diffusivities_mixavg(p, t, y)
+    assert np.all(np.isfinite(got))
+    assert np.all(np.abs(got - ref) <= TOL * diffusivity_scale(o, p, t, y))
+
+
 def test_shapes_scalars_and_empty():
     from pyrometheus_gb300 import synthetic
     sol = synthetic.config1_mechanism()
