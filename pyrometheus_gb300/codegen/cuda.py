@@ -731,9 +731,9 @@ class _Emitter:
         wilke = [1.0 / np.sqrt(8.0 * (1.0 + W[k] / W[j]))
                  for k in range(S) for j in range(S)]
         wq = [float(v) for v in W ** -0.25]
-        # four per-thread columns of S doubles in the mixture kernel
-        per_thread = 4 * S * 8
-        tblock = max(32, min(128, (227 * 1024 - 1024) // per_thread
+        # three per-thread columns of S doubles in the mixture kernel
+        per_thread = 3 * S * 8
+        tblock = max(32, min(256, (227 * 1024 - 1024) // per_thread
                              // 32 * 32))
         per_cta = per_thread * tblock + 1024
         tbps = max(1, min(8, (228 * 1024) // per_cta))

@@ -106,8 +106,8 @@ __device__ __forceinline__ void rcp4(const double R[4], double r[4]) {
 // keeps the FP64 pipe fed from one warp per scheduler.
 template <int K>
 __device__ __forceinline__ void wilke_block(int k0, TCols X, TCols V,
-                                            TCols Q, TCols A, double sq,
-                                            double& acc) {
+                                            TCols Q, const Powers& pw,
+                                            double sq, double& acc) {
   double s0[K], s1[K], s2[K];
 #pragma unroll
   for (int u = 0; u < K; ++u) s0[u] = s1[u] = s2[u] = 0.0;
@@ -124,7 +124,7 @@ __device__ __forceinline__ void wilke_block(int k0, TCols X, TCols V,
   }
 #pragma unroll
   for (int u = 0; u < K; ++u) {
-    const double pk = A[k0 + u];
+    const double pk = fit(k_tr_visc + 5 * (k0 + u), pw);
     const double a = fabs(pk) * k_tr_wq[k0 + u];
     const double f = fma(a, fma(a, s2[u], 2.0 * s1[u]), s0[u]);
     acc += X[k0 + u] * (sq * (pk * pk)) / f;
@@ -178,9 +178,8 @@ __global__ void __launch_bounds__(TBLOCK)
   extern __shared__ double smem[];
   using pyro_tr::fit;
   const pyro_tr::TCols X = pyro_tr::tcol(smem, 0),
-                       A = pyro_tr::tcol(smem, 1),
-                       V = pyro_tr::tcol(smem, 2),
-                       Q = pyro_tr::tcol(smem, 3);
+                       V = pyro_tr::tcol(smem, 1),
+                       Q = pyro_tr::tcol(smem, 2);
   for (int64_t i = (int64_t)blockIdx.x * TBLOCK + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * TBLOCK) {
     const double T = pyro_ld(Tp, t_inc, i);
@@ -195,11 +194,12 @@ __global__ void __launch_bounds__(TBLOCK)
       X[k] = k_inv_mw[k] * __ldg(Y + (int64_t)k * ldy + i) * mmw;
 
     if (mu_out) {
-      // A = P_k, V = x_k / a_k, Q = x_k / a_k^2
+      // V = x_k / a_k, Q = x_k / a_k^2 (P_k is formed again where it is
+      // used: four FMAs per species buy a third fewer shared-memory
+      // columns, so more states fit on an SM)
       for (int k = 0; k < NS; ++k) {
         const double pk = fit(k_tr_visc + 5 * k, pw);
         const double b = 1.0 / (fabs(pk) * k_tr_wq[k]);
-        A[k] = pk;
         const double v = X[k] * b;
         V[k] = v;
         Q[k] = v * b;
@@ -207,8 +207,8 @@ __global__ void __launch_bounds__(TBLOCK)
       double acc = 0.0;
       int k = 0;
       for (; k + 4 <= NS; k += 4)
-        pyro_tr::wilke_block<4>(k, X, V, Q, A, sq, acc);
-      for (; k < NS; ++k) pyro_tr::wilke_block<1>(k, X, V, Q, A, sq, acc);
+        pyro_tr::wilke_block<4>(k, X, V, Q, pw, sq, acc);
+      for (; k < NS; ++k) pyro_tr::wilke_block<1>(k, X, V, Q, pw, sq, acc);
       mu_out[i] = acc;
     }
 
@@ -232,6 +232,7 @@ __global__ void __launch_bounds__(TBLOCK)
         const double* __restrict__ c = k_tr_diff + 5 * (j * (j + 1) / 2);
         double acc = 0.0;
         int m = 0;
+#pragma unroll 2
         for (; m + 4 <= j; m += 4) {
           double R[4], r[4];
 #pragma unroll
@@ -339,7 +340,7 @@ PYRO_EXPORT int pyro_transport_mixavg(const double* P, int64_t p_inc,
   if (n == 0 || (!mu && !lam && !D)) return PYRO_OK;
   if (!T || !Y || ldy < n) return PYRO_ERR_ARGUMENT;
   if (D && (!P || ldd < n)) return PYRO_ERR_ARGUMENT;
-  const size_t bytes = (size_t)4 * NS * TBLOCK * sizeof(double);
+  const size_t bytes = (size_t)3 * NS * TBLOCK * sizeof(double);
   if (bytes > 48 * 1024 &&
       cudaFuncSetAttribute(k_transport_mixavg,
                            cudaFuncAttributeMaxDynamicSharedMemorySize,
