@@ -183,11 +183,15 @@ def transport_counts(n_species: int, symmetric: bool = True) -> Counter:
     # conductivity
     c["flops"] += S * 12 + 2
     c["div"] += S + 1
-    # diffusivities
+    # diffusivities: row j's j off-diagonal pairs in groups of four (one
+    # reciprocal and nine products per group, csrc/transport.cuh rcp4)
+    # and j mod 4 single reciprocals
     if symmetric:
         off = S * (S - 1) // 2
-        c["flops"] += off * 12 + S * 10
-        c["div"] += off + S
+        groups = sum(j // 4 for j in range(S))
+        singles = off - 4 * groups
+        c["flops"] += off * (8 + 4) + groups * 9 + S * 10
+        c["div"] += groups + singles + S
     else:
         c["flops"] += S * S * 10 + S * 8
         c["div"] += S * S + S
