@@ -55,6 +55,23 @@ int pyro_block_thomas_small(const double* L, const double* C, const double* U,
                             int nsys, int nv, double* work, int* status,
                             int threads, cudaStream_t stream);
 
+/* More right-hand sides for systems already solved: after pyro_block_thomas
+ * or pyro_block_thomas_small, `work` holds every row's LU factors and
+ * pivots of C'_i; for the same L, C, U this solves nrhs (1..4) further
+ * systems, B[c][rows][nv] -> X[c][rows][nv] (the c-th at offset
+ * c * rhs_stride), with the vector recurrences only (4 nv^2 FMAs per row
+ * and right-hand side).  The reference factorises again on every call to
+ * block_thomas, pyrometheus/flamelets/linear_solver.py:6-103, including
+ * the adjoint solves that share one operator in
+ * pyrometheus/flamelets/thermodynamic_consistency.py:105-307.  order and
+ * counter as for pyro_block_thomas; nv <= 64; B and X must not overlap. */
+int pyro_block_thomas_resolve(const double* L, const double* U,
+                              const double* B, double* X, int nrhs,
+                              int64_t rhs_stride, const int64_t* row_off,
+                              const int* order, int nsys, int nv,
+                              const double* work, int* counter,
+                              cudaStream_t stream);
+
 /* No counterpart in the reference (its block_thomas allocates through JAX
  * on every call).  For callers that cannot allocate device memory when they
  * solve: host applications that hand all device memory to their own pool at

@@ -209,6 +209,29 @@ int pyro_flamelet_blocks(const double* p, int64_t p_inc, const double* T,
                          double* L, double* C, double* U, int64_t rows,
                          cudaStream_t stream);
 
+/* Adjoint operator of the compressible-EOS consistency solves,
+ * FlameletEquations.adjoint_operator, equations.py:451-516 (used by
+ * CompressibleEOS.enthalpy_gradient / eos_gradient,
+ * thermodynamic_consistency.py:105-307).  Same arguments and in-place use
+ * of C as pyro_flamelet_blocks; the result: interior C_i = Lap_c I +
+ * (2 / chi_i) (dS/dphi_i)^T, boundary C_i = chi_i / 2 dx^-2 I, L and U the
+ * Laplacian's couplings dx^-2 I without the chi / 2 factor. */
+int pyro_flamelet_adjoint_blocks(const double* p, int64_t p_inc,
+                                 const double* T, const double* Y,
+                                 int64_t ldy, const double* chi,
+                                 const double* visc, const int64_t* row_off,
+                                 const int* sys_of_row,
+                                 const double* inv_dx2, double* L, double* C,
+                                 double* U, int64_t rows,
+                                 cudaStream_t stream);
+
+/* rt[rows] = R_u T / W_mix and, when J is not NULL, its gradient with
+ * respect to (h, Y) at T(h, Y), J[S+1][ldj]: compressible_eos_rt and
+ * compressible_eos_rt_jacobian, equations.py:136-147,517-535. */
+int pyro_flamelet_eos_rt(const double* T, const double* Y, int64_t ldy,
+                         double* rt, double* J, int64_t ldj, int64_t rows,
+                         cudaStream_t stream);
+
 /* ---- mixture-averaged transport (python.py:564-641) ---------------------
  * Present in every mechanism library; for a mechanism generated without
  * transport fits the three compute entry points return

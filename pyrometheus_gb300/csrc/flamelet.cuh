@@ -36,7 +36,11 @@
 #define FNV (NS + 1)
 
 // one warp per row: transform the reactor Jacobian held in C in place and
-// write L and U.
+// write L and U.  ADJ: the adjoint operator of the EOS-consistency solves
+// instead (FlameletEquations.adjoint_operator, equations.py:451-516):
+// interior C_i = Lap_c I + (2 / chi_i) (dS/dphi_i)^T, boundary C_i =
+// chi_i / 2 dx^-2 I, and L, U the Laplacian's own (unscaled) couplings.
+template <bool ADJ>
 __global__ void __launch_bounds__(128)
     k_flamelet_blocks(const double* __restrict__ Pp, int64_t p_inc,
                       const double* __restrict__ Tt,
@@ -106,16 +110,34 @@ __global__ void __launch_bounds__(128)
         }
         Cr[m] = v;
       }
+      if (ADJ) {
+        // (2 / chi) dS/dphi, transposed in place (each off-diagonal pair
+        // swapped by one lane)
+        __syncwarp();
+        const double sc = 2.0 / chi[r];
+        for (int e = lane; e < NB; e += 32) {
+          const int a = e / FNV, b = e - a * FNV;
+          if (a < b) {
+            const double x = Cr[e], y = Cr[b * FNV + a];
+            Cr[e] = sc * y;
+            Cr[b * FNV + a] = sc * x;
+          } else if (a == b) {
+            Cr[e] *= sc;
+          }
+        }
+      }
     } else {
       for (int e = lane; e < NB; e += 32) Cr[e] = 0.0;
     }
     __syncwarp();
     // Laplacian diagonal, and the couplings
     const double lap_c = interior ? -2.0 * idx2 : idx2;
-    for (int d = lane; d < FNV; d += 32) Cr[(int64_t)d * FNV + d] += 0.5 * chi[r] * lap_c;
+    const double dgl = (ADJ && interior) ? lap_c : 0.5 * chi[r] * lap_c;
+    for (int d = lane; d < FNV; d += 32) Cr[(int64_t)d * FNV + d] += dgl;
     const bool next_interior = !last && (r + 1 < r1 - 1);
-    const double lo = next_interior ? 0.5 * chi[r + 1] * idx2 : 0.0;
-    const double up = interior ? 0.5 * chi[r] * idx2 : 0.0;
+    const double lo =
+        next_interior ? (ADJ ? idx2 : 0.5 * chi[r + 1] * idx2) : 0.0;
+    const double up = interior ? (ADJ ? idx2 : 0.5 * chi[r] * idx2) : 0.0;
     double* Lr = L + r * NB;
     double* Ur = U + r * NB;
     for (int e = lane; e < NB; e += 32) {
@@ -124,6 +146,48 @@ __global__ void __launch_bounds__(128)
       Ur[e] = diag ? up : 0.0;
     }
     __syncwarp();
+  }
+}
+
+// thread per row: R T (R = R_u / W_mix) and its gradient with respect to
+// phi = (h, Y) at T(h, Y) (local_compressible_eos_rt and its jacfwd,
+// equations.py:517-535): d(RT)/dh = R_u sigma / cp,
+// d(RT)/dY_m = -R_u sigma h_m / cp + R_u T / W_m (sigma = sum Y/W).
+__global__ void __launch_bounds__(128)
+    k_flamelet_eos_rt(const double* __restrict__ Tt,
+                      const double* __restrict__ Y, int64_t ldy,
+                      double* __restrict__ rt, double* __restrict__ J,
+                      int64_t ldj, int64_t rows) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < rows;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const double T = Tt[r];
+    double sig = 0.0, cpp = 0.0;
+    for (int k = 0; k < NS; ++k) {
+      const double wk = __ldg(Y + (int64_t)k * ldy + r) * k_inv_mw[k];
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      sig += wk;
+      cpp = fma(wk,
+                fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]),
+                cpp);
+    }
+    const double rs = GAS_CONSTANT * sig;
+    rt[r] = GAS_CONSTANT * T / (1.0 / sig);
+    if (!J) continue;
+    const double inv_cp = 1.0 / (GAS_CONSTANT * cpp);
+    const double invT = 1.0 / T;
+    J[r] = rs * inv_cp;
+    for (int m = 0; m < NS; ++m) {
+      const pyro::Nasa a(m, T > k_tmid[m]);
+      const double hrt =
+          fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
+                            a[2] * (1.0 / 3.0)),
+                    a[1] * 0.5),
+              a[0]) +
+          a[5] * invT;
+      const double hm = GAS_CONSTANT * T * hrt * k_inv_mw[m];
+      J[(int64_t)(m + 1) * ldj + r] =
+          fma(-rs * inv_cp, hm, GAS_CONSTANT * T * k_inv_mw[m]);
+    }
   }
 }
 
@@ -199,9 +263,45 @@ PYRO_EXPORT int pyro_flamelet_blocks(const double* p, int64_t p_inc,
   int64_t blocks = (rows * 32 + 127) / 128;
   const int64_t cap = (int64_t)pyro_sm_count() * 32;
   if (blocks > cap) blocks = cap;
-  k_flamelet_blocks<<<(int)blocks, 128, 0, stream>>>(
+  k_flamelet_blocks<false><<<(int)blocks, 128, 0, stream>>>(
       p, p_inc, T, Y, ldy, chi, visc, row_off, sys_of_row, inv_dx2, L, C, U,
       rows);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_flamelet_adjoint_blocks(
+    const double* p, int64_t p_inc, const double* T, const double* Y,
+    int64_t ldy, const double* chi, const double* visc,
+    const int64_t* row_off, const int* sys_of_row, const double* inv_dx2,
+    double* L, double* C, double* U, int64_t rows, cudaStream_t stream) {
+  if (rows < 0 || ldy < rows) return PYRO_ERR_ARGUMENT;
+  if (rows == 0) return PYRO_OK;
+  if (!p || !T || !Y || !chi || !visc || !row_off || !sys_of_row ||
+      !inv_dx2 || !L || !C || !U)
+    return PYRO_ERR_ARGUMENT;
+  int64_t blocks = (rows * 32 + 127) / 128;
+  const int64_t cap = (int64_t)pyro_sm_count() * 32;
+  if (blocks > cap) blocks = cap;
+  k_flamelet_blocks<true><<<(int)blocks, 128, 0, stream>>>(
+      p, p_inc, T, Y, ldy, chi, visc, row_off, sys_of_row, inv_dx2, L, C, U,
+      rows);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+PYRO_EXPORT int pyro_flamelet_eos_rt(const double* T, const double* Y,
+                                     int64_t ldy, double* rt, double* J,
+                                     int64_t ldj, int64_t rows,
+                                     cudaStream_t stream) {
+  if (rows < 0 || ldy < rows || (J && ldj < rows)) return PYRO_ERR_ARGUMENT;
+  if (rows == 0) return PYRO_OK;
+  if (!T || !Y || !rt) return PYRO_ERR_ARGUMENT;
+  int64_t blocks = (rows + 127) / 128;
+  const int64_t cap = (int64_t)pyro_sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  k_flamelet_eos_rt<<<(int)blocks, 128, 0, stream>>>(T, Y, ldy, rt, J, ldj,
+                                                     rows);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }

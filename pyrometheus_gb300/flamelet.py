@@ -82,6 +82,7 @@ class BlockThomasSolver:
         self.use_graph = bool(use_graph)
         self._graph = None
         self._graph_key = None
+        self._factored = False
 
     def _launch(self, L, C, U, b, x, stream):
         if self.kernel == "small":
@@ -132,7 +133,45 @@ class BlockThomasSolver:
             self._graph.replay()
         else:
             self._launch(L, C, U, b, x, stream)
+        self._factored = True
         return x
+
+    def resolve(self, L, U, B, out=None):
+        """Solutions for further right-hand sides of the systems the last
+        :meth:`solve` factorised (its LU factors stay in the workspace):
+        ``B`` is ``[rows, nv]`` or ``[nrhs, rows, nv]``; ``L`` and ``U``
+        must be that call's blocks.  Only the vector recurrences run
+        (``4 nv^2`` FMAs per row and right-hand side)."""
+        if not self._factored:
+            raise RuntimeError("resolve() needs a solve() with the same "
+                               "blocks first")
+        nv, rows = self.nv, self.rows
+        single = B.dim() == 2
+        Bv = B[None] if single else B
+        if tuple(Bv.shape[1:]) != (rows, nv) or not (
+                Bv.is_cuda and Bv.dtype == torch.float64
+                and Bv.is_contiguous()):
+            raise ValueError(f"B must be a contiguous CUDA float64 tensor of "
+                             f"shape {(rows, nv)} or (nrhs, {rows}, {nv})")
+        for name, t in (("L", L), ("U", U)):
+            if tuple(t.shape) != (rows, nv, nv) or not t.is_contiguous():
+                raise ValueError(f"{name} must be the solved system's "
+                                 "blocks")
+        X = out if out is not None else torch.empty_like(B)
+        Xv = X[None] if single else X
+        if Xv.shape != Bv.shape or not Xv.is_contiguous():
+            raise ValueError("out must be contiguous and shaped like B")
+        stream = torch.cuda.current_stream(self.device)
+        n = Bv.shape[0]
+        for c0 in range(0, n, 4):
+            k = min(4, n - c0)
+            _check(self.lib.pyro_block_thomas_resolve(
+                L.data_ptr(), U.data_ptr(), Bv[c0].data_ptr(),
+                Xv[c0].data_ptr(), k, rows * nv, self.offsets.data_ptr(),
+                self.order.data_ptr(), self.nsys, nv, self.work.data_ptr(),
+                self.counter.data_ptr(), ctypes.c_void_p(stream.cuda_stream)),
+                "pyro_block_thomas_resolve")
+        return X
 
     def check_status(self):
         if int(self.status.item()) != 0:
@@ -386,6 +425,158 @@ class FlameletEquations:
             L.data_ptr(), C.data_ptr(), U.data_ptr(), self.rows,
             self._stream()), "flamelet blocks")
         return L, C, U
+
+    # {{{ compressible-EOS consistency (thermodynamic_consistency.py)
+
+    def adjoint_operator(self, h, Y, diss_rate, viscous_diss, temp_guess,
+                         pressure, temperature=None, out=None):
+        """Packed ``(L, C, U)`` of the adjoint operator of the
+        EOS-consistency solves (``FlameletEquations.adjoint_operator``,
+        ``equations.py:451-516``): ``Lap_c + (2/chi) dS/dphi^T`` inside,
+        ``chi/2 Lap_c`` at the boundary points, the Laplacian's own
+        couplings."""
+        h, Y = self._state(h, Y)
+        T = temperature if temperature is not None else \
+            self.temperature(h, Y, temp_guess)
+        p, p_inc = self._pressure(pressure)
+        nv = self.nv
+        if out is None:
+            f64 = dict(dtype=torch.float64, device=self.device)
+            out = tuple(torch.empty((self.rows, nv, nv), **f64)
+                        for _ in range(3))
+        L, C, U = out
+        self.th.get_reactor_jacobian(p, T, Y, out=C)
+        chi, visc = self._rowvec(diss_rate), self._rowvec(viscous_diss)
+        _check(self.th._lib.pyro_flamelet_adjoint_blocks(
+            p.data_ptr(), p_inc, T.data_ptr(), Y.data_ptr(), Y.stride(0),
+            chi.data_ptr(), visc.data_ptr(), self.row_off.data_ptr(),
+            self.sys_of_row.data_ptr(), self.inv_dx2.data_ptr(),
+            L.data_ptr(), C.data_ptr(), U.data_ptr(), self.rows,
+            self._stream()), "flamelet adjoint blocks")
+        return L, C, U
+
+    def eos_rt(self, h, Y, temp_guess=None, temperature=None,
+               jacobian=True):
+        """``(R T [rows], d(R T)/dphi [S+1, rows] or None)`` with
+        ``R = R_u / W_mix`` at T(h, Y) (``compressible_eos_rt`` and
+        ``compressible_eos_rt_jacobian``, ``equations.py:136-147,517-535``)."""
+        h, Y = self._state(h, Y)
+        T = temperature if temperature is not None else \
+            self.temperature(h, Y, temp_guess)
+        f64 = dict(dtype=torch.float64, device=self.device)
+        rt = torch.empty(self.rows, **f64)
+        J = torch.empty((self.nv, self.rows), **f64) if jacobian else None
+        _check(self.th._lib.pyro_flamelet_eos_rt(
+            T.data_ptr(), Y.data_ptr(), Y.stride(0), rt.data_ptr(),
+            J.data_ptr() if J is not None else None,
+            J.stride(0) if J is not None else self.rows, self.rows,
+            self._stream()), "flamelet eos rt")
+        return rt, J
+
+    def _sys_index(self):
+        if getattr(self, "_sidx", None) is None:
+            r0 = self.row_off[:-1]
+            r1 = self.row_off[1:]
+            self._sidx = (r0, r0 + 1, r0 + 2, r1 - 1, r1 - 2, r1 - 3)
+            w = torch.ones(self.rows, dtype=torch.float64, device=self.device)
+            w[r0] = 0.5
+            w[r1 - 1] = 0.5
+            self._trap_w = w
+            # (flamelet, position) of every row: per-flamelet sums as a
+            # dense [nsys, max length] reduction, in a fixed order
+            pos = np.concatenate([np.arange(n) for n in self.lengths])
+            self._pos = torch.as_tensor(pos, dtype=torch.int64,
+                                        device=self.device)
+        return self._sidx
+
+    def _traces(self, a):
+        """Per flamelet ``(1.5 a_0 + 2 a_1 - 0.5 a_2) / dx^2 + (1.5 a_{-1}
+        + 2 a_{-2} - 0.5 a_{-3}) / dx^2`` of a per-row field
+        (``thermodynamic_consistency.py:159-168``)."""
+        i0, i1, i2, j0, j1, j2 = self._sys_index()
+        ox = (1.5 * a[i0] + 2 * a[i1] - 0.5 * a[i2]) * self.inv_dx2
+        fu = (1.5 * a[j0] + 2 * a[j1] - 0.5 * a[j2]) * self.inv_dx2
+        return ox + fu
+
+    def _trapezoid(self, f):
+        """Per flamelet ``(f_0 + f_{N-1}) / 2 + sum of the interior``
+        (``trapezoidal_rule``, ``thermodynamic_consistency.py:31-42``)."""
+        self._sys_index()
+        dense = torch.zeros((self.nsys, int(self.lengths.max())),
+                            dtype=torch.float64, device=self.device)
+        dense[self.sys_of_row.long(), self._pos] = f * self._trap_w
+        return dense.sum(dim=1)
+
+    def _eos_solver(self, solver):
+        if solver is not None:
+            return solver
+        if getattr(self, "_bt", None) is None:
+            self._bt = BlockThomasSolver(self.nv, self.lengths,
+                                         device=self.device)
+        return self._bt
+
+    def enthalpy_gradient(self, h, Y, diss_rate, viscous_diss, temp_guess,
+                          pressure, pdf, solver=None):
+        """``(R T [rows], adjoint_h [S+1, rows], h_gradient [nsys])``: the
+        adjoint solve with right-hand side ``-e_h pdf`` and its boundary
+        traces, for every flamelet (``CompressibleEOS.enthalpy_gradient``,
+        ``thermodynamic_consistency.py:105-171``)."""
+        h, Y = self._state(h, Y)
+        T = self.temperature(h, Y, temp_guess)
+        rt, _ = self.eos_rt(h, Y, temperature=T, jacobian=False)
+        L, C, U = self.adjoint_operator(h, Y, diss_rate, viscous_diss, None,
+                                        pressure, temperature=T)
+        b = torch.zeros((self.rows, self.nv), dtype=torch.float64,
+                        device=self.device)
+        b[:, 0] = -self._rowvec(pdf)
+        bt = self._eos_solver(solver)
+        adj = bt.solve(L, C, U, b).T
+        bt.check_status()
+        return rt, adj, self._traces(adj[0])
+
+    def eos_gradient(self, h, Y, diss_rate, viscous_diss, temp_guess,
+                     pressure, pdf, solver=None):
+        """``((density_gradient [2, nsys], energy_gradient [2, nsys]),
+        (adjoint_d, adjoint_e) [S+1, rows])`` for every flamelet
+        (``CompressibleEOS.eos_gradient``,
+        ``thermodynamic_consistency.py:173-307``): row 0 of a gradient is
+        d/dp, row 1 d/dh at the boundaries.  The two adjoint solves share
+        one factorisation (``BlockThomasSolver.resolve``); the pressure
+        sensitivity of the source enters through the reactor VJP, ``v^T
+        dS/dp = -v_h S_h / p + v_Y^T d(W w / rho)/dp``."""
+        h, Y = self._state(h, Y)
+        T = self.temperature(h, Y, temp_guess)
+        p, _ = self._pressure(pressure)
+        chi, visc = self._rowvec(diss_rate), self._rowvec(viscous_diss)
+        pdf = self._rowvec(pdf)
+        rt, rtj = self.eos_rt(h, Y, temperature=T)
+        L, C, U = self.adjoint_operator(h, Y, chi, visc, None, p,
+                                        temperature=T)
+        f64 = dict(dtype=torch.float64, device=self.device)
+        B = torch.empty((2, self.rows, self.nv), **f64)
+        B[0] = (rtj * ((p / rt ** 2) * pdf)).T
+        B[1] = (rtj * pdf).T
+        B[1][:, 0] -= pdf
+        X = torch.empty_like(B)
+        bt = self._eos_solver(solver)
+        bt.solve(L, C, U, B[0], out=X[0])
+        bt.resolve(L, U, B[1:], out=X[1:])
+        bt.check_status()
+        adj_d, adj_e = X[0].T, X[1].T
+        rho = self.th.get_density(p, T, Y)
+        s_h = visc / rho
+        half_chi = 0.5 * chi
+        out = []
+        for adj, base in ((adj_d, pdf / rt), (adj_e, None)):
+            cot = torch.cat([torch.zeros((1, self.rows), **f64), adj[1:]])
+            _, _, gp = self.th.get_reactor_vjp(p, T, Y, cot)
+            g = (-adj[0] * s_h / p + gp) / half_chi
+            integrand = g if base is None else base + g
+            out.append(torch.stack([self._trapezoid(integrand),
+                                    self._traces(adj[0])]))
+        return (out[0], out[1]), (adj_d, adj_e)
+
+    # }}}
 
     def newton_step(self, h, Y, diss_rate, viscous_diss, temp_guess,
                     pressure, h_ox, h_fu, solver=None):

@@ -342,6 +342,35 @@ def make_mechanism(species_names: Sequence[str], n_reactions: int,
     return sol
 
 
+def scaled_rates(sol: Solution, factor: float) -> Solution:
+    """The mechanism with every rate coefficient multiplied by *factor*
+    (the pre-exponential factors of every Arrhenius expression, both limits
+    of a falloff reaction, so the falloff blending is unchanged); species,
+    thermo, stoichiometry and transport fits are shared.  A small factor
+    gives slow chemistry, e.g. flamelet operators dominated by diffusion."""
+    def arr(a):
+        return Arrhenius(a.pre_exponential_factor * factor,
+                         a.temperature_exponent, a.activation_energy)
+
+    reactions = []
+    for r in sol.reactions():
+        rate = r.rate
+        if isinstance(rate, TroeRate):
+            rate = TroeRate(arr(rate.low_rate), arr(rate.high_rate),
+                            rate.falloff_coeffs)
+        elif isinstance(rate, LindemannRate):
+            rate = LindemannRate(arr(rate.low_rate), arr(rate.high_rate))
+        else:
+            rate = arr(rate)
+        reactions.append(Reaction(r.equation, r.reactants, r.products, rate,
+                                  r.reversible, r.orders, r.third_body,
+                                  r.duplicate))
+    out = Solution(sol.species(), reactions, sol.element_names,
+                   source=sol.source, name=sol.name,
+                   transport=sol.transport)
+    return out
+
+
 def config1_mechanism(seed: int = 1) -> Solution:
     """9 species (H, O, N, Ar) / 24 reversible reactions: 3 three-body,
     2 Troe falloff, 19 elementary; written downhill at 1500 K."""

@@ -330,6 +330,119 @@ def golden_flamelet(fname="flamelet.npz"):
     print(f"wrote {fname}")
 
 
+def eos_adjoint(sol, case, cls, ref, pdf):
+    """The reference's compressible-EOS adjoint pieces for one flamelet:
+    ``FlameletEquations.adjoint_operator`` (``equations.py:451-516``),
+    ``compressible_eos_rt`` and its ``jacfwd`` (``:517-535``,
+    ``:136-147``), ``source_gradient_wrt_pressure`` (``:130-134``) and
+    ``CompressibleEOS.enthalpy_gradient`` / ``eos_gradient``
+    (``thermodynamic_consistency.py:105-307``).  The generated class
+    evaluates the chemistry (torch + ``jacfwd`` standing in for the
+    reference's ``jax.vmap(jax.jacfwd(...))``), the reference's own
+    ``block_thomas`` (numpy ``lax.scan`` stand-in, ``oracle/refgen.py``)
+    solves; the assembly and contractions are restated from the
+    reference's JAX modules, which cannot be imported here."""
+    import torch
+    from torch.func import jacfwd, vmap
+    S = sol.n_species
+    nv = S + 1
+    y, h, dx = case["Y"], case["h"], float(case["dx"])
+    n_x = y.shape[1]
+    p = float(case["P"])
+    chi, visc, tg = case["chi"], case["visc"], case["T_guess"]
+    mw = np.asarray(ref.molecular_weights, dtype=np.float64)
+    th = torch_reference(cls)
+    mwt = torch.tensor(mw)
+
+    def local(x, vd, tgi, pres):
+        hh, yy = x[0], x[1:]
+        tt = _enthalpy_newton(th, hh, yy, tgi, fixed_iters=40)
+        rr = th.get_density(pres, tt, yy)
+        ww = th.get_net_production_rates(rr, tt, yy)
+        return torch.cat([(vd / rr)[None], mwt * ww / rr])
+
+    def local_rt(x, tgi):
+        hh, yy = x[0], x[1:]
+        tt = _enthalpy_newton(th, hh, yy, tgi, fixed_iters=40)
+        return th.gas_constant * tt / th.get_mixture_molecular_weight(yy)
+
+    xs = torch.tensor(np.vstack([h, y]).T.copy())
+    args = (xs, torch.tensor(visc), torch.tensor(tg), torch.tensor(p))
+    sj = vmap(jacfwd(local), in_dims=(0, 0, 0, None))(*args).numpy()
+    ds_dp = vmap(jacfwd(local, argnums=3), in_dims=(0, 0, 0, None))(
+        *args).numpy()
+    rt_jac = vmap(jacfwd(local_rt), in_dims=(0, 0))(
+        xs, torch.tensor(tg)).numpy()
+    t = _enthalpy_newton(ref, h, y, tg)
+    rt = np.asarray(ref.gas_constant * t
+                    / ref.get_mixture_molecular_weight(y))
+    # adjoint operator
+    eye = np.eye(nv)
+    lap_c = np.stack([eye / dx ** 2] + [-2.0 * eye / dx ** 2] * (n_x - 2)
+                     + [eye / dx ** 2])
+    lap_l = np.stack([eye / dx ** 2] * (n_x - 2) + [0.0 * eye])
+    lap_u = np.stack([0.0 * eye] + [eye / dx ** 2] * (n_x - 2))
+    zeros = np.zeros((1, nv, nv))
+    src = np.concatenate([zeros, np.transpose(
+        2 * sj[1:-1] / chi[1:-1, None, None], (0, 2, 1)), zeros])
+    central = np.concatenate([
+        (0.5 * chi[0] * lap_c[0])[None], lap_c[1:-1],
+        (0.5 * chi[-1] * lap_c[-1])[None]]) + src
+    bt = refgen.reference_block_thomas()
+
+    def traces(a):
+        ox = (1.5 * a[0] + 2 * a[1] - 0.5 * a[2]) / dx ** 2
+        fu = (1.5 * a[-1] + 2 * a[-2] - 0.5 * a[-3]) / dx ** 2
+        return ox + fu
+
+    def trapezoid(f):
+        return 0.5 * (f[0] + f[-1]) + np.sum(f[1:-1])
+
+    unit_h = np.zeros((nv, n_x))
+    unit_h[0] = 1.0
+    adj_h = np.asarray(bt(lap_l, central, lap_u, (-unit_h * pdf).T)).T
+    dsdp = ds_dp / (0.5 * chi[:, None])
+    rhs_d = (p / rt ** 2) * rt_jac.T * pdf
+    adj_d = np.asarray(bt(lap_l, central, lap_u, rhs_d.T)).T
+    integ = (1 / rt) * pdf + np.einsum("ij,ji->i", dsdp, adj_d)
+    dens = np.array([trapezoid(integ), traces(adj_d[0])])
+    rhs_e = -(unit_h - rt_jac.T) * pdf
+    adj_e = np.asarray(bt(lap_l, central, lap_u, rhs_e.T)).T
+    integ = np.einsum("ij,ji->i", dsdp, adj_e)
+    ener = np.array([trapezoid(integ), traces(adj_e[0])])
+    return dict(pdf=pdf, src_jac_all=sj, ds_dp=ds_dp, rt=rt, rt_jac=rt_jac,
+                adj_L=lap_l, adj_C=central, adj_U=lap_u, adj_h=adj_h,
+                h_gradient=np.asarray(traces(adj_h[0])), adj_d=adj_d,
+                adj_e=adj_e, density_gradient=dens, energy_gradient=ener)
+
+
+def golden_eos_adjoint(fname="eos_adjoint.npz"):
+    """Two cases per mechanism: the benchmark mechanism (stiff: its adjoint
+    operators have condition numbers of 1e15 and more, so gradients are
+    compared stage by stage), and the same mechanism with every rate
+    scaled down (``synthetic.scaled_rates``: 1e-12 and 1e-30), whose
+    diffusion-dominated adjoint systems are well conditioned, for
+    end-to-end gradient comparisons."""
+    out = {}
+    for tag, sol, n_x, seed in (
+            ("s9", synthetic.config1_mechanism(), 12, 41),
+            ("s53", synthetic.config2_mechanism(), 8, 43),
+            ("s9slow", synthetic.scaled_rates(synthetic.config1_mechanism(),
+                                              1e-12), 12, 44),
+            ("s53slow", synthetic.scaled_rates(
+                synthetic.config2_mechanism(), 1e-30), 8, 45)):
+        case, cls, ref = flamelet_case(sol, n_x, seed)
+        z = case["z"]
+        pdf = 1e-3 + z ** 1.5 * (1.0 - z) ** 2.5
+        pdf = pdf / pdf.sum()
+        case.update(eos_adjoint(sol, case, cls, ref, pdf))
+        case["mech_yaml"] = np.array(dump_mechanism(sol))
+        for k, v in case.items():
+            out[f"{tag}_{k}"] = v
+    np.savez_compressed(os.path.join(HERE, fname), **out)
+    print(f"wrote {fname}")
+
+
 def golden_transport(fname="transport.npz"):
     """The reference's generated transport methods (``python.py:564-641``)
     on the synthetic mechanisms' kinetic-theory fits.  The last two states
@@ -379,6 +492,7 @@ def main():
     golden_block_thomas()
     golden_flamelet()
     golden_transport()
+    golden_eos_adjoint()
 
 
 if __name__ == "__main__":
