@@ -368,6 +368,7 @@ def secondary_legs(sol, th, dev, dfma):
     out["block_thomas"] = bt
     torch.cuda.empty_cache()
     out["flamelet_newton"] = flamelet_newton_legs(dev, dfma)
+    out["eos_adjoint"] = eos_adjoint_legs(dev)
     return out
 
 
@@ -486,6 +487,67 @@ def flamelet_newton_legs(dev, dfma):
             "residual_inf_after": r_after,
             "block_thomas": f"{solver.kernel}:{solver.threads}"}
         del blocks, solver, x, b, eq, th, Y, h, R0
+        torch.cuda.empty_cache()
+    return res
+
+
+def eos_adjoint_legs(dev):
+    """The compressible-EOS consistency gradients
+    (``CompressibleEOS.eos_gradient``) of 4,096 flamelets at once, for the
+    9- and 53-species mechanisms on the flamelet leg's seeded profiles: T
+    Newton, R T and its gradient, the adjoint operator (reactor Jacobian +
+    block assembly), one block-Thomas factorisation shared by the density
+    and energy adjoint solves (the second through the re-solve with kept
+    factors), the pressure sensitivities through the reactor VJP and the
+    per-flamelet contractions.  Also times one factorising solve against
+    a two-right-hand-side re-solve on the same blocks."""
+    import numpy as np
+    import torch
+
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
+    from pyrometheus_gb300.flamelet import FlameletEquations
+    res = {}
+    for tag, sol in (("s9", synthetic.config1_mechanism()),
+                     ("s53", synthetic.config2_mechanism())):
+        lengths = np.random.default_rng(3).integers(64, 1025, size=4096)
+        prof = synthetic.flamelet_profiles(sol, lengths, seed=4)
+        th = get_thermochem_class(sol)(device=dev)
+        eq = FlameletEquations(th, lengths, prof["dx"], prof["y_ox"],
+                               prof["y_fu"], device=dev)
+        Y = torch.as_tensor(prof["Y"], device=dev)
+        T0 = torch.as_tensor(prof["T"], device=dev)
+        h = th.get_mixture_enthalpy_mass(T0, Y)
+        chi = torch.as_tensor(prof["chi"], device=dev)
+        visc = torch.zeros_like(chi)
+        rows, nv = int(np.sum(lengths)), sol.n_species + 1
+        z = torch.cat([torch.linspace(0.0, 1.0, int(n), dtype=torch.float64,
+                                      device=dev) for n in lengths])
+        pdf = 1e-3 + z ** 1.5 * (1.0 - z) ** 2.5
+        # one factorising solve vs a two-right-hand-side re-solve
+        L, C, U = eq.adjoint_operator(h, Y, chi, visc, T0, 1e5)
+        bt = eq._eos_solver(None)
+        g = torch.Generator(device=dev).manual_seed(7)
+        b = torch.randn((rows, nv), generator=g, dtype=torch.float64,
+                        device=dev)
+        B2 = torch.randn((2, rows, nv), generator=g, dtype=torch.float64,
+                         device=dev)
+        ms_solve = _event_ms(lambda: bt.solve(L, C, U, b), 1)
+        ms_resolve = _event_ms(lambda: bt.resolve(L, U, B2), 2)
+        del L, C, U, b, B2
+        torch.cuda.empty_cache()
+        ms = _event_ms(lambda: eq.eos_gradient(h, Y, chi, visc, T0, 1e5,
+                                               pdf), 2)
+        (dens, ener), _ = eq.eos_gradient(h, Y, chi, visc, T0, 1e5, pdf)
+        res[tag] = {
+            "flamelets": len(lengths), "points": rows, "nv": nv,
+            "eos_gradient_ms": ms,
+            "flamelet_gradients_per_s": len(lengths) / ms * 1e3,
+            "factorising_solve_ms": ms_solve,
+            "resolve_2rhs_ms": ms_resolve,
+            "finite_gradients": int(torch.isfinite(dens).all()
+                                    & torch.isfinite(ener).all()),
+            "pdf": "1e-3 + Z^1.5 (1 - Z)^2.5 per flamelet"}
+        del eq, th, Y, h, T0, chi, visc, z, pdf, dens, ener
         torch.cuda.empty_cache()
     return res
 

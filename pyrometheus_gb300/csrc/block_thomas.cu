@@ -585,22 +585,35 @@ PYRO_EXPORT int pyro_block_thomas_small(const double* L, const double* C,
 //   forward:  b'_0 = b_0, b'_i = b_i - L_{i-1} t_{i-1}, t_i = C'_i^-1 b'_i
 //   backward: x_{N-1} = t_{N-1}, x_i = C'_i^-1 (b'_i - U_i x_{i+1})
 // -- 4 nv^2 FMAs per row and right-hand side instead of ~4.7 nv^3.  One
-// warp per system; the lanes take matrix rows, the NRHS right-hand sides
-// share every block element they load; b'_i is kept in x until the
-// backward pass overwrites it.  Systems come from an atomic counter in the
-// caller's order.
+// warp per system, the lanes over matrix rows, the NRHS right-hand sides
+// sharing every block element the lanes read (through L1).  A warp-wide
+// FP64 instruction costs the FP64 pipe the same however few lanes it
+// uses, so the nv diagonal reciprocals of a row's factors are formed by
+// the lanes side by side once per row, not one per elimination step.
+// b'_i is kept in x until the backward pass overwrites it.  Systems come
+// from an atomic counter in the caller's order.
 
 namespace {
 
+constexpr int kResolveWarps = 4;
+
 // y <- C'^-1 y for NRHS vectors y[q * 64 + i] (warp-private shared
-// memory), factors A (nv x nv, row-major) and pivots from the workspace.
+// memory), factors A (nv x nv, row-major) and pivots from the workspace;
+// rd: warp-private scratch for the diagonal reciprocals (64 doubles) and
+// the pivots (64 ints after them).
 template <int NRHS>
 __device__ void warp_lu_solve(const double* __restrict__ A,
                               const double* __restrict__ pv, int nv,
-                              double* y, int lane) {
+                              double* y, double* rd, int lane) {
+  int* ps = (int*)(rd + 64);
+  for (int k = lane; k < nv; k += 32) {
+    rd[k] = 1.0 / __ldg(A + k * nv + k);
+    ps[k] = (int)__ldg(pv + k);
+  }
+  __syncwarp();
   if (lane == 0) {
     for (int k = 0; k < nv; ++k) {
-      const int p = (int)pv[k];
+      const int p = ps[k];
       if (p != k)
 #pragma unroll
         for (int q = 0; q < NRHS; ++q) {
@@ -627,7 +640,7 @@ __device__ void warp_lu_solve(const double* __restrict__ A,
   // upper
   for (int k = nv - 1; k >= 0; --k) {
     double yk[NRHS];
-    const double inv = 1.0 / __ldg(A + k * nv + k);
+    const double inv = rd[k];
 #pragma unroll
     for (int q = 0; q < NRHS; ++q) yk[q] = y[q * 64 + k] * inv;
     __syncwarp();
@@ -644,7 +657,7 @@ __device__ void warp_lu_solve(const double* __restrict__ A,
   }
 }
 
-// y[q][j] = v[q][j] - sum_k M[j][k] z[q][k] for the warp's rows j.
+// y[q][j] -= sum_k M[j][k] z[q][k] for the warp's rows j.
 template <int NRHS>
 __device__ __forceinline__ void warp_matvec_sub(
     const double* __restrict__ M, const double* z, int nv, int lane,
@@ -663,8 +676,6 @@ __device__ __forceinline__ void warp_matvec_sub(
   }
 }
 
-constexpr int kResolveWarps = 4;
-
 template <int NRHS>
 __global__ void __launch_bounds__(32 * kResolveWarps)
     k_block_thomas_resolve(const double* __restrict__ Lm,
@@ -675,10 +686,11 @@ __global__ void __launch_bounds__(32 * kResolveWarps)
                            const int* __restrict__ order, int nsys, int nv,
                            const double* __restrict__ work,
                            int* __restrict__ counter) {
-  __shared__ double s_vec[kResolveWarps][2][NRHS * 64];
+  __shared__ double s_vec[kResolveWarps][2 * NRHS * 64 + 96];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* y = s_vec[wid][0];  // current vector
-  double* z = s_vec[wid][1];  // previous t_{i-1} / x_{i+1}
+  double* y = s_vec[wid];            // current vector
+  double* z = y + NRHS * 64;         // previous t_{i-1} / x_{i+1}
+  double* rd = z + NRHS * 64;        // diagonal reciprocals, pivots
   const int64_t nn = (int64_t)nv * nv, wrow = nn + 2 * nv;
   for (;;) {
     int q = 0;
@@ -706,7 +718,7 @@ __global__ void __launch_bounds__(32 * kResolveWarps)
         for (int c = 0; c < NRHS; ++c)
           X[c * rhs_stride + row * nv + j] = y[c * 64 + j];
       const double* w = work + row * wrow;
-      warp_lu_solve<NRHS>(w, w + nn + nv, nv, y, lane);
+      warp_lu_solve<NRHS>(w, w + nn + nv, nv, y, rd, lane);
       double* t = z;
       z = y;
       y = t;
@@ -729,7 +741,7 @@ __global__ void __launch_bounds__(32 * kResolveWarps)
       warp_matvec_sub<NRHS>(Um + row * nn, z, nv, lane, y);
       __syncwarp();
       const double* w = work + row * wrow;
-      warp_lu_solve<NRHS>(w, w + nn + nv, nv, y, lane);
+      warp_lu_solve<NRHS>(w, w + nn + nv, nv, y, rd, lane);
       for (int j = lane; j < nv; j += 32)
 #pragma unroll
         for (int c = 0; c < NRHS; ++c)
@@ -740,6 +752,20 @@ __global__ void __launch_bounds__(32 * kResolveWarps)
       __syncwarp();
     }
   }
+}
+
+template <int NRHS>
+int launch_resolve(const double* L, const double* U, const double* B,
+                   double* X, int64_t rhs_stride, const int64_t* row_off,
+                   const int* order, int nsys, int nv, const double* work,
+                   int* counter, cudaStream_t stream) {
+  int blocks = (nsys + kResolveWarps - 1) / kResolveWarps;
+  const int cap = pyro_sm_count() * 16;
+  if (blocks > cap) blocks = cap;
+  k_block_thomas_resolve<NRHS><<<blocks, 32 * kResolveWarps, 0, stream>>>(
+      L, U, B, X, rhs_stride, row_off, order, nsys, nv, work, counter);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
 }
 
 }  // namespace
@@ -762,30 +788,20 @@ PYRO_EXPORT int pyro_block_thomas_resolve(
   if (nrhs > 1 && rhs_stride < 1) return PYRO_ERR_ARGUMENT;
   if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess)
     return PYRO_ERR_LAUNCH;
-  int blocks = (nsys + kResolveWarps - 1) / kResolveWarps;
-  const int cap = pyro_sm_count() * 16;
-  if (blocks > cap) blocks = cap;
-  const int threads = 32 * kResolveWarps;
   switch (nrhs) {
     case 1:
-      k_block_thomas_resolve<1><<<blocks, threads, 0, stream>>>(
-          L, U, B, X, rhs_stride, row_off, order, nsys, nv, work, counter);
-      break;
+      return launch_resolve<1>(L, U, B, X, rhs_stride, row_off, order, nsys,
+                               nv, work, counter, stream);
     case 2:
-      k_block_thomas_resolve<2><<<blocks, threads, 0, stream>>>(
-          L, U, B, X, rhs_stride, row_off, order, nsys, nv, work, counter);
-      break;
+      return launch_resolve<2>(L, U, B, X, rhs_stride, row_off, order, nsys,
+                               nv, work, counter, stream);
     case 3:
-      k_block_thomas_resolve<3><<<blocks, threads, 0, stream>>>(
-          L, U, B, X, rhs_stride, row_off, order, nsys, nv, work, counter);
-      break;
+      return launch_resolve<3>(L, U, B, X, rhs_stride, row_off, order, nsys,
+                               nv, work, counter, stream);
     default:
-      k_block_thomas_resolve<4><<<blocks, threads, 0, stream>>>(
-          L, U, B, X, rhs_stride, row_off, order, nsys, nv, work, counter);
-      break;
+      return launch_resolve<4>(L, U, B, X, rhs_stride, row_off, order, nsys,
+                               nv, work, counter, stream);
   }
-  PYRO_CHECK_LAUNCH();
-  return PYRO_OK;
 }
 
 // ------------------------------------------------------------------------
