@@ -1,6 +1,6 @@
 """Writes exp_table.cuh: 2^(j/2048), j = 0..2047, correctly rounded to
-double (60-digit mpmath evaluation), plus the Cody-Waite split of ln2/2048,
-for the table-driven exponential of pyro_math.cuh.
+double (60-digit mpmath evaluation), plus ln2/2048 rounded to double and
+its Cody-Waite split, for the table-driven exponential of pyro_math.cuh.
 
     python pyrometheus_gb300/csrc/make_exp_table.py
 """
@@ -35,6 +35,7 @@ def main():
                 "rounded, j = 0..2047.\n#pragma once\n\n")
         f.write(f"#define PYRO_EXP_N {N}\n")
         f.write(f"#define PYRO_EXP_INV_L {float.hex(inv)}  // 2048/ln2\n")
+        f.write(f"#define PYRO_EXP_L {float.hex(rn(ln2_n))}  // ln2/2048\n")
         f.write(f"#define PYRO_EXP_L1 {float.hex(l1)}  // ln2/2048, 32 bits\n")
         f.write(f"#define PYRO_EXP_L2 {float.hex(l2)}  // ln2/2048 - L1\n\n")
         f.write("__device__ const double pyro_exp_table[PYRO_EXP_N] = {\n")

@@ -9,11 +9,15 @@
 //   exp(r) - 1 ~= r + r^2/2 + r^3/6   (truncation < 0.15 ulp at |r| max).
 //
 // k = round(x 2048/ln2) comes from adding 1.5 * 2^52 (its low word is k);
-// r uses a two-constant Cody-Waite split of ln2/2048 whose leading part has
-// 32 significant bits, so k * L1 is exact for |x| < 708.  The 2^(j/2048)
-// values (correctly rounded, exp_table.cuh) are staged in shared memory once
-// per block.  Cost: 8 FP64 instructions per call (CUDA's exp costs about
-// 20 DFMA-equivalents on GB300's FP64 pipe).  |x| >= 708, inf and nan go to
+// r = x - k L with L = ln2/2048 rounded to double, one FMA.  L's rounding
+// (|L - ln2/2048| < 2.7e-20) puts a relative error below |x| 8e-17 on the
+// result: under the |x| 1.1e-16 that the rounding of x itself carries
+// through exp, so the one-constant reduction loses nothing against the
+// argument's own precision (a two-constant Cody-Waite split, PYRO_EXP_L1 /
+// L2, would cost one more FMA per call).  The 2^(j/2048) values (correctly
+// rounded, exp_table.cuh) are staged in shared memory once per block.
+// Cost: 7 FP64 instructions per call (CUDA's exp costs about 20
+// DFMA-equivalents on GB300's FP64 pipe).  |x| >= 708, inf and nan go to
 // CUDA's exp, which handles overflow, gradual underflow and specials.
 #pragma once
 
@@ -34,8 +38,7 @@ __device__ __forceinline__ double pyro_exp_core(double x) {
   const double s = fma(x, PYRO_EXP_INV_L, 0x1.8p52);
   const double kd = s - 0x1.8p52;
   const int k = __double2loint(s);
-  double r = fma(-kd, PYRO_EXP_L1, x);
-  r = fma(-kd, PYRO_EXP_L2, r);
+  const double r = fma(-kd, PYRO_EXP_L, x);
   const double p = fma(r * r, fma(r, 1.0 / 6.0, 0.5), r);
   const double t = pyro_exp_smem[k & (PYRO_EXP_N - 1)];
   const double v = fma(t, p, t);

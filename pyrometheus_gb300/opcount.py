@@ -8,7 +8,7 @@ arithmetic as 1 flop, FMA as 2, division as 1 -- and, separately, the
 transcendental calls (``exp``, ``log``, ``log10``, ``exp10``, ``pow``).
 
 A transcendental is charged the FP64 flops of the implementation the
-kernels use: the table-driven exponential and logarithm (14 and 22 flops
+kernels use: the table-driven exponential and logarithm (12 and 22 flops
 per call, see ``csrc/pyro_math.cuh``) and, for ``pow``, CUDA's libm log at
 the FP64-pipe cost the benchmark measures (``DFMA FLOP/s / log/s``).  Then
 ``algorithmic flops / kernel time / DFMA peak`` is the fraction of the FP64
@@ -143,8 +143,8 @@ def libm_weights(dfma_flops: float, exp_rate: float, log_rate: float
 
 
 #: FP64 flops of one call of the table-driven exponential
-#: (csrc/pyro_math.cuh): 6 FMAs, one add, one multiply.
-TANG_EXP_FLOPS = 14.0
+#: (csrc/pyro_math.cuh): 5 FMAs, one add, one multiply.
+TANG_EXP_FLOPS = 12.0
 
 #: FP64 flops of one call of the table-driven logarithm
 #: (csrc/pyro_math.cuh): 8 FMAs, three multiplies, three adds (the two

@@ -460,7 +460,7 @@ class CudaThermochemistryBase:
 
     def get_net_production_rates_and_temperature(
             self, pressure, temperature, mass_fractions, energy, t_guess,
-            do_energy=True, check=True, out=None, chunk=1 << 19):
+            do_energy=True, check=True, out=None, chunk=1 << 18):
         """One pass per state of ``rho = get_density(p, T, Y)``,
         ``get_net_production_rates(rho, T, Y)`` and
         ``get_temperature(energy, t_guess, Y, do_energy)``.
