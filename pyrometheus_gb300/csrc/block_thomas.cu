@@ -147,7 +147,11 @@ __device__ void lu_solve(const double* A, double* R, int ld, int nv,
 }
 
 // One system (rows r0 .. r0+N-1): forward elimination, then the backward
-// solves with the kept factors.  All threads of the CTA take part.
+// solves with the kept factors.  All threads of the CTA take part.  Three
+// shared blocks: A (C'_i and its factors) and two that trade roles every
+// row -- P holds S_{i-1} | t_{i-1}, R first L_{i-1}, then U_i | b'_i, then
+// S_i | t_i, after which the two swap (no copy, and three blocks instead
+// of four let more CTAs share an SM).
 __device__ void solve_system(const double* __restrict__ Lm,
                              const double* __restrict__ Cm,
                              const double* __restrict__ Um,
@@ -157,17 +161,16 @@ __device__ void solve_system(const double* __restrict__ Lm,
                              double* smem, int* s_sing) {
   const int ld = nv + 1;
   double* A = smem;          // C'_i | b'_i, then LU factors | b'_i
-  double* R = A + nv * ld;   // U_i | b'_i -> S_i | t_i
-  double* Lb = R + nv * ld;  // L_{i-1}
-  double* P = Lb + nv * ld;  // S_{i-1} | t_{i-1}
-  int* piv = (int*)(P + nv * ld);
+  double* P = A + nv * ld;   // S_{i-1} | t_{i-1}
+  double* R = P + nv * ld;   // L_{i-1}, then U_i | b'_i -> S_i | t_i
+  int* piv = (int*)(R + nv * ld);
   const int64_t wrow = (int64_t)nv * nv + 2 * nv;
   for (int i = 0; i < N; ++i) {
     const int64_t row = r0 + i;
     load_block(A, ld, Cm + row * nv * nv, nv);
     for (int j = threadIdx.x; j < nv; j += blockDim.x)
       A[j * ld + nv] = __ldg(B + row * nv + j);  // b in column nv of A
-    if (i > 0) load_block(Lb, ld, Lm + (row - 1) * nv * nv, nv);
+    if (i > 0) load_block(R, ld, Lm + (row - 1) * nv * nv, nv);
     __syncthreads();
     if (i > 0) {
       // C' = C - L S_prev ; b' = b - L t_prev (t_prev in column nv of P)
@@ -175,7 +178,7 @@ __device__ void solve_system(const double* __restrict__ Lm,
         const int r = e / ld, c = e - (e / ld) * ld;
         double acc = A[r * ld + c];
         for (int k = 0; k < nv; ++k)
-          acc = fma(-Lb[r * ld + k], P[k * ld + c], acc);
+          acc = fma(-R[r * ld + k], P[k * ld + c], acc);
         A[r * ld + c] = acc;
       }
       __syncthreads();
@@ -202,11 +205,14 @@ __device__ void solve_system(const double* __restrict__ Lm,
       lu_solve(A, R, ld, nv, nv + 1, 0, piv);
     else
       lu_solve(A, R, ld, nv, 1, nv, piv);
-    for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) P[e] = R[e];
-    __syncthreads();
+    double* t = P;  // lu_solve ended with a barrier
+    P = R;
+    R = t;
   }
-  // backward: x_{N-1} = t_{N-1}; x_i = C'_i^-1 (b'_i - U_i x_{i+1})
-  double* xs = Lb;  // x_{i+1}
+  // backward: x_{N-1} = t_{N-1}; x_i = C'_i^-1 (b'_i - U_i x_{i+1}).
+  // x_{i+1} lives in the first nv entries of P (row 0 of the block; the
+  // t column read below sits at indices >= nv).
+  double* xs = P;
   {
     const int64_t row = r0 + N - 1;
     for (int j = threadIdx.x; j < nv; j += blockDim.x) {
@@ -493,7 +499,7 @@ PYRO_EXPORT int64_t pyro_block_thomas_work_doubles(int nv, int64_t rows) {
 
 // Shared memory of one CTA for block size nv.
 PYRO_EXPORT int64_t pyro_block_thomas_smem_bytes(int nv) {
-  return (int64_t)4 * nv * (nv + 1) * 8 + (int64_t)nv * 4;
+  return (int64_t)3 * nv * (nv + 1) * 8 + (int64_t)nv * 4;
 }
 
 // Solve nsys block-tridiagonal systems (packed as described above).

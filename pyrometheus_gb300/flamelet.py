@@ -221,7 +221,7 @@ def _tuned():
 
 
 def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
-             n_max: int = 1024, candidates=(32, 64, 128, 256),
+             n_max: int = 1024, candidates=(32, 64, 128, 256, 384, 512),
              seed: int = 0, device=None, repeats: int = 3, lengths=None):
     """Time the solve for each kernel and CTA size (the CTA kernel at each
     of *candidates*, and for nv <= 16 the one-thread-per-system kernel at 32
@@ -244,7 +244,10 @@ def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
                     generator=gen)
     b = torch.randn((rows, nv), dtype=torch.float64, device=dev,
                     generator=gen)
-    plans = [("cta", th) for th in candidates if not (nv > th and th < 64)]
+    # CTAs narrower than a block row, or wider than 256 threads for blocks
+    # of at most 24 (too few matrix elements to share), are skipped
+    plans = [("cta", th) for th in candidates
+             if not (nv > th and th < 64) and not (nv <= 24 and th > 256)]
     if nv <= 16:
         plans += [("small", th) for th in (32, 64)
                   if 3 * nv * (nv + 1) * 8 * th <= 227 * 1024]
