@@ -147,11 +147,12 @@ __device__ void lu_solve(const double* A, double* R, int ld, int nv,
 }
 
 // One system (rows r0 .. r0+N-1): forward elimination, then the backward
-// solves with the kept factors.  All threads of the CTA take part.  Three
-// shared blocks: A (C'_i and its factors) and two that trade roles every
-// row -- P holds S_{i-1} | t_{i-1}, R first L_{i-1}, then U_i | b'_i, then
-// S_i | t_i, after which the two swap (no copy, and three blocks instead
-// of four let more CTAs share an SM).
+// solves with the kept factors.  All threads of the CTA take part.  Two
+// shared blocks: A (C'_i and its factors) and Q, which holds S_{i-1} |
+// t_{i-1} for the update C'_i = C_i - L_{i-1} S_{i-1} (L_{i-1} is read
+// from global memory: a CTA's threads share each element through L1), then
+// U_i | b'_i, solved in place into S_i | t_i for the next row.  Two blocks
+// instead of four let four CTAs share an SM at nv = 54.
 __device__ void solve_system(const double* __restrict__ Lm,
                              const double* __restrict__ Cm,
                              const double* __restrict__ Um,
@@ -161,33 +162,32 @@ __device__ void solve_system(const double* __restrict__ Lm,
                              double* smem, int* s_sing) {
   const int ld = nv + 1;
   double* A = smem;          // C'_i | b'_i, then LU factors | b'_i
-  double* P = A + nv * ld;   // S_{i-1} | t_{i-1}
-  double* R = P + nv * ld;   // L_{i-1}, then U_i | b'_i -> S_i | t_i
-  int* piv = (int*)(R + nv * ld);
+  double* Q = A + nv * ld;   // S_{i-1} | t_{i-1}, then U_i | b'_i -> S_i | t_i
+  int* piv = (int*)(Q + nv * ld);
   const int64_t wrow = (int64_t)nv * nv + 2 * nv;
   for (int i = 0; i < N; ++i) {
     const int64_t row = r0 + i;
     load_block(A, ld, Cm + row * nv * nv, nv);
     for (int j = threadIdx.x; j < nv; j += blockDim.x)
       A[j * ld + nv] = __ldg(B + row * nv + j);  // b in column nv of A
-    if (i > 0) load_block(R, ld, Lm + (row - 1) * nv * nv, nv);
     __syncthreads();
     if (i > 0) {
-      // C' = C - L S_prev ; b' = b - L t_prev (t_prev in column nv of P)
+      // C' = C - L S_prev ; b' = b - L t_prev (t_prev in column nv of Q)
+      const double* __restrict__ Lb = Lm + (row - 1) * nv * nv;
       for (int e = threadIdx.x; e < nv * ld; e += blockDim.x) {
         const int r = e / ld, c = e - (e / ld) * ld;
         double acc = A[r * ld + c];
         for (int k = 0; k < nv; ++k)
-          acc = fma(-R[r * ld + k], P[k * ld + c], acc);
+          acc = fma(-__ldg(Lb + r * nv + k), Q[k * ld + c], acc);
         A[r * ld + c] = acc;
       }
       __syncthreads();
     }
     // right-hand sides: U_i (if any) and b'_i
     const bool has_u = i < N - 1;
-    if (has_u) load_block(R, ld, Um + row * nv * nv, nv);
+    if (has_u) load_block(Q, ld, Um + row * nv * nv, nv);
     for (int j = threadIdx.x; j < nv; j += blockDim.x)
-      R[j * ld + nv] = A[j * ld + nv];
+      Q[j * ld + nv] = A[j * ld + nv];
     __syncthreads();
     lu_factor(A, ld, nv, piv, s_sing);
     // keep the factors, b'_i and the pivots for the backward solve
@@ -202,21 +202,18 @@ __device__ void solve_system(const double* __restrict__ Lm,
     for (int k = threadIdx.x; k < nv; k += blockDim.x)
       w[nv * nv + nv + k] = (double)piv[k];
     if (has_u)
-      lu_solve(A, R, ld, nv, nv + 1, 0, piv);
+      lu_solve(A, Q, ld, nv, nv + 1, 0, piv);
     else
-      lu_solve(A, R, ld, nv, 1, nv, piv);
-    double* t = P;  // lu_solve ended with a barrier
-    P = R;
-    R = t;
+      lu_solve(A, Q, ld, nv, 1, nv, piv);
   }
   // backward: x_{N-1} = t_{N-1}; x_i = C'_i^-1 (b'_i - U_i x_{i+1}).
-  // x_{i+1} lives in the first nv entries of P (row 0 of the block; the
-  // t column read below sits at indices >= nv).
-  double* xs = P;
+  // x_{i+1} lives in the first nv entries of Q (row 0 of the block); the
+  // right-hand side column nv sits at indices >= nv.
+  double* xs = Q;
   {
     const int64_t row = r0 + N - 1;
     for (int j = threadIdx.x; j < nv; j += blockDim.x) {
-      const double v = P[j * ld + nv];
+      const double v = Q[j * ld + nv];
       X[row * nv + j] = v;
       xs[j] = v;
     }
@@ -233,13 +230,13 @@ __device__ void solve_system(const double* __restrict__ Lm,
     for (int j = threadIdx.x; j < nv; j += blockDim.x) {
       double v = w[nv * nv + j];
       for (int k = 0; k < nv; ++k) v = fma(-__ldg(Ui + j * nv + k), xs[k], v);
-      R[j * ld + nv] = v;
+      Q[j * ld + nv] = v;  // column nv: disjoint from xs
       piv[j] = (int)w[nv * nv + nv + j];
     }
     __syncthreads();
-    lu_solve(A, R, ld, nv, 1, nv, piv);
+    lu_solve(A, Q, ld, nv, 1, nv, piv);
     for (int j = threadIdx.x; j < nv; j += blockDim.x) {
-      const double v = R[j * ld + nv];
+      const double v = Q[j * ld + nv];
       X[row * nv + j] = v;
       xs[j] = v;
     }
@@ -499,7 +496,7 @@ PYRO_EXPORT int64_t pyro_block_thomas_work_doubles(int nv, int64_t rows) {
 
 // Shared memory of one CTA for block size nv.
 PYRO_EXPORT int64_t pyro_block_thomas_smem_bytes(int nv) {
-  return (int64_t)3 * nv * (nv + 1) * 8 + (int64_t)nv * 4;
+  return (int64_t)2 * nv * (nv + 1) * 8 + (int64_t)nv * 4;
 }
 
 // Solve nsys block-tridiagonal systems (packed as described above).
