@@ -36,9 +36,9 @@ if ROOT not in sys.path:
 
 N_STATES = 4_194_304
 # DRAM bytes per state of k_fused_step_u measured by ncu on 262,144 states
-# of this workload (read 119,283,968 B + write 111,984,128 B); the traffic
+# of this workload (read 119,270,656 B + write 111,297,280 B); the traffic
 # grows with the states processed (one pass, no re-reads)
-NCU_DRAM_BYTES_PER_STATE = (119_283_968 + 111_984_128) / 262_144
+NCU_DRAM_BYTES_PER_STATE = (119_270_656 + 111_297_280) / 262_144
 WORKLOAD = "synthetic53_325: density + net production rates + T(e) Newton"
 METRIC = ("FP64 states/s (density + net production rates + temperature "
           "Newton)")
@@ -520,9 +520,8 @@ def eos_adjoint_legs(dev):
         chi = torch.as_tensor(prof["chi"], device=dev)
         visc = torch.zeros_like(chi)
         rows, nv = int(np.sum(lengths)), sol.n_species + 1
-        z = torch.cat([torch.linspace(0.0, 1.0, int(n), dtype=torch.float64,
-                                      device=dev) for n in lengths])
-        pdf = 1e-3 + z ** 1.5 * (1.0 - z) ** 2.5
+        z = np.concatenate([np.linspace(0.0, 1.0, int(n)) for n in lengths])
+        pdf = torch.as_tensor(1e-3 + z ** 1.5 * (1.0 - z) ** 2.5, device=dev)
         # one factorising solve vs a two-right-hand-side re-solve
         L, C, U = eq.adjoint_operator(h, Y, chi, visc, T0, 1e5)
         bt = eq._eos_solver(None)
@@ -766,7 +765,7 @@ def run_gb300(args):
             "traffic": NCU_DRAM_BYTES_PER_STATE * n,
             "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum "
                               "of one ncu capture of k_fused_step_u on "
-                              "262,144 states (231.3 MB = 882.2 B/state), "
+                              "262,144 states (230.6 MB = 879.7 B/state), "
                               "scaled to this launch's states",
             "peak_source": "DFMA throughput measured live by bench.py "
                            "(MEASURED_PEAKS.json has no FP64 figure)",

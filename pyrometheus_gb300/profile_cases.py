@@ -2,7 +2,7 @@
 
     python -m pyrometheus_gb300.profile_cases jacobian [states]
     python -m pyrometheus_gb300.profile_cases vjp [states]
-    python -m pyrometheus_gb300.profile_cases block_thomas [nv] [systems]
+    python -m pyrometheus_gb300.profile_cases block_thomas [nv] [systems] [n_min] [n_max]
     python -m pyrometheus_gb300.profile_cases batched_lu [nv] [cells]
     python -m pyrometheus_gb300.profile_cases transport [states]
 
@@ -53,12 +53,14 @@ def jacobian(states: int = 1 << 15, vjp: bool = False):
     torch.cuda.synchronize()
 
 
-def block_thomas(nv: int = 10, systems: int = 304):
+def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
+                 n_max: int = 1024):
     import torch
 
     from .flamelet import BlockThomasSolver
     dev = _dev()
-    lengths = np.random.default_rng(0).integers(64, 1025, size=systems)
+    lengths = np.random.default_rng(0).integers(n_min, n_max + 1,
+                                                size=systems)
     rows = int(lengths.sum())
     g = torch.Generator(device=dev).manual_seed(nv)
     f64 = dict(dtype=torch.float64, device=dev)
