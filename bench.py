@@ -299,6 +299,144 @@ def _event_ms(fn, reps):
     return e0.elapsed_time(e1) / reps
 
 
+def _cpu_timed(fn):
+    """Seconds of one call of *fn* (host only)."""
+    t0 = time.perf_counter()
+    fn()
+    return time.perf_counter() - t0
+
+
+def _blas_threads():
+    """Threads the host BLAS/LAPACK uses (threadpoolctl when installed)."""
+    try:
+        from threadpoolctl import threadpool_info
+        return max((int(i.get("num_threads", 1)) for i in threadpool_info()
+                    if i.get("user_api") == "blas"), default=1)
+    except ImportError:
+        return os.cpu_count() or 1
+
+
+def jacobian_cpu_baseline(sol, t, p, y, m=256):
+    """The oracle's central-difference reactor Jacobian (2 (S+1) source
+    evaluations per state; the reference differentiates its generated class
+    with JAX jacfwd) on *m* states of the leg's workload, one core; the VJP
+    baseline is J^T v with that Jacobian."""
+    import numpy as np
+
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    o = Oracle(sol)
+    rng = np.random.default_rng(3)
+    v = rng.standard_normal((sol.n_species + 1, m))
+    holder = {}
+
+    def jac():
+        holder["j"] = o.reactor_jacobian_fd(p[:m], t[:m], y[:, :m])
+
+    dt = _cpu_timed(jac)
+    dv = _cpu_timed(lambda: np.einsum("nij,in->nj", holder["j"], v))
+    sample = (f"{m} states of the workload (oracle numpy restatement, "
+              "central differences)")
+    return ({"value": m / dt, "unit": "states/s", "cores": 1, "kind": "port",
+             "sample": sample},
+            {"value": m / (dt + dv), "unit": "states/s", "cores": 1,
+             "kind": "port", "sample": sample + ", J^T v"})
+
+
+def block_thomas_cpu_baseline(nv, lengths, k=6):
+    """The oracle's numpy block-Thomas (np.linalg.solve per block, the
+    reference's recurrence) on the first *k* systems of the leg's lengths,
+    scaled to systems/s; BLAS threads as numpy runs them."""
+    import numpy as np
+
+    from oracle.block_thomas_oracle import block_thomas
+    rng = np.random.default_rng(nv)
+    sel = [int(n) for n in lengths[:k]]
+    systems = []
+    for n in sel:
+        c = rng.standard_normal((n, nv, nv)) + 10.0 * np.eye(nv)
+        lo = rng.standard_normal((n - 1, nv, nv))
+        up = rng.standard_normal((n - 1, nv, nv))
+        b = rng.standard_normal((n, nv))
+        systems.append((lo, c, up, b))
+    dt = _cpu_timed(lambda: [block_thomas(*sy) for sy in systems])
+    rows = sum(sel)
+    mean_rows = float(np.mean(lengths))
+    return {"value": rows / mean_rows / dt, "unit": "solves/s",
+            "cores": _blas_threads(), "kind": "port",
+            "sample": f"{k} systems ({rows} rows) of the leg's lengths, "
+                      "numpy block_thomas, scaled to the mean length"}
+
+
+def _cpu_flamelet(sol, prof, h, lengths):
+    """(oracle, slice data) of the flamelet whose length is nearest the
+    mean, for the CPU baselines of the flamelet legs."""
+    import numpy as np
+
+    from oracle.flamelet_oracle import FlameletOracle
+    i = int(np.argmin(np.abs(lengths - lengths.mean())))
+    offs = np.concatenate([[0], np.cumsum(lengths)])
+    sl = slice(int(offs[i]), int(offs[i + 1]))
+    d = {"h": np.asarray(h[sl].cpu(), dtype=np.float64),
+         "Y": np.asarray(prof["Y"][:, sl]), "T": np.asarray(prof["T"][sl]),
+         "chi": np.asarray(prof["chi"][sl]),
+         "dx": float(np.broadcast_to(prof["dx"], (len(lengths),))[i]),
+         "n": int(lengths[i])}
+    return FlameletOracle(sol), d
+
+
+def flamelet_cpu_baseline(sol, prof, h, lengths):
+    """One flamelet Newton step (enthalpy Newton, residual, central-
+    difference source Jacobian, blocks, numpy block_thomas) of a flamelet
+    of about the mean length, on the oracle; flamelet steps/s."""
+    import numpy as np
+
+    from oracle.block_thomas_oracle import block_thomas
+    fo, d = _cpu_flamelet(sol, prof, h, lengths)
+    visc = np.zeros(d["n"])
+
+    def step():
+        r = fo.residual(d["h"], d["Y"], d["chi"], visc, d["T"], 1e5,
+                        d["h"][0], d["h"][-1], d["Y"][:, 0], d["Y"][:, -1],
+                        d["dx"])
+        sj = fo.source_jacobian_fd(d["h"], d["Y"], visc, d["T"], 1e5)
+        lo, c, up = fo.blocks(sj, d["chi"], d["dx"])
+        block_thomas(lo, c, up, -r.T)
+
+    dt = _cpu_timed(step)
+    return {"value": 1.0 / dt, "unit": "flamelet Newton steps/s",
+            "cores": _blas_threads(), "kind": "port",
+            "sample": f"one {d['n']}-point flamelet of the workload (oracle "
+                      "numpy restatement, central-difference source "
+                      "Jacobian)"}
+
+
+def eos_cpu_baseline(sol, prof, h, lengths, pdf):
+    """``eos_gradient`` of a flamelet of about the mean length on the
+    oracle (central-difference source Jacobian, R T gradient and dS/dp;
+    numpy block_thomas); flamelet gradients/s."""
+    import numpy as np
+
+    fo, d = _cpu_flamelet(sol, prof, h, lengths)
+    visc = np.zeros(d["n"])
+    offs = np.concatenate([[0], np.cumsum(lengths)])
+    i = int(np.argmin(np.abs(lengths - lengths.mean())))
+    w = np.asarray(pdf[int(offs[i]):int(offs[i + 1])].cpu())
+
+    def grad():
+        sj = fo.source_jacobian_fd(d["h"], d["Y"], visc, d["T"], 1e5)
+        rt = fo.eos_rt(d["h"], d["Y"], d["T"])
+        rtj = fo.eos_rt_jacobian_fd(d["h"], d["Y"], d["T"])
+        dsdp = fo.source_pressure_gradient_fd(d["h"], d["Y"], visc, d["T"],
+                                              1e5)
+        fo.eos_gradient(sj, rt, rtj, dsdp, d["chi"], d["dx"], w, 1e5)
+
+    dt = _cpu_timed(grad)
+    return {"value": 1.0 / dt, "unit": "flamelet gradients/s",
+            "cores": _blas_threads(), "kind": "port",
+            "sample": f"one {d['n']}-point flamelet of the workload (oracle "
+                      "numpy restatement, central differences)"}
+
+
 def secondary_legs(sol, th, dev, dfma):
     """The other rows of the workload set, each measured with CUDA events on
     device-resident seeded inputs: the 54x54 reactor Jacobian and the VJP
@@ -329,6 +467,8 @@ def secondary_legs(sol, th, dev, dfma):
         "output_gbs": n * nc * nc * 8 / ms_j / 1e6}
     out["vjp"] = {"states": n, "ms": ms_v, "states_per_s": n / ms_v * 1e3,
                   "cotangents": "N(0,1), seeded"}
+    out["jacobian"]["cpu_baseline"], out["vjp"]["cpu_baseline"] = \
+        jacobian_cpu_baseline(sol, t, p, y)
     del V
     out["transport"] = transport_leg(sol, th, dev, dfma, t, p, y, T, P, Y)
     del T, P, Y
@@ -362,7 +502,9 @@ def secondary_legs(sol, th, dev, dfma):
             "hbm_gbs": rows * (5 * nv * nv + 4 * nv) * 8 / ms / 1e6,
             "kernel": solver.kernel, "threads": solver.threads,
             "cuda_graph": True, "autotune_ms": tuning,
-            "autotune_systems": len(tune_lengths)}
+            "autotune_systems": len(tune_lengths),
+            "cpu_baseline": block_thomas_cpu_baseline(
+                nv, lengths, 6 if nv == 10 else 2)}
         del C, L, U, b, solver
         torch.cuda.empty_cache()
     out["block_thomas"] = bt
@@ -485,7 +627,8 @@ def flamelet_newton_legs(dev, dfma):
             "solve_fp64_frac": flops / ms_s / 1e9 / (dfma / 1e12),
             "residual_inf_before": float(R0.abs().max()),
             "residual_inf_after": r_after,
-            "block_thomas": f"{solver.kernel}:{solver.threads}"}
+            "block_thomas": f"{solver.kernel}:{solver.threads}",
+            "cpu_baseline": flamelet_cpu_baseline(sol, prof, h, lengths)}
         del blocks, solver, x, b, eq, th, Y, h, R0
         torch.cuda.empty_cache()
     return res
@@ -545,7 +688,8 @@ def eos_adjoint_legs(dev):
             "resolve_2rhs_ms": ms_resolve,
             "finite_gradients": int(torch.isfinite(dens).all()
                                     & torch.isfinite(ener).all()),
-            "pdf": "1e-3 + Z^1.5 (1 - Z)^2.5 per flamelet"}
+            "pdf": "1e-3 + Z^1.5 (1 - Z)^2.5 per flamelet",
+            "cpu_baseline": eos_cpu_baseline(sol, prof, h, lengths, pdf)}
         del eq, th, Y, h, T0, chi, visc, z, pdf, dens, ener
         torch.cuda.empty_cache()
     return res
