@@ -209,6 +209,15 @@ int pyro_flamelet_blocks(const double* p, int64_t p_inc, const double* T,
                          double* L, double* C, double* U, int64_t rows,
                          cudaStream_t stream);
 
+/* dF/dp [S+1][ldf] of the reactor source at fixed (T, Y), in forward mode
+ * (the concentrations and [M] scale with p): the pressure derivative the
+ * reference takes with jacfwd, FlameletEquations.source_gradient_wrt_pressure,
+ * pyrometheus/flamelets/equations.py:130-134. */
+int pyro_reactor_source_dp(const double* p, int64_t p_inc, const double* T,
+                           int64_t t_inc, const double* Y, int64_t ldy,
+                           double* F, int64_t ldf, int64_t n,
+                           cudaStream_t stream);
+
 /* Adjoint operator of the compressible-EOS consistency solves,
  * FlameletEquations.adjoint_operator, equations.py:451-516 (used by
  * CompressibleEOS.enthalpy_gradient / eos_gradient,

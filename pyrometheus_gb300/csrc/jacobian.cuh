@@ -660,6 +660,83 @@ __global__ void __launch_bounds__(BLOCK)
   }
 }
 
+// df/dp at fixed (T, Y), F [S+1][ldf], for f = (dT/dt, W w / rho): the
+// concentrations and [M] scale with p (rho = p / (R T sigma)), so
+// dq/d ln p = rf (n_f + m) - rr (n_r + m) per reaction, n_f / n_r the sums
+// of its forward orders / product coefficients and m = d ln kf / d ln [M]
+// (the homogeneity of mass-action rates), then
+//   d(W_k w_k / rho)/dp = (W_k / rho) (dw_k / d ln p - w_k) / p,
+//   d(dT/dt)/dp = -(sum_k H_k dw_k / d ln p) / (rho cp p) - (dT/dt) / p.
+// The forward-mode pressure derivative the reference takes with jacfwd
+// (FlameletEquations.source_gradient_wrt_pressure, equations.py:130-134).
+__global__ void __launch_bounds__(BLOCK)
+    k_reactor_source_dp(const double* __restrict__ Pp, int64_t p_inc,
+                        const double* __restrict__ Tp, int64_t t_inc,
+                        const double* __restrict__ Y, int64_t ldy,
+                        double* __restrict__ F, int64_t ldf, int64_t n) {
+  extern __shared__ double smem[];
+  PEXP_PRELOAD();
+  const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
+                   w = pyro::col(smem, 2), dw = pyro::col(smem, 3);
+  PYRO_LOOP(i) {
+    const double T = pyro_ld(Tp, t_inc, i);
+    const double lnT = log(T), invT = 1.0 / T;
+    double sigma = 0.0, cpp = 0.0;
+    for (int k = 0; k < NS; ++k) {
+      const double wk = __ldg(Y + (int64_t)k * ldy + i) * k_inv_mw[k];
+      sigma += wk;
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      cpp = fma(wk,
+                fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]),
+                cpp);
+    }
+    const double P = pyro_ld(Pp, p_inc, i);
+    const double rho = P / (GAS_CONSTANT * T * sigma);
+    const pyro::StateScalars s = pyro::state_from_mass(T, rho, Y, ldy, i, c);
+    pyro::gibbs_all(s.T, s.lnT, s.invT, g);
+    for (int k = 0; k < NS; ++k) {
+      w[k] = 0.0;
+      dw[k] = 0.0;
+    }
+    for (int j = 0; j < NR; ++j) {
+      double kf, rf, rr, mlog;
+      pyro::reaction_rates(j, s.T, s.lnT, s.invT, s.c0, s.ctot, c, g, true,
+                           kf, rf, rr, &mlog);
+      const int fl = k_rx_flags[j];
+      const int nr = k_rx_nr[j], np = k_rx_np[j];
+      const bool frac = (fl & RX_FRACTIONAL) != 0;
+      const int fr = k_rx_frac[j];
+      double nf = 0.0, nb = 0.0;
+      for (int a = 0; a < MAXSIDE; ++a) {
+        if (a < nr)
+          nf += frac ? k_frac[fr][2 * MAXSIDE + a] : (double)k_rx_ord[j][a];
+        if (a < np)
+          nb += frac ? k_frac[fr][MAXSIDE + a]
+                     : (double)k_rx_nu[j][MAXSIDE + a];
+      }
+      pyro::scatter_net(j, rf - rr, w);
+      pyro::scatter_net(j, rf * (nf + mlog) - rr * (nb + mlog), dw);
+    }
+    double q = 0.0, dq = 0.0;
+    const double invP = 1.0 / P;
+    for (int k = 0; k < NS; ++k) {
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      const double hrt =
+          fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
+                            a[2] * (1.0 / 3.0)),
+                    a[1] * 0.5),
+              a[0]) +
+          a[5] * invT;
+      const double H = GAS_CONSTANT * T * hrt;
+      q = fma(H, w[k], q);
+      dq = fma(H, dw[k], dq);
+      F[(int64_t)(k + 1) * ldf + i] = k_mw[k] / rho * (dw[k] - w[k]) * invP;
+    }
+    const double rcp = rho * GAS_CONSTANT * cpp;
+    F[i] = (-dq / rcp + q / rcp) * invP;
+  }
+}
+
 // Vector-Jacobian product v^T df/dx for x = (T, Y) and df/dp, with v
 // [S+1][ldv]; outputs gT[n], gY[S][ldg], gp[n] (gp may be NULL).
 #ifndef VBLOCK

@@ -174,12 +174,15 @@ __device__ __forceinline__ double log_keq(int j, int f, double T, double c0,
 //       (python.py:399-473)
 //   rf = kf prod c^ord'  (orders paired positionally, chem_expr.py:436-446)
 //   rr = kf exp(log K) prod c^nu''  (0 when irreversible or !want_rev)
+// With dlnk_dlnm, also d ln kf / d ln [M] (0 elementary, 1 three-body,
+// 1/(1 + Pr) + d ln F / d ln Pr falloff; the reverse coefficient shares it).
 template <class CT>
 __device__ __forceinline__ void reaction_rates(int j, double T, double lnT,
                                                double invT, double c0,
                                                double ctot, CT c, CT g,
                                                bool want_rev, double& kf,
-                                               double& rf, double& rr) {
+                                               double& rf, double& rr,
+                                               double* dlnk_dlnm = nullptr) {
   const int f = k_rx_flags[j];
   const int kind = f & RX_KIND_MASK;
   const int form = (f >> RX_FORM_SHIFT) & 3;
@@ -204,7 +207,7 @@ __device__ __forceinline__ void reaction_rates(int j, double T, double lnT,
         arrhenius(k_fo_lowform[s], k_fo_low[s][0], k_fo_low[s][1],
                   k_fo_low[s][2], T, lnT, invT, xl);
     const double pr = m * k_lo / k_hi;
-    double blend = 1.0;
+    double blend = 1.0, dlnf = 0.0;
     if (f & RX_TROE) {
       // log10 Fcent, Troe broadening (chem_expr.py:348-420)
       double fsum = k_fo_troe[s][0] * PEXP(T * k_fo_troe[s][1]) +
@@ -214,16 +217,25 @@ __device__ __forceinline__ void reaction_rates(int j, double T, double lnT,
       double fac = -1.0 / 0.14;
       if (pr > 0.0) {
         const double xx = log10(pr) + (-0.4 - 0.67 * log_fc);
-        fac = xx / ((0.75 - 1.27 * log_fc) - 0.14 * xx);
+        const double den = 0.75 - 1.27 * log_fc;
+        const double dd = den - 0.14 * xx;
+        fac = xx / dd;
+        if (dlnk_dlnm) {
+          // d log10 F / d log10 Pr = -2 log10 Fcent f / (1 + f^2)^2 df/dxx
+          const double q = 1.0 + fac * fac;
+          dlnf = -2.0 * log_fc * fac / (q * q) * (den / (dd * dd));
+        }
       }
       blend = PEXP10(log_fc / (1.0 + fac * fac));
     }
     kf = k_hi * (blend * pr / (1.0 + pr));
+    if (dlnk_dlnm) *dlnk_dlnm = 1.0 / (1.0 + pr) + dlnf;
   } else {
     const double ek = arrhenius(form, k_rx_rate[j][0], k_rx_rate[j][1],
                                 k_rx_rate[j][2], T, lnT, invT, x);
     exp_form = form == FORM_EXP;
     kf = kind == RX_THREE_BODY ? ek * m : ek;
+    if (dlnk_dlnm) *dlnk_dlnm = kind == RX_THREE_BODY ? 1.0 : 0.0;
   }
   const int nr = k_rx_nr[j], np = k_rx_np[j];
   const bool frac = (f & RX_FRACTIONAL) != 0;

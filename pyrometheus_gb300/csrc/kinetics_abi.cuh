@@ -276,6 +276,23 @@ PYRO_EXPORT int pyro_reactor_source(const double* p, int64_t p_inc,
   return PYRO_OK;
 }
 
+PYRO_EXPORT int pyro_reactor_source_dp(const double* p, int64_t p_inc,
+                                       const double* T, int64_t t_inc,
+                                       const double* Y, int64_t ldy,
+                                       double* F, int64_t ldf, int64_t n,
+                                       cudaStream_t stream) {
+  if (n < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!p || !T || !Y || !F || ldy < n || ldf < n) return PYRO_ERR_ARGUMENT;
+  const size_t sm = smem_cols(4);
+  if (prepare_smem((const void*)k_reactor_source_dp, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  k_reactor_source_dp<<<grid_for(n), BLOCK, sm, stream>>>(
+      p, p_inc, T, t_inc, Y, ldy, F, ldf, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
 PYRO_EXPORT int pyro_reactor_jacobian(const double* p, int64_t p_inc,
                                       const double* T, int64_t t_inc,
                                       const double* Y, int64_t ldy, double* J,

@@ -476,6 +476,22 @@ class FlameletEquations:
             self._stream()), "flamelet eos rt")
         return rt, J
 
+    def source_gradient_wrt_pressure(self, h, Y, viscous_diss, temp_guess,
+                                     pressure, temperature=None):
+        """dS/dp per point, ``[rows, S+1]`` (``source_gradient_wrt_pressure``,
+        ``equations.py:130-134``): ``-S_h / p`` for the enthalpy source
+        ``v / rho`` and the reactor source's pressure derivative for the
+        species rows (T(h, Y) does not depend on p)."""
+        h, Y = self._state(h, Y)
+        T = temperature if temperature is not None else \
+            self.temperature(h, Y, temp_guess)
+        p, _ = self._pressure(pressure)
+        visc = self._rowvec(viscous_diss)
+        dfdp = self.th.get_reactor_source_dp(p, T, Y)
+        rho = self.th.get_density(p, T, Y)
+        dfdp[0] = -(visc / rho) / p
+        return dfdp.T
+
     def _sys_index(self):
         if getattr(self, "_sidx", None) is None:
             r0 = self.row_off[:-1]
@@ -545,8 +561,9 @@ class FlameletEquations:
         ``thermodynamic_consistency.py:173-307``): row 0 of a gradient is
         d/dp, row 1 d/dh at the boundaries.  The two adjoint solves share
         one factorisation (``BlockThomasSolver.resolve``); the pressure
-        sensitivity of the source enters through the reactor VJP, ``v^T
-        dS/dp = -v_h S_h / p + v_Y^T d(W w / rho)/dp``."""
+        sensitivity of the source is formed once in forward mode
+        (:meth:`source_gradient_wrt_pressure`) and contracted with both
+        adjoint states."""
         h, Y = self._state(h, Y)
         T = self.temperature(h, Y, temp_guess)
         p, _ = self._pressure(pressure)
@@ -566,14 +583,13 @@ class FlameletEquations:
         bt.resolve(L, U, B[1:], out=X[1:])
         bt.check_status()
         adj_d, adj_e = X[0].T, X[1].T
-        rho = self.th.get_density(p, T, Y)
-        s_h = visc / rho
+        # dS/dp once (forward mode), contracted with both adjoint states
+        dsdp = self.source_gradient_wrt_pressure(h, Y, visc, None, p,
+                                                 temperature=T).T
         half_chi = 0.5 * chi
         out = []
         for adj, base in ((adj_d, pdf / rt), (adj_e, None)):
-            cot = torch.cat([torch.zeros((1, self.rows), **f64), adj[1:]])
-            _, _, gp = self.th.get_reactor_vjp(p, T, Y, cot)
-            g = (-adj[0] * s_h / p + gp) / half_chi
+            g = (adj * dsdp).sum(dim=0) / half_chi
             integrand = g if base is None else base + g
             out.append(torch.stack([self._trapezoid(integrand),
                                     self._traces(adj[0])]))

@@ -68,6 +68,8 @@ _SIGNATURES = {
                             _P],
     "pyro_reactor_jacobian": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _I64,
                               _P],
+    "pyro_reactor_source_dp": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _I64,
+                               _P],
     "pyro_reactor_vjp": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P,
                          _I64, _P, _I64, _P],
     "pyro_reactor_bdf2": [_P, _P, _P, _I64] + [_P] * 17 + [_I64, _INT, _D,
@@ -681,6 +683,21 @@ class CudaThermochemistryBase:
         _check(self._lib.pyro_reactor_source(
             pv.ptr, pv.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
             out.data_ptr(), out.stride(0), n, self._stream), "reactor source")
+        return self._shape_rows(out, single and n == 1)
+
+    def get_reactor_source_dp(self, pressure, temperature, mass_fractions):
+        """``d[dT/dt, dY/dt]/dp`` ([S+1, N]) at fixed temperature and mass
+        fractions, in forward mode from the homogeneity of the mass-action
+        rates in the concentrations and [M] (the pressure derivative the
+        reference takes with ``jacfwd``,
+        ``flamelets/equations.py:130-134``)."""
+        pv, tv, ym, n, single = self._reactor_args(pressure, temperature,
+                                                   mass_fractions)
+        out = self._out(self.num_species + 1, n)
+        _check(self._lib.pyro_reactor_source_dp(
+            pv.ptr, pv.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
+            out.data_ptr(), out.stride(0), n, self._stream),
+            "reactor source pressure derivative")
         return self._shape_rows(out, single and n == 1)
 
     def get_reactor_jacobian(self, pressure, temperature, mass_fractions,

@@ -70,6 +70,38 @@ def test_adjoint_operator_and_rt(tag):
     assert np.all(np.abs(_np(rtj) - ref) <= 1e-11 * scale)
 
 
+@pytest.mark.parametrize("tag", TAGS)
+def test_source_gradient_wrt_pressure(tag):
+    """Forward-mode dS/dp (homogeneity of the rates in the concentrations
+    and [M]) against the golden forward-mode derivative through the
+    reference's generated class, per point at 1e-10 of its largest entry;
+    the reactor-level derivative against the VJP kernel's pressure
+    cotangent for unit cotangents."""
+    sol, g = eos_golden(tag)
+    n_x = g["h"].shape[0]
+    eq = _eqs(sol, [n_x], float(g["dx"]), g["y_ox"], g["y_fu"])
+    got = _np(eq.source_gradient_wrt_pressure(
+        g["h"], torch.as_tensor(g["Y"]), g["visc"], g["T_guess"],
+        float(g["P"])))
+    ref = g["ds_dp"]
+    scale = np.abs(ref).max(axis=1, keepdims=True)
+    assert np.all(np.abs(got - ref) <= 1e-10 * scale), \
+        float((np.abs(got - ref) / scale).max())
+    th = eq.th
+    T = eq.temperature(g["h"], torch.as_tensor(g["Y"]), g["T_guess"])
+    Y = torch.as_tensor(g["Y"], device="cuda")
+    p = float(g["P"])
+    dfdp = _np(th.get_reactor_source_dp(p, T, Y))
+    nv = dfdp.shape[0]
+    for k in range(nv):
+        cot = torch.zeros((nv, n_x), dtype=torch.float64, device="cuda")
+        cot[k] = 1.0
+        _, _, gp = th.get_reactor_vjp(p, T, Y, cot)
+        gp = _np(gp)
+        assert np.all(np.abs(dfdp[k] - gp) <= 1e-10 * np.abs(dfdp).max(
+            axis=0) + 1e-300), k
+
+
 @pytest.mark.parametrize("nv,kernel", [(10, "cta"), (10, "small"),
                                        (54, "cta")])
 def test_resolve_matches_fresh_solves(nv, kernel):
