@@ -44,6 +44,11 @@ enum PyroStatus {
 int pyro_mechanism_info(int* n_species, int* n_reactions, int* n_falloff,
                         int* block_size, int* table_bytes);
 
+/* Threads per block of the hot kernels (pyro_fused_step,
+ * pyro_net_production_rates): one block per SM runs at a time, so batches
+ * of a multiple of (SM count x this) states fill whole waves. */
+int pyro_hot_block_size(void);
+
 /* Species NASA-7 properties at T, out[S][ldo]; which:
  *   0 cp/R          get_species_specific_heats_r            python.py:334
  *   1 h/RT          get_species_enthalpies_rt               python.py:341

@@ -113,6 +113,10 @@ int prepare_smem(const void* fn, size_t bytes) {
 
 }  // namespace
 
+// Threads per block of the straight-line hot kernels (the fused step and
+// the net production rates), for callers that size batches in whole waves.
+PYRO_EXPORT int pyro_hot_block_size(void) { return HOT_BLOCK; }
+
 PYRO_EXPORT int pyro_mechanism_info(int* n_species, int* n_reactions,
                                     int* n_falloff, int* block_size,
                                     int* table_bytes) {

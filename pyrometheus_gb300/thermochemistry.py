@@ -50,6 +50,7 @@ _INT = ctypes.c_int
 _D = ctypes.c_double
 
 _SIGNATURES = {
+    "pyro_hot_block_size": [],
     "pyro_mechanism_info": [_P, _P, _P, _P, _P],
     "pyro_species_property": [_INT, _P, _I64, _P, _I64, _I64, _P],
     "pyro_mixture_property": [_INT, _P, _I64, _P, _I64, _P, _I64, _P, _I64,
@@ -462,7 +463,7 @@ class CudaThermochemistryBase:
 
     def get_net_production_rates_and_temperature(
             self, pressure, temperature, mass_fractions, energy, t_guess,
-            do_energy=True, check=True, out=None, chunk=1 << 18):
+            do_energy=True, check=True, out=None, chunk=None):
         """One pass per state of ``rho = get_density(p, T, Y)``,
         ``get_net_production_rates(rho, T, Y)`` and
         ``get_temperature(energy, t_guess, Y, do_energy)``.
@@ -470,7 +471,8 @@ class CudaThermochemistryBase:
         With host (CPU, preferably pinned) torch tensors for ``pressure``,
         ``temperature``, ``energy`` ([N]) and ``mass_fractions`` ([S, N]) and
         ``out = (wdot_host[S, N], T_host[N])``, the batch is streamed in
-        chunks of *chunk* states: host-to-device copies, the kernel and
+        chunks of *chunk* states (default: the whole waves of the hot kernel
+        nearest 2^18 states): host-to-device copies, the kernel and
         device-to-host copies of successive chunks run on three streams
         with double-buffered device chunks, so the transfers overlap the
         FP64 work.  Results land in *out*.
@@ -531,6 +533,10 @@ class CudaThermochemistryBase:
             self._copy_streams = (torch.cuda.Stream(dev),
                                   torch.cuda.Stream(dev))
         h2d, d2h = self._copy_streams
+        if chunk is None:
+            wave = self._lib.pyro_hot_block_size() * torch.cuda.\
+                get_device_properties(dev).multi_processor_count
+            chunk = max(1, round((1 << 18) / wave)) * wave
         m0 = int(min(chunk, n))
         f64 = dict(dtype=torch.float64, device=dev)
         bufs = []
