@@ -36,9 +36,10 @@ if ROOT not in sys.path:
 
 N_STATES = 4_194_304
 # DRAM bytes per state of k_fused_step_u measured by ncu on 262,144 states
-# of this workload (read 119,270,656 B + write 111,297,280 B); the traffic
-# grows with the states processed (one pass, no re-reads)
-NCU_DRAM_BYTES_PER_STATE = (119_270_656 + 111_297_280) / 262_144
+# of this workload (read 120,921,600 B + write 136,243,456 B: the 880 B of
+# inputs and outputs plus register-spill traffic); the traffic grows with
+# the states processed (one pass over the inputs)
+NCU_DRAM_BYTES_PER_STATE = (120_921_600 + 136_243_456) / 262_144
 WORKLOAD = "synthetic53_325: density + net production rates + T(e) Newton"
 METRIC = ("FP64 states/s (density + net production rates + temperature "
           "Newton)")
@@ -909,7 +910,7 @@ def run_gb300(args):
             "traffic": NCU_DRAM_BYTES_PER_STATE * n,
             "traffic_source": "dram__bytes_read.sum + dram__bytes_write.sum "
                               "of one ncu capture of k_fused_step_u on "
-                              "262,144 states (230.6 MB = 879.7 B/state), "
+                              "262,144 states (257.2 MB = 981.0 B/state), "
                               "scaled to this launch's states",
             "peak_source": "DFMA throughput measured live by bench.py "
                            "(MEASURED_PEAKS.json has no FP64 figure)",
