@@ -687,8 +687,16 @@ class _Emitter:
         L.extend(self._jacobian_tables(perm, flags, rates, dnu, defeff,
                                        tb_start, tb_idx, tb_de, fo_slot,
                                        fo_form, fo_low, fo_troe))
-        vblock = max(32, min(128, (100 * 1024 // (5 * S * 8)) // 32 * 32))
+        # VJP: five per-thread columns; as many threads per CTA as fit
+        # beside the exp table (one CTA per SM at 53 species: 96 threads,
+        # three warps, where 32-thread CTAs left two warps per SM)
+        vblock = max(32, min(128, ((227 * 1024 - 17408) // (5 * S * 8))
+                             // 32 * 32))
         w(f"#define VBLOCK {vblock}")
+        # pressure derivative of the source: four per-thread columns
+        dpblock = max(32, min(128, ((227 * 1024 - 17408) // (4 * S * 8))
+                              // 32 * 32))
+        w(f"#define DPBLOCK {dpblock}")
         w("")
         w('#include "kinetics.cuh"')
         w('#include "jacobian.cuh"')

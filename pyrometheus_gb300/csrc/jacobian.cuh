@@ -669,16 +669,23 @@ __global__ void __launch_bounds__(BLOCK)
 //   d(dT/dt)/dp = -(sum_k H_k dw_k / d ln p) / (rho cp p) - (dT/dt) / p.
 // The forward-mode pressure derivative the reference takes with jacfwd
 // (FlameletEquations.source_gradient_wrt_pressure, equations.py:130-134).
-__global__ void __launch_bounds__(BLOCK)
+#ifndef DPBLOCK
+#define DPBLOCK 64
+#endif
+
+__global__ void __launch_bounds__(DPBLOCK)
     k_reactor_source_dp(const double* __restrict__ Pp, int64_t p_inc,
                         const double* __restrict__ Tp, int64_t t_inc,
                         const double* __restrict__ Y, int64_t ldy,
                         double* __restrict__ F, int64_t ldf, int64_t n) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
-  const pyro::Cols c = pyro::col(smem, 0), g = pyro::col(smem, 1),
-                   w = pyro::col(smem, 2), dw = pyro::col(smem, 3);
-  PYRO_LOOP(i) {
+  using DC = pyro::ColsT<DPBLOCK>;
+  double* col0 = smem + threadIdx.x;
+  const DC c{col0}, g{col0 + NS * DPBLOCK}, w{col0 + 2 * NS * DPBLOCK},
+      dw{col0 + 3 * NS * DPBLOCK};
+  for (int64_t i = (int64_t)blockIdx.x * DPBLOCK + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * DPBLOCK) {
     const double T = pyro_ld(Tp, t_inc, i);
     const double lnT = log(T), invT = 1.0 / T;
     double sigma = 0.0, cpp = 0.0;

@@ -288,11 +288,12 @@ PYRO_EXPORT int pyro_reactor_source_dp(const double* p, int64_t p_inc,
   if (n < 0) return PYRO_ERR_ARGUMENT;
   if (n == 0) return PYRO_OK;
   if (!p || !T || !Y || !F || ldy < n || ldf < n) return PYRO_ERR_ARGUMENT;
-  const size_t sm = smem_cols(4);
+  const size_t sm = (size_t)4 * NS * DPBLOCK * sizeof(double);
   if (prepare_smem((const void*)k_reactor_source_dp, sm) != PYRO_OK)
     return PYRO_ERR_LAUNCH;
-  k_reactor_source_dp<<<grid_for(n), BLOCK, sm, stream>>>(
-      p, p_inc, T, t_inc, Y, ldy, F, ldf, n);
+  k_reactor_source_dp<<<pyro_grid(n, DPBLOCK, pyro_sm_count() * 16),
+                        DPBLOCK, sm, stream>>>(p, p_inc, T, t_inc, Y, ldy, F,
+                                               ldf, n);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
