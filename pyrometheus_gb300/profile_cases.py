@@ -5,6 +5,7 @@
     python -m pyrometheus_gb300.profile_cases block_thomas [nv] [systems] [n_min] [n_max]
     python -m pyrometheus_gb300.profile_cases batched_lu [nv] [cells]
     python -m pyrometheus_gb300.profile_cases transport [states]
+    python -m pyrometheus_gb300.profile_cases serving [cells] [launches]
 
 Each case builds its inputs on the current CUDA device (inputs larger than
 the 129 MB L2 at the default sizes, a few GB at most), runs the kernel three
@@ -131,6 +132,32 @@ def transport(states: int = 1 << 18):
           f"({states / ms * 1e3:.4g} states/s)")
 
 
+def serving(cells: int = 1 << 16, launches: int = 3):
+    """The fused reactor integrator (``k_reactor_bdf2``): one request of
+    *cells* cells of the 9-species mechanism (T0 ~ U[900, 1800] K, H2/O2/N2
+    stoichiometric to lean, 1 ms), *launches* engine steps of up to 64 step
+    attempts per cell; prints the time per launch."""
+    import torch
+
+    from . import get_thermochem_class, synthetic
+    from .serving import CudaReactorBackend, ReactorPool, poisson_requests
+    dev = _dev()
+    sol = synthetic.config1_mechanism()
+    th = get_thermochem_class(sol)(device=dev)
+    pool = ReactorPool(CudaReactorBackend(th), cells)
+    req = poisson_requests(1e4, 1.0, {"s9": sol}, seed=3,
+                           cells=(cells, cells))[0]
+    pool.admit(req)
+    torch.cuda.synchronize()
+    import time
+    t0 = time.perf_counter()
+    for _ in range(launches):
+        pool.step()
+    torch.cuda.synchronize()
+    ms = (time.perf_counter() - t0) * 1e3 / launches
+    print(f"serving: {cells} cells, {ms:.3f} ms per engine step")
+
+
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     if not argv:
@@ -146,6 +173,8 @@ def main(argv=None):
         batched_lu(*rest)
     elif case == "transport":
         transport(*rest)
+    elif case == "serving":
+        serving(*rest)
     else:
         raise SystemExit(f"unknown case {case!r}")
     print("ok")
