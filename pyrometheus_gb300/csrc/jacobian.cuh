@@ -508,30 +508,6 @@ __global__ void __launch_bounds__(JWARPS * 32)
     for (int qq = lane; qq < NR; qq += 32)
       pyro::jac_reaction(qq, s, c, g, h, D, Dq, DdT, Hq, Qc);
     __syncwarp();
-    // dw/dc into the interior of this state's output block: elements
-    // without contributions are zeroed, the others summed by the lane that
-    // owns them (its run of the update list) and stored once
-    for (int it = 0; it < JZ_ITERS; ++it) {
-      const int off = __ldg(jz_off + it * 32 + lane);
-      if (off != 0xFFFF) Ji[off] = 0.0;
-    }
-    {
-      int cur = -1;
-      double acc = 0.0;
-      for (int it = 0; it < JU_ITERS; ++it) {
-        const int e = it * 32 + lane;
-        const int off = __ldg(ju_off + e);
-        const double cf = __ldg(ju_coef + e);
-        const double dv = D[__ldg(ju_src + e)];
-        if (off != cur) {
-          if (cur >= 0 && cur != 0xFFFF) Ji[cur] = acc;
-          cur = off;
-          acc = 0.0;
-        }
-        acc = fma(cf, dv, acc);
-      }
-      if (cur >= 0 && cur != 0xFFFF) Ji[cur] = acc;
-    }
     // per species k: w_k, dw_k/dT|c, the rank-1 third-body vector a_k,
     // u_k = sum_m dw_k/dc_m c_m and the column sum
     // shj_k = RT sum_j h_j dw_j/dc_k, from per-reaction sums; then the
@@ -577,10 +553,42 @@ __global__ void __launch_bounds__(JWARPS * 32)
     const double rcp = rho * cpm;
     const double inv_rcp = 1.0 / rcp;
     const double qr2 = Q * inv_rcp * inv_rcp;
-    // the output-block writes above are by other lanes: make them visible
-    __threadfence_block();
     __syncwarp();
-#define Jc(k, m) Ji[(int64_t)((k) + 1) * NC + (m) + 1]
+    // rows 1..S, columns 1..S: d(dY_k/dt)/dY_m = W_k/rho ((Jc + a_k) rho
+    //   / W_m + (w_k - u_k) / (sigma W_m)) = (W_k Jc_km + B_k) / W_m with
+    // Jc = dw/dc.  Elements of dw/dc without contributions are B_k / W_m;
+    // the others are summed by the lane that owns them (its run of the
+    // update list) and stored once, transformed, with no read-back.
+    for (int it = 0; it < JZ_ITERS; ++it) {
+      const int off = __ldg(jz_off + it * 32 + lane);
+      if (off != 0xFFFF) {
+        const int k = off / NC - 1, m = off - (k + 1) * NC - 1;
+        Ji[off] = __ldg(jg_invmw + m) * sg[k];
+      }
+    }
+    {
+      int cur = -1;
+      double acc = 0.0;
+      for (int it = 0; it < JU_ITERS; ++it) {
+        const int e = it * 32 + lane;
+        const int off = __ldg(ju_off + e);
+        const double cf = __ldg(ju_coef + e);
+        const double dv = D[__ldg(ju_src + e)];
+        if (off != cur) {
+          if (cur >= 0 && cur != 0xFFFF) {
+            const int k = cur / NC - 1, m = cur - (k + 1) * NC - 1;
+            Ji[cur] = __ldg(jg_invmw + m) * fma(__ldg(jg_mw + k), acc, sg[k]);
+          }
+          cur = off;
+          acc = 0.0;
+        }
+        acc = fma(cf, dv, acc);
+      }
+      if (cur >= 0 && cur != 0xFFFF) {
+        const int k = cur / NC - 1, m = cur - (k + 1) * NC - 1;
+        Ji[cur] = __ldg(jg_invmw + m) * fma(__ldg(jg_mw + k), acc, sg[k]);
+      }
+    }
     // row 0: d(dT/dt)/dx
     for (int col = lane; col < NC; col += 32) {
       double v;
@@ -596,24 +604,8 @@ __global__ void __launch_bounds__(JWARPS * 32)
       }
       Ji[col] = v;
     }
-    // rows 1..S: d(dY_k/dt)/dx = W_k/rho ((Jc + a_k) rho / W_m
-    //                                     + (w_k - u_k) / (sigma W_m))
-    //          = (W_k Jc + B_k) / W_m
-    for (int k = 0; k < NS; ++k) {
-      const double A = __ldg(jg_mw + k);
-      const double Bk = sg[k];
-      for (int col = lane; col < NC; col += 32) {
-        double v;
-        if (col == 0) {
-          v = sjt[k];
-        } else {
-          const int jj = col - 1;
-          v = __ldg(jg_invmw + jj) * fma(A, Jc(k, jj), Bk);
-        }
-        Ji[(int64_t)(k + 1) * NC + col] = v;
-      }
-    }
-#undef Jc
+    // column 0 of rows 1..S
+    for (int k = lane; k < NS; k += 32) Ji[(int64_t)(k + 1) * NC] = sjt[k];
     __syncwarp();
   }
 }
