@@ -221,7 +221,8 @@ def _tuned():
 
 
 def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
-             n_max: int = 1024, candidates=(32, 64, 128, 256, 384, 512),
+             n_max: int = 1024,
+             candidates=(32, 64, 96, 128, 192, 256, 384, 512),
              seed: int = 0, device=None, repeats: int = 3, lengths=None):
     """Time the solve for each kernel and CTA size (the CTA kernel at each
     of *candidates*, and for nv <= 16 the one-thread-per-system kernel at 32
