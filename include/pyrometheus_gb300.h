@@ -168,16 +168,19 @@ int pyro_reactor_vjp(const double* p, int64_t p_inc, const double* T,
  * [ld] doubles; nsteps, nattempts, jage [ld] int64; active, failed, jstale,
  * done [ld] bytes; J, M [(S+1)^2][ld] doubles; piv [S+1][ld] ints.  Cells
  * with active == 0 are skipped; a cell that reaches t_end or fails gets
- * active = 0 and done = 1 (failed = 1 on failure).  Allocates nothing. */
+ * active = 0 and done = 1 (failed = 1 on failure).  With slots != NULL the
+ * call integrates the n cells slots[0..n) instead (the active cells of a
+ * fragmented pool, so no thread idles on a finished cell).  Allocates
+ * nothing. */
 int pyro_reactor_bdf2(double* y, double* y_prev, double* f_n, int64_t ld,
                       const double* p, double* t, const double* t_end,
                       double* h, double* h_prev, double* g_lu, double* crate,
                       int64_t* nsteps, int64_t* nattempts, int64_t* jage,
                       unsigned char* active, unsigned char* failed,
                       unsigned char* jstale, unsigned char* done, double* J,
-                      double* M, int* piv, int64_t n, int attempts,
-                      double rtol, double atol, int64_t max_attempts,
-                      cudaStream_t stream);
+                      double* M, int* piv, const int64_t* slots, int64_t n,
+                      int attempts, double rtol, double atol,
+                      int64_t max_attempts, cudaStream_t stream);
 
 /* Steady-flamelet residual, R[nv][ldr] = chi/2 Lap(phi) + S(phi) m - BC,
  * for flamelets packed along rows (system s owns rows [row_off[s],

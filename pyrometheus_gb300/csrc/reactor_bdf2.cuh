@@ -106,7 +106,9 @@ __device__ __forceinline__ void cell_rhs(double P, ICols X, ICols F, ICols c,
 
 }  // namespace pyro
 
-// Device-side BDF2 integration of cells [0, n) (inactive cells skipped).
+// Device-side BDF2 integration of cells [0, n), or of the n cells listed in
+// Slots (the pool's active cells, so every thread has a cell; inactive
+// cells are skipped either way).
 // done[i] is set when cell i finished (reached t_end or failed) in this
 // launch; failed[i] marks a failure.
 __global__ void __launch_bounds__(IBLOCK)
@@ -121,7 +123,8 @@ __global__ void __launch_bounds__(IBLOCK)
                    unsigned char* __restrict__ Failed,
                    unsigned char* __restrict__ Jstale,
                    unsigned char* __restrict__ Done, double* __restrict__ Jm,
-                   double* __restrict__ Mm, int* __restrict__ Piv, int64_t n,
+                   double* __restrict__ Mm, int* __restrict__ Piv,
+                   const int64_t* __restrict__ Slots, int64_t n,
                    int attempts, double rtol, double atol,
                    int64_t max_attempts) {
   extern __shared__ double smem[];
@@ -141,8 +144,9 @@ __global__ void __launch_bounds__(IBLOCK)
 #define EJ(r, q) Jm[((int64_t)(r) * INV + (q)) * ld + i]
 #define EM(r, q) Mm[((int64_t)(r) * INV + (q)) * ld + i]
 #define EP(r) Piv[(int64_t)(r) * ld + i]
-  for (int64_t i = (int64_t)blockIdx.x * IBLOCK + threadIdx.x; i < n;
-       i += (int64_t)gridDim.x * IBLOCK) {
+  for (int64_t q = (int64_t)blockIdx.x * IBLOCK + threadIdx.x; q < n;
+       q += (int64_t)gridDim.x * IBLOCK) {
+    const int64_t i = Slots ? Slots[q] : q;
     if (!Active[i]) continue;
     const double P = Pp[i], te = Te[i];
     double t = Tt[i], h = Hh[i], hp = Hp[i], glu = Glu[i], crate = Crate[i];
@@ -346,10 +350,11 @@ PYRO_EXPORT int pyro_reactor_bdf2(
     double* t, const double* t_end, double* h, double* h_prev, double* g_lu,
     double* crate, int64_t* nsteps, int64_t* nattempts, int64_t* jage,
     unsigned char* active, unsigned char* failed, unsigned char* jstale,
-    unsigned char* done, double* J, double* M, int* piv, int64_t n,
-    int attempts, double rtol, double atol, int64_t max_attempts,
-    cudaStream_t stream) {
-  if (n < 0 || ld < n || attempts < 1 || !(rtol > 0.0) || !(atol > 0.0))
+    unsigned char* done, double* J, double* M, int* piv,
+    const int64_t* slots, int64_t n, int attempts, double rtol, double atol,
+    int64_t max_attempts, cudaStream_t stream) {
+  if (n < 0 || (!slots && ld < n) || attempts < 1 || !(rtol > 0.0) ||
+      !(atol > 0.0))
     return PYRO_ERR_ARGUMENT;
   if (n == 0) return PYRO_OK;
   if (!y || !y_prev || !f_n || !p || !t || !t_end || !h || !h_prev ||
@@ -363,8 +368,8 @@ PYRO_EXPORT int pyro_reactor_bdf2(
   if (blocks > cap) blocks = cap;
   k_reactor_bdf2<<<(int)blocks, IBLOCK, BDF2_SMEM, stream>>>(
       y, y_prev, f_n, ld, p, t, t_end, h, h_prev, g_lu, crate, nsteps,
-      nattempts, jage, active, failed, jstale, done, J, M, piv, n, attempts,
-      rtol, atol, max_attempts);
+      nattempts, jage, active, failed, jstale, done, J, M, piv, slots, n,
+      attempts, rtol, atol, max_attempts);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }

@@ -139,9 +139,10 @@ class CudaReactorBackend:
             raise RuntimeError(f"per-cell norm failed ({st})")
         return out
 
-    def fused_step(self, pool, n: int, attempts: int):
-        """Up to *attempts* step attempts of cells [0, n) of *pool* inside
-        one launch of the mechanism library's ``pyro_reactor_bdf2``."""
+    def fused_step(self, pool, n: int, attempts: int, slots=None):
+        """Up to *attempts* step attempts of cells [0, n) of *pool* (or of
+        the *n* cells listed in the device int64 tensor *slots*) inside one
+        launch of the mechanism library's ``pyro_reactor_bdf2``."""
         ptr = lambda x: x.data_ptr()  # noqa: E731
         st = self.th._lib.pyro_reactor_bdf2(
             ptr(pool.y), ptr(pool.y_prev), ptr(pool.f_n), pool.cap,
@@ -149,7 +150,8 @@ class CudaReactorBackend:
             ptr(pool.h_prev), ptr(pool.g_lu), ptr(pool.crate),
             ptr(pool.nsteps), ptr(pool.nattempts), ptr(pool.jage),
             ptr(pool.active), ptr(pool.failed), ptr(pool.jstale),
-            ptr(pool.done), ptr(pool.J), ptr(pool.M), ptr(pool.piv), n,
+            ptr(pool.done), ptr(pool.J), ptr(pool.M), ptr(pool.piv),
+            ptr(slots) if slots is not None else None, n,
             int(attempts), pool.rtol, pool.atol, pool.max_attempts,
             self._stream())
         if st != 0:
@@ -238,6 +240,7 @@ class ReactorPool:
         self.slot_req = np.full(cap, -1, dtype=np.int64)
         self.n_active = 0
         self._done = None
+        self._slots = None      # device list of active cells (fused)
         self.engine_steps = 0
 
     @classmethod
@@ -294,6 +297,7 @@ class ReactorPool:
             self.jstale[idx] = True
             self.failed[idx] = False
             self.active[idx] = True
+        self._slots = None
         self.n_active += req.n
         return slots
 
@@ -340,8 +344,15 @@ class ReactorPool:
         self.engine_steps += 1
         if self.fused:
             with self._on_stream():
+                if self._slots is None:
+                    # the active cells of [0, n): rebuilt after admissions
+                    # and harvests, so a fragmented pool launches only
+                    # threads that have a cell
+                    self._slots = torch.nonzero(self.active[:n]).flatten()
                 self.done[:n].zero_()
-                be.fused_step(self, n, self.attempts)
+                if self._slots.numel():
+                    be.fused_step(self, int(self._slots.numel()),
+                                  self.attempts, slots=self._slots)
                 self._done = self.done[:n]
             return
         with self._on_stream():
@@ -468,6 +479,8 @@ class ReactorPool:
         self.synchronize()
         fin = np.nonzero(self._done.cpu().numpy())[0]
         self._done = None
+        if fin.size:
+            self._slots = None
         return fin
 
     def results(self, slots: np.ndarray):
@@ -483,6 +496,7 @@ class ReactorPool:
         with self._on_stream():
             self.active[torch.as_tensor(slots, device=self.device)] = False
         self.synchronize()
+        self._slots = None
 
     def reset(self):
         """Drop every cell (after a failed engine step)."""
@@ -495,6 +509,7 @@ class ReactorPool:
         self.n_active = 0
         self.high_water = 0
         self._done = None
+        self._slots = None
 
 
 class ReactorServer:

@@ -73,7 +73,7 @@ _SIGNATURES = {
                                _P],
     "pyro_reactor_vjp": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P,
                          _I64, _P, _I64, _P],
-    "pyro_reactor_bdf2": [_P, _P, _P, _I64] + [_P] * 17 + [_I64, _INT, _D,
+    "pyro_reactor_bdf2": [_P, _P, _P, _I64] + [_P] * 18 + [_I64, _INT, _D,
                                                           _D, _I64, _P],
     "pyro_flamelet_blocks": [_P, _I64, _P, _P, _I64, _P, _P, _P, _P, _P, _P,
                              _P, _P, _I64, _P],
