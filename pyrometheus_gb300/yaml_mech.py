@@ -423,8 +423,18 @@ def _species(entry: Dict[str, Any]) -> Species:
 
 
 def load_mechanism(source: str, phase: Optional[str] = None,
-                   text: Optional[str] = None) -> Solution:
-    """Load a Cantera-YAML mechanism (``ct.Solution(source, phase)``)."""
+                   text: Optional[str] = None,
+                   transport: Optional[str] = None) -> Solution:
+    """Load a Cantera-YAML mechanism (``ct.Solution(source, phase)``).
+
+    ``transport="kinetic-theory"`` attaches mixture-averaged transport fits
+    made from the species' Lennard-Jones ``diameter`` and ``well-depth``
+    by first-order Chapman-Enskog theory
+    (:func:`pyrometheus_gb300.transport_fits.kinetic_theory_fits`).  These
+    approximate Cantera's fits, which add polar and rotational corrections
+    and tabulated collision integrals; with Cantera installed, pass its
+    ``Solution`` to the code generator instead.  By default no fits are
+    attached."""
     if text is None:
         with open(source) as f:
             text = f.read()
@@ -452,8 +462,23 @@ def load_mechanism(source: str, phase: Optional[str] = None,
         r = _reaction(e, units, names)
         if all(k in names for k in list(r.reactants) + list(r.products)):
             reactions.append(r)
-    return Solution(species, reactions, elements, source=str(source),
-                    name=(ph or {}).get("name", "gas"))
+    sol = Solution(species, reactions, elements, source=str(source),
+                   name=(ph or {}).get("name", "gas"))
+    if transport is not None:
+        if transport != "kinetic-theory":
+            raise ValueError(f"unknown transport fits '{transport}'")
+        from .transport_fits import kinetic_theory_fits
+        sigma, eps = [], []
+        for n in names:
+            tr = all_species[n].get("transport")
+            if not tr or "diameter" not in tr or "well-depth" not in tr:
+                raise ValueError(f"species '{n}' has no Lennard-Jones "
+                                 "transport data")
+            sigma.append(float(tr["diameter"]))
+            eps.append(float(tr["well-depth"]))
+        sol.transport = kinetic_theory_fits(sol, sigma=sigma,
+                                            well_depth=eps)
+    return sol
 
 
 # }}}

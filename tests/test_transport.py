@@ -139,3 +139,33 @@ def test_generated_transport_tables():
     src = CudaCodeGenerator.generate("s9", sol)
     assert "#define PYRO_TR_SYM 0" in src
     assert f"k_tr_diff[{S * S * 5}]" in src
+
+
+def test_yaml_lennard_jones_fits():
+    """Kinetic-theory fits from a YAML mechanism's species transport data
+    (diameter, well-depth); none unless requested; a species without the
+    data is an error."""
+    text = dump_mechanism(synthetic.config1_mechanism())
+    sol = load_mechanism("m.yaml", text=text)
+    assert sol.transport is None
+    lines, out, in_species = text.splitlines(), [], False
+    for ln in lines:
+        out.append(ln)
+        if not ln.startswith((" ", "-")):
+            in_species = ln.startswith("species:")
+        if in_species and ln.startswith("- name: "):
+            out += ["  transport:", "    model: gas",
+                    "    geometry: linear", "    diameter: 3.0",
+                    "    well-depth: 100.0"]
+    lj = "\n".join(out) + "\n"
+    sol = load_mechanism("m.yaml", text=lj, transport="kinetic-theory")
+    S = sol.n_species
+    assert sol.transport.viscosity.shape == (S, 5)
+    assert sol.transport.symmetric
+    t = np.array([1000.0])
+    mu = Oracle(sol).get_species_viscosities(t)
+    assert np.all((mu > 1e-6) & (mu < 1e-3))
+    with pytest.raises(ValueError):
+        load_mechanism("m.yaml", text=text, transport="kinetic-theory")
+    with pytest.raises(ValueError):
+        load_mechanism("m.yaml", text=lj, transport="cantera")
