@@ -52,3 +52,37 @@ def test_oracle_matches_reference_generator(mech):
     e = o.get_mixture_internal_energy_mass(t, y)
     assert np.abs(o.get_temperature(e, 1500.0, y, True)
                   - ref.get_temperature(e, 1500.0, y, True)).max() < 1e-10
+
+
+@pytest.mark.parametrize("mech", ["sandiego", "gri30"])
+def test_oracle_transport_matches_reference_generator(mech):
+    """The reference's generated transport methods (python.py:564-641) on
+    its own fixture mechanisms, with kinetic-theory fits from their
+    Lennard-Jones data, against the oracle."""
+    path = os.path.join(refgen.REFERENCE_ROOT, "test", "mechs",
+                        f"{mech}.yaml")
+    sol = load_mechanism(path, transport="kinetic-theory")
+    ref = refgen.reference_class(sol)()
+    o = Oracle(sol)
+    n = 32
+    t, p, y = synthetic.sample_states(sol, n, seed=22, dilute="N2")
+
+    def dense(a):
+        a = np.asarray(a)
+        if a.dtype == object:
+            return np.array([dense(v) for v in a])
+        return a.astype(np.float64)
+
+    assert np.array_equal(o.get_species_viscosities(t),
+                          dense(ref.get_species_viscosities(t)))
+    assert np.array_equal(o.get_species_binary_mass_diffusivities(t[:4]),
+                          dense(ref.get_species_binary_mass_diffusivities(
+                              t[:4])))
+    assert rel_err(o.get_mixture_viscosity_mixavg(t, y),
+                   dense(ref.get_mixture_viscosity_mixavg(t, y))) < 1e-14
+    assert rel_err(o.get_mixture_thermal_conductivity_mixavg(t, y),
+                   dense(ref.get_mixture_thermal_conductivity_mixavg(
+                       t, y))) < 1e-14
+    assert rel_err(o.get_species_mass_diffusivities_mixavg(p, t, y),
+                   dense(ref.get_species_mass_diffusivities_mixavg(
+                       p, t, y))) < 1e-13
