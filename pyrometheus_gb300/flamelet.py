@@ -330,9 +330,23 @@ class FlameletEquations:
             np.repeat(np.arange(self.nsys, dtype=np.int32), lengths),
             device=dev)
         dx = np.broadcast_to(np.asarray(dx, dtype=np.float64), (self.nsys,))
+        self.dx = np.array(dx)
         self.inv_dx2 = torch.as_tensor(1.0 / dx ** 2, device=dev)
         self.y_ox = self._bc_mat(y_ox)
         self.y_fu = self._bc_mat(y_fu)
+
+    def subset(self, systems):
+        """The equations of the flamelets *systems* (indices into this
+        batch, in the order given), packed in that order."""
+        idx = np.asarray(systems, dtype=np.int64)
+        sel = torch.as_tensor(idx, device=self.device)
+        return FlameletEquations(self.th, self.lengths[idx], self.dx[idx],
+                                 self.y_ox[:, sel], self.y_fu[:, sel],
+                                 device=self.device)
+
+    def linear_solver(self):
+        """A :class:`BlockThomasSolver` for these flamelets' blocks."""
+        return BlockThomasSolver(self.nv, self.lengths, device=self.device)
 
     def _bc_mat(self, y):
         y = torch.as_tensor(np.asarray(y, dtype=np.float64)
@@ -379,11 +393,16 @@ class FlameletEquations:
     def _stream():
         return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 
-    def temperature(self, h, Y, temp_guess):
+    def temperature(self, h, Y, temp_guess, check=True):
         """T with h_mix(T, Y) = h (``equation_of_state``,
-        ``equations.py:320-338``)."""
-        return self.th.get_temperature_from_enthalpy(
-            h, Y, self._rowvec(temp_guess))
+        ``equations.py:320-338``).  ``check=False`` returns the last
+        iterate of states whose iteration did not converge (nan for nan
+        states) instead of raising."""
+        if check:
+            return self.th.get_temperature_from_enthalpy(
+                h, Y, self._rowvec(temp_guess))
+        return self.th._temperature(h, self._rowvec(temp_guess), Y, False,
+                                    1.0e-10, 500, check=False)
 
     def rhs(self, h, Y, diss_rate, viscous_diss, temp_guess, pressure,
             h_ox, h_fu, temperature=None):
