@@ -6,6 +6,7 @@
     python -m pyrometheus_gb300.profile_cases batched_lu [nv] [cells]
     python -m pyrometheus_gb300.profile_cases transport [states]
     python -m pyrometheus_gb300.profile_cases serving [cells] [launches]
+    python -m pyrometheus_gb300.profile_cases flamelet_solve [copies]
 
 Each case builds its inputs on the current CUDA device (inputs larger than
 the 129 MB L2 at the default sizes, a few GB at most), runs the kernel three
@@ -158,6 +159,58 @@ def serving(cells: int = 1 << 16, launches: int = 3):
     print(f"serving: {cells} cells, {ms:.3f} ms per engine step")
 
 
+def flamelet_solve(copies: int = 256):
+    """The flamelet solver driver (``FlameletSolver.solve`` with the time
+    march first, as the reference notebook runs it: 10 Crank-Nicolson steps
+    of 1e-5 s, then Newton to |v| < 1e-8) on *copies* copies of three
+    seeded flamelets (12, 12 and 9 points; peak dissipation 100, 10 and
+    1000 1/s) of the 9-species mechanism with every rate coefficient times
+    1e-12; prints the wall time and flamelets solved per second."""
+    import time
+
+    import torch
+
+    from . import get_thermochem_class, synthetic
+    from .flamelet_solver import FlameletSolver
+    dev = _dev()
+    sol = synthetic.scaled_rates(synthetic.config1_mechanism(), 1e-12)
+    th = get_thermochem_class(sol)(device=dev)
+    lengths, dxs, ys, ts, chis = [], [], [], [], []
+    for n, chi_max, seed in ((12, 100.0, 1), (12, 10.0, 1),
+                             (9, 1000.0, 5)):
+        prof = synthetic.flamelet_profiles(sol, [n], seed=seed,
+                                           chi_max=chi_max)
+        chi = prof["chi"].copy()
+        chi[0] = chi[-1] = 2.0 * prof["dx"][0] ** 2
+        lengths.append(n)
+        dxs.append(prof["dx"][0])
+        ys.append(prof["Y"])
+        ts.append(prof["T"])
+        chis.append(chi)
+    y_ox, y_fu = prof["y_ox"], prof["y_fu"]
+    lengths, dxs = lengths * copies, dxs * copies
+    Y = torch.as_tensor(np.hstack(ys * copies), device=dev)
+    T = torch.as_tensor(np.concatenate(ts * copies), device=dev)
+    chi = torch.as_tensor(np.concatenate(chis * copies), device=dev)
+    h = th.get_mixture_enthalpy_mass(T, Y)
+    offs = np.concatenate([[0], np.cumsum(lengths)])
+    h_ox, h_fu = h[offs[:-1]], h[offs[1:] - 1]
+    fs = FlameletSolver(th, lengths, dxs, (y_ox, y_fu))
+    args = (False, 20, 1e-8, 20, 1e-9, 1e-5, 10, False, 2, chi,
+            torch.zeros_like(chi), T, 101325.0, h_ox, h_fu, (h, Y))
+    fs.solve(*args)                         # plans, kernels, first touch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fs.solve(*args)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    stages = np.bincount(fs.last_solve["stage"] + 1, minlength=4)
+    print(f"flamelet_solve: {len(lengths)} flamelets ({offs[-1]} points) "
+          f"in {wall:.3f} s = {len(lengths) / wall:.1f} flamelets/s; "
+          f"flamelets per stage -1/0/1/2: "
+          f"{'/'.join(str(int(c)) for c in stages[:4])}")
+
+
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     if not argv:
@@ -175,6 +228,8 @@ def main(argv=None):
         transport(*rest)
     elif case == "serving":
         serving(*rest)
+    elif case == "flamelet_solve":
+        flamelet_solve(*rest)
     else:
         raise SystemExit(f"unknown case {case!r}")
     print("ok")
