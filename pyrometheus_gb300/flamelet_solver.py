@@ -85,10 +85,8 @@ class _Subset:
         else:
             self.eq = eq.subset(systems)
             lengths = eq.lengths[systems]
-            rows = np.concatenate([np.arange(parent.offs[s],
-                                             parent.offs[s + 1])
-                                   for s in systems])
-            self.rows = torch.as_tensor(rows, dtype=torch.int64, device=dev)
+            self.rows = torch.as_tensor(parent.rows_of(systems),
+                                        dtype=torch.int64, device=dev)
             self.sys = torch.as_tensor(systems, dtype=torch.int64,
                                        device=dev)
         n_rows = int(np.sum(lengths))
@@ -163,6 +161,16 @@ class FlameletSolver:
         self.offs = np.concatenate([[0], np.cumsum(eq.lengths)])
         self._subsets = {}
         self.last_solve = None
+
+    def subset(self, systems):
+        """A solver of the flamelets *systems* alone (indices into this
+        batch, packed in the order given)."""
+        return FlameletSolver.from_equations(self.eq.subset(systems))
+
+    def rows_of(self, systems):
+        """The rows of the flamelets *systems*, in that order."""
+        return np.concatenate([np.arange(self.offs[s], self.offs[s + 1])
+                               for s in np.asarray(systems, dtype=np.int64)])
 
     # {{{ inputs
 

@@ -151,3 +151,96 @@ class OracleEquations:
             L[r0:r0 + n - 1], C[r0:r0 + n], U[r0:r0 + n - 1] = lo, c, up
             r0 += n
         return torch.as_tensor(L), torch.as_tensor(C), torch.as_tensor(U)
+
+    # the compressible-EOS pieces, flamelet by flamelet
+
+    def _parts(self, h, Y, *rowvecs):
+        return zip(range(self.nsys), self._rows(h),
+                   split(Y.numpy(), self.lengths),
+                   *(self._rows(x) for x in rowvecs))
+
+    def eos_rt(self, h, Y, temp_guess=None, temperature=None,
+               jacobian=True):
+        assert not jacobian
+        rt = [self.fo.eos_rt(hs, ys, tg)
+              for _, hs, ys, tg in self._parts(h, Y, temp_guess)]
+        return torch.as_tensor(np.concatenate(rt)), None
+
+    def enthalpy_gradient(self, h, Y, diss_rate, viscous_diss, temp_guess,
+                          pressure, pdf):
+        rts, adjs, gs = [], [], []
+        for s, hs, ys, chi, visc, tg, p, w in self._parts(
+                h, Y, diss_rate, viscous_diss, temp_guess, pressure, pdf):
+            p = float(np.asarray(p).ravel()[0])
+            rts.append(self.fo.eos_rt(hs, ys, tg))
+            sj = self.fo.source_jacobian_fd(hs, ys, visc, tg, p)
+            adj, g = self.fo.enthalpy_gradient(sj, chi, self.dx[s], w)
+            adjs.append(adj)
+            gs.append(g)
+        return (torch.as_tensor(np.concatenate(rts)),
+                torch.as_tensor(np.hstack(adjs)), torch.as_tensor(gs))
+
+    def eos_gradient(self, h, Y, diss_rate, viscous_diss, temp_guess,
+                     pressure, pdf):
+        fo = self.fo
+        dgs, egs, ads, aes = [], [], [], []
+        for s, hs, ys, chi, visc, tg, p, w in self._parts(
+                h, Y, diss_rate, viscous_diss, temp_guess, pressure, pdf):
+            p = float(np.asarray(p).ravel()[0])
+            rt = fo.eos_rt(hs, ys, tg)
+            rtj = fo.eos_rt_jacobian_fd(hs, ys, tg)
+            dsdp = fo.source_pressure_gradient_fd(hs, ys, visc, tg, p)
+            sj = fo.source_jacobian_fd(hs, ys, visc, tg, p)
+            (dg, eg), (ad, ae) = fo.eos_gradient(sj, rt, rtj, dsdp, chi,
+                                                 self.dx[s], w, p)
+            dgs.append(dg)
+            egs.append(eg)
+            ads.append(ad)
+            aes.append(ae)
+        t = torch.as_tensor
+        return ((t(np.stack(dgs, axis=1)), t(np.stack(egs, axis=1))),
+                (t(np.hstack(ads)), t(np.hstack(aes))))
+
+
+# compressible-EOS consistency: two flamelets whose steady Newton converges,
+# targets from their solutions at (PRESSURE, h_ox, h_fu), iterations
+# started 10 % off in pressure
+EOS_FLAMELETS = [FLAMELETS[0], FLAMELETS[3]]
+
+
+def eos_config(method, maxiter=3, tol=1e-12):
+    return dict(verbosity=False,
+                newton=dict(maxiter=SOLVE["newton_maxiter"],
+                            tol=SOLVE["newton_tol"]),
+                bdf=dict(newton=dict(maxiter=SOLVE["bdf_newton_maxiter"],
+                                     tol=SOLVE["bdf_newton_tol"]),
+                         time_step=SOLVE["bdf_time_step"],
+                         maxsteps=SOLVE["bdf_maxsteps"]),
+                max_attempts=SOLVE["max_attempts"],
+                eos=dict(update_size=1.0, update_method=method,
+                         maxiter=maxiter, tol=tol))
+
+
+def eos_case(sol, b):
+    """Per-flamelet PDF weights [rows], true params [3, n], start params
+    [3, n] and the targets (density, energy) [n] of the true params (from
+    the oracle)."""
+    from oracle.eos_consistency_oracle import CompressibleEOSOracle
+    n = b["lengths"]
+    pdfs, rho, e = [], [], []
+    true = np.stack([np.full(len(n), PRESSURE), b["h_ox"], b["h_fu"]])
+    for s, (phi0, chi, visc, tg) in enumerate(zip(
+            split(b["phi"], n), split(b["chi"], n), split(b["visc"], n),
+            split(b["T"], n))):
+        z = np.linspace(0.0, 1.0, n[s])
+        pdf = 1e-3 + z ** 1.5 * (1.0 - z) ** 2.5
+        pdfs.append(pdf / pdf.sum())
+        orc = CompressibleEOSOracle(sol, b["dx"][s], b["y_ox"], b["y_fu"],
+                                    eos_config("gauss_newton"))
+        out = orc.evaluate_flamelet(true[:, s], pdfs[-1], chi, visc, tg,
+                                    phi0)
+        rho.append(out[2])
+        e.append(out[3])
+    start = true.copy()
+    start[0] *= 1.1
+    return np.concatenate(pdfs), true, start, np.array(rho), np.array(e)
