@@ -110,3 +110,23 @@ def test_no_attempts_returns_the_guess(case):
     np.testing.assert_array_equal(_phi(st), b["phi"])
     np.testing.assert_array_equal(temp.numpy(), b["T"])
     assert not fs.last_solve["converged"].any()
+
+
+def test_verbose_solve_reports_each_stage(capsys):
+    """The progress lines of ``solver.py`` (Newton iterations, time steps,
+    attempts, the summary) on one flamelet that needs a march."""
+    np.seterr(all="ignore")
+    sol = mechanism()
+    b = flamelet_batch(sol, [(9, 1000.0, 5, False)])
+    eq = OracleEquations(sol, b["lengths"], b["dx"], b["y_ox"], b["y_fu"])
+    fs = FlameletSolver.from_equations(eq)
+    kw = dict(SOLVE, try_newton=False, max_attempts=1, bdf_maxsteps=2)
+    fs.solve(True, *kw.values(), b["chi"], b["visc"], b["T"], PRESSURE,
+             b["h_ox"], b["h_fu"], b["phi"])
+    out = capsys.readouterr().out
+    assert "Attempt 0 of BDF time marching" in out
+    assert out.count("BDF time step") == 2
+    assert "Newton iter 0" in out
+    assert fs.last_solve["stage"][0] in (1, -1)
+    if fs.last_solve["stage"][0] == -1:
+        assert "did not converge" in out
