@@ -1,0 +1,239 @@
+"""Run the reference's flamelet solver driver and compressible-EOS loop in
+this container.
+
+TEST INFRASTRUCTURE ONLY -- used by CPU tests that are skipped when the
+reference checkout is absent.  Nothing in the product imports this module.
+
+``pyrometheus/flamelets/solver.py`` and ``thermodynamic_consistency.py``
+import JAX, which is not installed here.  Their control flow needs only a
+small part of it, supplied by a stand-in while the reference files are
+executed:
+
+* ``jax.numpy`` is numpy (``array`` returns an array that also answers
+  ``block_until_ready``); ``jax.jit`` returns the function unchanged;
+  ``jax.lax.while_loop`` and ``jax.lax.scan`` are Python loops (the scan
+  is :func:`oracle.refgen._scan`, which already runs the reference's
+  ``linear_solver.block_thomas``); ``jax.tree_util`` registration and
+  ``jax.config`` are no-ops;
+* the reference's ``state.py`` and ``make_pyro.py`` run unchanged;
+  ``_array_to_state`` is wrapped so the fields it builds answer
+  ``block_until_ready`` as JAX arrays do;
+* ``FlameletEquations`` (``equations.py``, ``jax.vmap``/``jax.jacfwd`` over
+  the generated class) is replaced by :class:`OracleGovEquations`, the
+  same methods over the :class:`~oracle.flamelet_oracle.FlameletOracle`
+  pieces for one flamelet.
+
+The reference's ``FlameletSolver`` and ``CompressibleEOS`` classes are then
+used unchanged (instances are made without their constructors, which build
+the JAX equations, and given the attributes the constructors would set).
+"""
+
+from __future__ import annotations
+
+import os
+import sys
+import types
+
+import numpy as np
+
+from .flamelet_oracle import FlameletOracle
+from .refgen import REFERENCE_ROOT, _scan, reference_available
+
+
+class _Ready(np.ndarray):
+    """A numpy array that also answers JAX's ``block_until_ready``."""
+
+    def block_until_ready(self):
+        return self
+
+
+def _ready(x):
+    return np.asarray(x).view(_Ready)
+
+
+def _while_loop(cond, body, carry):
+    while cond(carry):
+        carry = body(carry)
+    return carry
+
+
+def _jax_modules():
+    jnp = types.ModuleType("jax.numpy")
+    jnp.__dict__.update({k: getattr(np, k) for k in dir(np)
+                         if not k.startswith("__")})
+    jnp.array = lambda *a, **k: _ready(np.array(*a, **k))
+    lax = types.ModuleType("jax.lax")
+    lax.scan = _scan
+    lax.while_loop = _while_loop
+    tree_util = types.ModuleType("jax.tree_util")
+    tree_util.register_pytree_node_class = lambda cls: cls
+    jax = types.ModuleType("jax")
+    jax.numpy, jax.lax, jax.tree_util = jnp, lax, tree_util
+    jax.config = types.SimpleNamespace(update=lambda *a, **k: None)
+
+    def jit(fun=None, **kwargs):
+        return fun if fun is not None else (lambda f: f)
+    jax.jit = jit
+    return {"jax": jax, "jax.numpy": jnp, "jax.lax": lax,
+            "jax.tree_util": tree_util}
+
+
+def _exec(name, relpath):
+    path = os.path.join(REFERENCE_ROOT, *relpath.split("/"))
+    mod = types.ModuleType(name)
+    mod.__file__ = path
+    sys.modules[name] = mod
+    with open(path) as f:
+        exec(compile(f.read(), path, "exec"), mod.__dict__)
+    return mod
+
+
+_CACHE = {}
+
+
+def reference_flamelet_modules():
+    """``(state, solver, thermodynamic_consistency)`` modules of the
+    reference, executed against the stand-in."""
+    if "mods" in _CACHE:
+        return _CACHE["mods"]
+    if not reference_available():
+        raise RuntimeError("reference checkout not found")
+    names = ["jax", "jax.numpy", "jax.lax", "jax.tree_util", "pyrometheus",
+             "pyrometheus.flamelets", "pyrometheus.flamelets.make_pyro",
+             "pyrometheus.flamelets.state",
+             "pyrometheus.flamelets.linear_solver",
+             "pyrometheus.flamelets.equations",
+             "pyrometheus.flamelets.onedim_laplacian",
+             "pyrometheus.flamelets.solver",
+             "pyrometheus.flamelets.thermodynamic_consistency"]
+    saved = {k: sys.modules.get(k) for k in names}
+    try:
+        sys.modules.update(_jax_modules())
+        for pkg in ("pyrometheus", "pyrometheus.flamelets"):
+            m = types.ModuleType(pkg)
+            m.__path__ = []
+            sys.modules[pkg] = m
+        eqs = types.ModuleType("pyrometheus.flamelets.equations")
+        eqs.FlameletEquations = None
+        lap = types.ModuleType("pyrometheus.flamelets.onedim_laplacian")
+        lap.Laplacian = None
+        sys.modules[eqs.__name__] = eqs
+        sys.modules[lap.__name__] = lap
+        fl = "pyrometheus/flamelets/"
+        _exec("pyrometheus.flamelets.make_pyro", fl + "make_pyro.py")
+        state = _exec("pyrometheus.flamelets.state", fl + "state.py")
+        _exec("pyrometheus.flamelets.linear_solver", fl + "linear_solver.py")
+        solver = _exec("pyrometheus.flamelets.solver", fl + "solver.py")
+        tc = _exec("pyrometheus.flamelets.thermodynamic_consistency",
+                   fl + "thermodynamic_consistency.py")
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    base = state._array_to_state
+
+    def array_to_state(array):
+        s = base(array)
+        return type(s)(enthalpy=_ready(s.enthalpy),
+                       mass_fractions=_ready(s.mass_fractions))
+    solver._array_to_state = array_to_state
+    tc._array_to_state = array_to_state
+    _CACHE["mods"] = (state, solver, tc)
+    return _CACHE["mods"]
+
+
+class _Gas:
+    def __init__(self, fo, n_species):
+        self.fo = fo
+        self.num_species = n_species
+
+    def get_temperature_from_enthalpy(self, h, y, t_guess):
+        return _ready(self.fo.temperature(h, y, t_guess))
+
+
+class OracleGovEquations:
+    """The reference ``FlameletEquations`` methods the driver and the EOS
+    loop call, for one flamelet, on the oracle pieces (central-difference
+    source Jacobian, ``R T`` Jacobian and pressure gradient)."""
+
+    def __init__(self, state_module, sol, n_x, dx, y_ox, y_fu):
+        self.fo = FlameletOracle(sol)
+        self.pyro_gas = _Gas(self.fo, sol.n_species)
+        self.dx = float(dx)
+        self.laplacian = types.SimpleNamespace(
+            domain=types.SimpleNamespace(dx=self.dx, num_x=int(n_x)))
+        self.y_ox = np.asarray(y_ox, dtype=np.float64)
+        self.y_fu = np.asarray(y_fu, dtype=np.float64)
+        self.State = state_module.FlameletState
+
+    def rhs(self, state, diss_rate, viscous_diss, temp_guess, pressure,
+            h_ox, h_fu):
+        r = self.fo.residual(np.asarray(state.enthalpy),
+                             np.asarray(state.mass_fractions), diss_rate,
+                             viscous_diss, temp_guess, pressure, h_ox, h_fu,
+                             self.y_ox, self.y_fu, self.dx)
+        return self.State(enthalpy=_ready(r[0]), mass_fractions=_ready(r[1:]))
+
+    def _source_jac(self, state, viscous_diss, temp_guess, pressure):
+        return self.fo.source_jacobian_fd(np.asarray(state.enthalpy),
+                                          np.asarray(state.mass_fractions),
+                                          viscous_diss, temp_guess, pressure)
+
+    def jac(self, state, diss_rate, viscous_diss, temp_guess, pressure):
+        sj = self._source_jac(state, viscous_diss, temp_guess, pressure)
+        return self.fo.blocks(sj, diss_rate, self.dx)
+
+    def adjoint_operator(self, state, diss_rate, viscous_diss, temp_guess,
+                         pressure):
+        sj = self._source_jac(state, viscous_diss, temp_guess, pressure)
+        return self.fo.adjoint_blocks(sj, diss_rate, self.dx)
+
+    def compressible_eos_rt(self, state_as_array, temp_guess, pressure):
+        a = np.asarray(state_as_array)
+        return self.fo.eos_rt(a[0], a[1:], temp_guess)
+
+    def compressible_eos_rt_jacobian(self, state_as_array, temp_guess,
+                                     pressure):
+        a = np.asarray(state_as_array)
+        return self.fo.eos_rt_jacobian_fd(a[0], a[1:], temp_guess)
+
+    def source_gradient_wrt_pressure(self, state_as_array, viscous_diss,
+                                     temp_guess, pressure):
+        a = np.asarray(state_as_array)
+        return self.fo.source_pressure_gradient_fd(a[0], a[1:], viscous_diss,
+                                                   temp_guess, pressure)
+
+
+def reference_solver(sol, n_x, dx, y_ox, y_fu):
+    """The reference's ``FlameletSolver`` for one flamelet of *n_x* points
+    of spacing *dx*, on the oracle pieces."""
+    state, solver, _ = reference_flamelet_modules()
+    fs = solver.FlameletSolver.__new__(solver.FlameletSolver)
+    fs.domain = None
+    fs.gov_eqns = OracleGovEquations(state, sol, n_x, dx, y_ox, y_fu)
+    fs.num_v = sol.n_species + 1
+    return fs
+
+
+def reference_eos(config, forward_solver):
+    """The reference's ``CompressibleEOS`` around a
+    :func:`reference_solver`."""
+    _, _, tc = reference_flamelet_modules()
+    eos = tc.CompressibleEOS.__new__(tc.CompressibleEOS)
+    eos.config = config
+    eos.fwd_solver = forward_solver
+    nv = forward_solver.num_v
+    n_x = forward_solver.gov_eqns.laplacian.domain.num_x
+    unit_h = np.zeros((nv, n_x))
+    unit_h[0] = 1.0
+    eos.unit_h = unit_h
+    return eos
+
+
+def state_of(phi):
+    """A reference ``FlameletState`` of an ``[S+1, N]`` array."""
+    state, _, _ = reference_flamelet_modules()
+    return state.FlameletState(enthalpy=_ready(phi[0]),
+                               mass_fractions=_ready(phi[1:]))

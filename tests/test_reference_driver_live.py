@@ -1,0 +1,112 @@
+"""The flamelet-solver and compressible-EOS oracles against the reference's
+own driver code (``pyrometheus/flamelets/solver.py``,
+``thermodynamic_consistency.py``) run live on the same oracle pieces, with
+a JAX stand-in (``oracle/refdriver.py``).  This pins the single-flamelet
+restatements that the batched product drivers are tested against.
+Skipped where the reference checkout is not present (it never is on a GPU
+host)."""
+
+import numpy as np
+import pytest
+
+from flamelet_solver_cases import (EOS_FLAMELETS, FLAMELETS, PRESSURE,
+                                   SOLVE, eos_case, eos_config,
+                                   flamelet_batch, mechanism, split)
+from oracle import refgen
+
+pytestmark = pytest.mark.skipif(not refgen.reference_available(),
+                                reason="reference checkout not present")
+
+
+def _cases(b):
+    n = b["lengths"]
+    return enumerate(zip(split(b["phi"], n), split(b["chi"], n),
+                         split(b["visc"], n), split(b["T"], n)))
+
+
+def _arr(state):
+    return np.vstack([np.asarray(state.enthalpy),
+                      np.asarray(state.mass_fractions)])
+
+
+def test_oracle_driver_matches_the_reference_solver():
+    """``FlameletSolver.solve`` of the reference and the oracle driver:
+    identical states and temperatures on a steady-Newton flamelet, a
+    time-march rescue and a second steady-Newton flamelet."""
+    from oracle import refdriver
+    from oracle.flamelet_solver_oracle import FlameletSolverOracle
+    np.seterr(all="ignore")
+    sol = mechanism()
+    b = flamelet_batch(sol, [FLAMELETS[i] for i in (0, 1, 3)])
+    stages = []
+    for s, (phi0, chi, visc, tg) in _cases(b):
+        ref = refdriver.reference_solver(sol, b["lengths"][s], b["dx"][s],
+                                         b["y_ox"], b["y_fu"])
+        st, temp = ref.solve(False, *SOLVE.values(), chi, visc, tg,
+                             PRESSURE, b["h_ox"][s], b["h_fu"][s],
+                             refdriver.state_of(phi0))
+        orc = FlameletSolverOracle(sol, b["dx"][s], b["y_ox"], b["y_fu"])
+        phi, t, info = orc.solve(*SOLVE.values(), chi, visc, tg, PRESSURE,
+                                 b["h_ox"][s], b["h_fu"][s], phi0)
+        np.testing.assert_array_equal(_arr(st), phi)
+        np.testing.assert_array_equal(np.asarray(temp), t)
+        stages.append(info["stage"])
+    assert stages == [0, 1, 0]
+
+
+def test_oracle_steps_match_the_reference():
+    """``flamelet_newton_step`` and ``flamelet_time_step`` (with the
+    reference's ``block_thomas``) against the oracle's update and step."""
+    from oracle import refdriver
+    from oracle.flamelet_solver_oracle import FlameletSolverOracle
+    np.seterr(all="ignore")
+    sol = mechanism()
+    b = flamelet_batch(sol, [FLAMELETS[0]])
+    _, (phi0, chi, visc, tg) = next(_cases(b))
+    args = (chi, visc, tg, PRESSURE, b["h_ox"][0], b["h_fu"][0])
+    ref = refdriver.reference_solver(sol, b["lengths"][0], b["dx"][0],
+                                     b["y_ox"], b["y_fu"])
+    orc = FlameletSolverOracle(sol, b["dx"][0], b["y_ox"], b["y_fu"])
+    v = ref.flamelet_newton_step(refdriver.state_of(phi0), *args)
+    ref_v = orc.newton_update(lambda x: orc.rhs(x, *args),
+                              lambda x: orc.jac(x, *args[:4]), phi0)
+    np.testing.assert_array_equal(_arr(v), ref_v)
+    st, it, delta = ref.flamelet_time_step(
+        refdriver.state_of(phi0), 20, 1e-9, refdriver.state_of(phi0), 1e-5,
+        *args)
+    phi, it2, d2 = orc.time_step(phi0, 20, 1e-9, phi0, 1e-5, *args)
+    np.testing.assert_array_equal(_arr(st), phi)
+    assert int(it) == it2 and float(delta) == d2
+
+
+@pytest.mark.parametrize("method, tol", [("gauss_newton", 1e-12),
+                                         ("picard", 1e-6)])
+def test_oracle_eos_loop_matches_the_reference(method, tol):
+    """``CompressibleEOS.ensure_consistency`` of the reference (its own
+    adjoint gradients and updates) and the oracle loop: identical params,
+    iteration counts, update norms, residual and ``(<h>, <T>)`` histories
+    and states."""
+    from oracle import refdriver
+    from oracle.eos_consistency_oracle import CompressibleEOSOracle
+    np.seterr(all="ignore")
+    sol = mechanism()
+    b = flamelet_batch(sol, EOS_FLAMELETS)
+    pdf, true, start, rho, e = eos_case(sol, b)
+    cfg = eos_config(method, maxiter=3, tol=tol)
+    pdfs = split(pdf, b["lengths"])
+    for s, (phi0, chi, visc, tg) in _cases(b):
+        ref = refdriver.reference_eos(cfg, refdriver.reference_solver(
+            sol, b["lengths"][s], b["dx"][s], b["y_ox"], b["y_fu"]))
+        st, temp, params, it, delta, res, hist, flag = \
+            ref.ensure_consistency(rho[s], e[s], start[:, s], pdfs[s], chi,
+                                   visc, tg, refdriver.state_of(phi0))
+        orc = CompressibleEOSOracle(sol, b["dx"][s], b["y_ox"], b["y_fu"],
+                                    cfg)
+        phi, t, p, it2, d2, r2, h2 = orc.ensure_consistency(
+            rho[s], e[s], start[:, s], pdfs[s], chi, visc, tg, phi0)
+        assert flag is False and it == it2 and float(delta) == d2
+        np.testing.assert_array_equal(np.asarray(params), p)
+        np.testing.assert_array_equal(res, r2)
+        np.testing.assert_array_equal(hist, h2)
+        np.testing.assert_array_equal(_arr(st), phi)
+        np.testing.assert_array_equal(np.asarray(temp), t)
