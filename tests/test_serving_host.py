@@ -6,7 +6,6 @@ latency statistics.  Failures are injected on the host."""
 import heapq
 
 import numpy as np
-import pytest
 
 from pyrometheus_gb300.serving import ReactorServer, Request, latency_stats
 
