@@ -69,7 +69,15 @@ class CudaGenerationOptions(CodeGenerationOptions):
     ``accum_in_smem``: keep that variant's production-rate accumulators in
     a shared-memory column instead of registers;
     ``hot_block``: threads per block of the unrolled kernels (``None``: one
-    block per SM with about 134 KB of shared-memory columns).
+    block per SM, as many threads as fit their shared-memory columns beside
+    the exp and log tables, at most 256; 224 at 53 species);
+    ``fence_every``: in the unrolled kernels, a compiler memory fence (an
+    empty ``asm volatile`` with a memory clobber; no instruction) after
+    every that many reactions, which keeps the scheduler from hoisting the
+    shared-memory loads of later reactions and so bounds register pressure
+    (``None``: no fences).  At 53 species ``-Xptxas -v`` reports 2,504
+    bytes of spill stores without fences and 148-188 with one every 2 to 16
+    reactions; its effect on run time is not yet measured, so it is off.
     """
 
     block_size: Optional[int] = None
@@ -77,6 +85,7 @@ class CudaGenerationOptions(CodeGenerationOptions):
     unrolled: bool = True
     accum_in_smem: bool = False
     hot_block: Optional[int] = None
+    fence_every: Optional[int] = None
 
 
 # {{{ mechanism model
@@ -702,7 +711,8 @@ class _Emitter:
         w('#include "jacobian.cuh"')
         if self.opts.unrolled:
             L.extend(_UnrolledEmitter(m, self.opts.accum_in_smem,
-                                      self.opts.hot_block).render())
+                                      self.opts.hot_block,
+                                      self.opts.fence_every).render())
         w('#include "kinetics_abi.cuh"')
         # fused per-cell reactor integrator: threads per CTA so that seven
         # per-thread columns (3 NS + 4 (NS + 1) doubles) fit beside the exp
@@ -783,9 +793,13 @@ class _UnrolledEmitter:
     """
 
     def __init__(self, m: _Model, accum_in_smem: bool = False,
-                 hot_block: Optional[int] = None):
+                 hot_block: Optional[int] = None,
+                 fence_every: Optional[int] = None):
         self.m = m
         self.acc_smem = accum_in_smem
+        if fence_every is not None and int(fence_every) < 1:
+            raise ValueError("fence_every must be a positive reaction count")
+        self.fence_every = int(fence_every) if fence_every else 0
         self.hot_block = int(hot_block) if hot_block else \
             _default_hot_block(m.S, 3 if accum_in_smem else 2)
         self.L: List[str] = []
@@ -978,8 +992,11 @@ class _UnrolledEmitter:
         for k in range(m.S):
             w(f"  {self.W(k)} = 0.0;")
         w("  bool bad = false;")
-        for r in m.rx:
+        for j, r in enumerate(m.rx):
             self.reaction(r)
+            if self.fence_every and (j + 1) % self.fence_every == 0 \
+                    and j + 1 < len(m.rx):
+                w('  asm volatile("" ::: "memory");')
         w("  if (bad) {  // exact recompute through the table-driven path")
         w("    double lc[NS], lg[NS], lw[NS];")
         w("    const pyro::LocalCols C{lc}, G{lg}, W{lw};")

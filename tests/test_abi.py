@@ -119,6 +119,25 @@ def test_generator_options_like_reference():
     assert CudaCodeGenerator.supports_overloading()
 
 
+def test_scheduling_fences_are_opt_in():
+    """``fence_every`` puts an empty memory-clobber ``asm`` after every k-th
+    reaction of the unrolled body and nowhere by default."""
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.codegen.cuda import (CudaCodeGenerator,
+                                                CudaGenerationOptions)
+    sol = synthetic.config1_mechanism()
+    fence = 'asm volatile("" ::: "memory");'
+    assert fence not in CudaCodeGenerator.generate("t", sol)
+    n_rx = len(sol.reactions())
+    for k in (1, 4, 7):
+        src = CudaCodeGenerator.generate(
+            "t", sol, CudaGenerationOptions(fence_every=k))
+        assert src.count(fence) == (n_rx - 1) // k
+    with pytest.raises(ValueError, match="fence_every"):
+        CudaCodeGenerator.generate("t", sol,
+                                   CudaGenerationOptions(fence_every=0))
+
+
 def test_cli_writes_source(tmp_path):
     from pyrometheus_gb300 import synthetic
     from pyrometheus_gb300.cli import main
