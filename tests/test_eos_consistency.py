@@ -87,3 +87,33 @@ def test_config_and_errors(case):
     with pytest.raises(ValueError, match="params"):
         eos.ensure_consistency(rho, e, start[:2], pdf, b["chi"], b["visc"],
                                b["T"], b["phi"])
+
+
+def test_flamelets_leave_the_batch_as_they_converge(case):
+    """One flamelet starts at the parameters its targets came from and stops
+    after its first update (|v| = 0); the other goes on alone as a packed
+    sub-batch.  Both still match the single-flamelet oracle bit for bit."""
+    sol, b, (pdf, true, start, rho, e) = case
+    start = start.copy()
+    start[:, 0] = true[:, 0]
+    cfg = eos_config("gauss_newton", maxiter=3, tol=1e-6)
+    eos = _eos(sol, b, cfg)
+    st, temp, params, its, deltas, res, hist, _ = eos.ensure_consistency(
+        rho, e, start, pdf, b["chi"], b["visc"], b["T"], b["phi"])
+    assert its.tolist() == [0, 2] and deltas[0] == 0.0
+    assert np.isnan(res[1:, 0]).all() and not np.isnan(res[:, 1]).any()
+    n = b["lengths"]
+    phis = split(torch.cat([st.enthalpy[None], st.mass_fractions]).numpy(),
+                 n)
+    for s, (phi0, chi, visc, tg, w) in enumerate(zip(
+            split(b["phi"], n), split(b["chi"], n), split(b["visc"], n),
+            split(b["T"], n), split(pdf, n))):
+        orc = CompressibleEOSOracle(sol, b["dx"][s], b["y_ox"], b["y_fu"],
+                                    cfg)
+        phi, t, p, it, d, r, h = orc.ensure_consistency(
+            rho[s], e[s], start[:, s], w, chi, visc, tg, phi0)
+        assert its[s] == it
+        np.testing.assert_array_equal(params[:, s], p)
+        np.testing.assert_array_equal(res[:, s], r)
+        np.testing.assert_array_equal(phis[s], phi)
+        np.testing.assert_array_equal(split(temp.numpy(), n)[s], t)
