@@ -1088,6 +1088,29 @@ class CudaCodeGenerator(CodeGenerator):
         return build_shared_library(source, name, build_dir)
 
     @staticmethod
+    def compile_class(name: str, source: str, sol):
+        """Compile generated CUDA *source* into the drop-in class named
+        *name* (``python.py:689-697`` counterpart).  The reference's Python
+        source carries the class attributes inline; here they come from the
+        mechanism *sol* the source was generated from, and the compiled
+        library's own species and reaction counts are checked against it.
+        The source is kept as ``_MODULE_SOURCE_CODE``."""
+        import ctypes
+
+        from ..thermochemistry import load_library, make_thermochem_class
+        lib_path = build_shared_library(source, name)
+        ns, nr = ctypes.c_int(), ctypes.c_int()
+        load_library(lib_path).pyro_mechanism_info(
+            ctypes.byref(ns), ctypes.byref(nr), None, None, None)
+        if (ns.value, nr.value) != (sol.n_species, sol.n_reactions):
+            raise ValueError(
+                f"source is for {ns.value} species / {nr.value} reactions, "
+                f"the mechanism has {sol.n_species} / {sol.n_reactions}")
+        cls = make_thermochem_class(sol, lib_path, name)
+        cls._MODULE_SOURCE_CODE = source
+        return cls
+
+    @staticmethod
     def get_thermochem_class(sol, opts: Optional[CodeGenerationOptions] = None,
                              name: str = "Thermochemistry"):
         """For the mechanism *sol*, return the drop-in CUDA

@@ -105,6 +105,22 @@ def test_no_cpu_fallback():
         cls()
 
 
+def test_compile_class_like_reference():
+    """``compile_class(name, source, sol)`` builds the generated source into
+    the named class and keeps the source (``python.py:689-697``); a source
+    generated for another mechanism is refused."""
+    import pyrometheus_gb300 as pg
+    from pyrometheus_gb300 import synthetic
+    sol = synthetic.config1_mechanism()
+    src = pg.generate("Thermochemistry", sol)
+    cls = pg.compile_class("Thermochemistry", src, sol)
+    assert cls.__name__ == "Thermochemistry"
+    assert cls._MODULE_SOURCE_CODE == src
+    with pytest.raises(ValueError, match="9 species"):
+        pg.compile_class("Thermochemistry", src,
+                         synthetic.config2_mechanism())
+
+
 def test_generator_options_like_reference():
     from pyrometheus_gb300 import CodeGenerationOptions, synthetic
     from pyrometheus_gb300.codegen.cuda import CudaCodeGenerator
