@@ -154,6 +154,18 @@ class FlameletSolver:
         self._setup(equations)
         return self
 
+    @classmethod
+    def from_domain(cls, domain, pyro_gas, mass_frac_bcs, device=None):
+        """The reference's constructor order, ``FlameletSolver(domain,
+        pyro_gas, mass_frac_bcs)`` (``solver.py:53-60``): *domain* is a
+        uniform mixture-fraction grid with ``num_x`` points of spacing
+        ``dx`` (the reference's ``Domain``), or a sequence of such grids,
+        one flamelet each."""
+        domains = domain if isinstance(domain, (list, tuple)) else [domain]
+        lengths = [int(d.num_x) for d in domains]
+        dx = [float(d.dx) for d in domains]
+        return cls(pyro_gas, lengths, dx, mass_frac_bcs, device=device)
+
     def _setup(self, eq):
         self.eq = eq
         self.gov_eqns = eq

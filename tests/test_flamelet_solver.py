@@ -130,3 +130,29 @@ def test_verbose_solve_reports_each_stage(capsys):
     assert fs.last_solve["stage"][0] in (1, -1)
     if fs.last_solve["stage"][0] == -1:
         assert "did not converge" in out
+
+
+def test_from_domain_takes_the_reference_constructor_order(monkeypatch):
+    """``FlameletSolver.from_domain(domain, gas, (y_ox, y_fu))``: grids with
+    ``num_x`` and ``dx`` (one or a list) become the packed lengths and
+    spacings of the flamelet equations."""
+    import types
+
+    import pyrometheus_gb300.flamelet as fl
+    seen = {}
+
+    class Recorder:
+        def __init__(self, thermo, lengths, dx, y_ox, y_fu, device=None):
+            seen.update(thermo=thermo, lengths=list(lengths), dx=list(dx),
+                        y_ox=y_ox, y_fu=y_fu)
+            self.nv, self.lengths = 3, np.asarray(lengths)
+
+    monkeypatch.setattr(fl, "FlameletEquations", Recorder)
+    grid = types.SimpleNamespace(num_x=101, dx=0.01)
+    FlameletSolver.from_domain(grid, "gas", ("ox", "fu"))
+    assert seen == dict(thermo="gas", lengths=[101], dx=[0.01], y_ox="ox",
+                        y_fu="fu")
+    FlameletSolver.from_domain([grid, types.SimpleNamespace(num_x=11,
+                                                            dx=0.1)],
+                               "gas", ("ox", "fu"))
+    assert seen["lengths"] == [101, 11] and seen["dx"] == [0.01, 0.1]
