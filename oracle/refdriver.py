@@ -26,6 +26,7 @@ executed:
 The reference's ``FlameletSolver`` and ``CompressibleEOS`` classes are then
 used unchanged (instances are made without their constructors, which build
 the JAX equations, and given the attributes the constructors would set).
+Its ``utils.py`` set-up helpers run the same way.
 """
 
 from __future__ import annotations
@@ -237,3 +238,27 @@ def state_of(phi):
     state, _, _ = reference_flamelet_modules()
     return state.FlameletState(enthalpy=_ready(phi[0]),
                                mass_fractions=_ready(phi[1:]))
+
+
+def reference_flamelet_utils():
+    """The reference's ``flamelets/utils.py`` module (``bell_profile``,
+    ``stoichiometric_mixture_fraction``), executed against the stand-in."""
+    if "utils" in _CACHE:
+        return _CACHE["utils"]
+    if not reference_available():
+        raise RuntimeError("reference checkout not found")
+    names = ["jax", "jax.numpy", "jax.lax", "jax.tree_util",
+             "pyrometheus.flamelets.utils"]
+    saved = {k: sys.modules.get(k) for k in names}
+    try:
+        sys.modules.update(_jax_modules())
+        mod = _exec("pyrometheus.flamelets.utils",
+                    "pyrometheus/flamelets/utils.py")
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    _CACHE["utils"] = mod
+    return mod

@@ -284,6 +284,14 @@ class Solution:
                                           ) -> np.ndarray:
         return np.array(self._fits().diffusivity[i, j], dtype=np.float64)
 
+    def n_atoms(self, species, element) -> float:
+        """Atoms of *element* (index or name) in *species* (index or
+        name), as Cantera's ``Solution.n_atoms``."""
+        sp = self.species(species)
+        el = element if isinstance(element, str) else \
+            self.element_names[element]
+        return float(sp.composition.get(el, 0.0))
+
     # -- convenience (not part of the Cantera surface) ---------------------
     def element_matrix(self) -> np.ndarray:
         """(n_elements, n_species) atom counts."""
