@@ -262,3 +262,39 @@ def reference_flamelet_utils():
                 sys.modules[k] = v
     _CACHE["utils"] = mod
     return mod
+
+
+def reference_laplacian(num_x):
+    """The reference's ``Laplacian`` (``onedim_laplacian.py``, with its
+    ``stencils.py`` and ``domain.py``) on the uniform grid of *num_x* points
+    over [0, 1], executed against the stand-in."""
+    state, _, _ = reference_flamelet_modules()
+    if "lap" not in _CACHE:
+        names = ["jax", "jax.numpy", "jax.lax", "jax.tree_util", "pyrometheus",
+                 "pyrometheus.flamelets", "pyrometheus.flamelets.state",
+                 "pyrometheus.flamelets.stencils",
+                 "pyrometheus.flamelets.domain",
+                 "pyrometheus.flamelets.onedim_laplacian"]
+        saved = {k: sys.modules.get(k) for k in names}
+        try:
+            sys.modules.update(_jax_modules())
+            for pkg in ("pyrometheus", "pyrometheus.flamelets"):
+                m = types.ModuleType(pkg)
+                m.__path__ = []
+                sys.modules[pkg] = m
+            sys.modules["pyrometheus.flamelets.state"] = state
+            fl = "pyrometheus/flamelets/"
+            _exec("pyrometheus.flamelets.stencils", fl + "stencils.py")
+            domain = _exec("pyrometheus.flamelets.domain", fl + "domain.py")
+            lap = _exec("pyrometheus.flamelets.onedim_laplacian",
+                        fl + "onedim_laplacian.py")
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    sys.modules.pop(k, None)
+                else:
+                    sys.modules[k] = v
+        _CACHE["lap"] = (domain, lap)
+    domain, lap = _CACHE["lap"]
+    return lap.Laplacian(domain.Domain(domain.DomainConfig(
+        num_x=int(num_x), x_l=0.0, x_r=1.0)))

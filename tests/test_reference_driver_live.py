@@ -110,3 +110,26 @@ def test_oracle_eos_loop_matches_the_reference(method, tol):
         np.testing.assert_array_equal(hist, h2)
         np.testing.assert_array_equal(_arr(st), phi)
         np.testing.assert_array_equal(np.asarray(temp), t)
+
+
+@pytest.mark.parametrize("n, nv", [(3, 10), (12, 10), (64, 54)])
+def test_oracle_laplacian_matches_the_reference(n, nv):
+    """The reference's ``Laplacian.assemble_block_form`` and
+    ``apply_operator`` (``onedim_laplacian.py:144-212``, with its stencils
+    and domain) against the oracle's blocks and Laplacian, bit for bit."""
+    from oracle import refdriver
+    from oracle.flamelet_oracle import FlameletOracle
+    lap = refdriver.reference_laplacian(n)
+    lap.assemble_block_form(nv)
+    dx = 1.0 / (n - 1)
+    assert lap.domain.dx == dx
+    # chi = 2 makes the oracle's chi/2 factor exactly one
+    lo, c, up = FlameletOracle.blocks(np.zeros((n, nv, nv)),
+                                      np.full(n, 2.0), dx)
+    np.testing.assert_array_equal(lo, lap.lower_blocks)
+    np.testing.assert_array_equal(c, lap.central_blocks)
+    np.testing.assert_array_equal(up, lap.upper_blocks)
+    phi = np.random.default_rng(n).standard_normal((nv, n))
+    np.testing.assert_array_equal(
+        _arr(lap.apply_operator(refdriver.state_of(phi))),
+        FlameletOracle.laplacian(phi, dx))
