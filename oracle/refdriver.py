@@ -26,7 +26,10 @@ executed:
 The reference's ``FlameletSolver`` and ``CompressibleEOS`` classes are then
 used unchanged (instances are made without their constructors, which build
 the JAX equations, and given the attributes the constructors would set).
-Its ``utils.py`` set-up helpers run the same way.
+Its ``utils.py`` set-up helpers, its ``Laplacian`` and its
+``FlameletEquations`` (around the reference's generated class and its own
+``make_pyro_object``; ``jax.vmap`` is a loop, ``jax.jacfwd`` is not
+provided) run the same way.
 """
 
 from __future__ import annotations
@@ -41,11 +44,34 @@ from .flamelet_oracle import FlameletOracle
 from .refgen import REFERENCE_ROOT, _scan, reference_available
 
 
+class _AtIndex:
+    def __init__(self, array, index):
+        self.array, self.index = array, index
+
+    def set(self, value):
+        out = self.array.copy()
+        out[self.index] = value
+        return out
+
+
+class _At:
+    def __init__(self, array):
+        self.array = array
+
+    def __getitem__(self, index):
+        return _AtIndex(self.array, index)
+
+
 class _Ready(np.ndarray):
-    """A numpy array that also answers JAX's ``block_until_ready``."""
+    """A numpy array that also answers JAX's ``block_until_ready`` and
+    functional ``.at[index].set(value)`` (a copy with the update)."""
 
     def block_until_ready(self):
         return self
+
+    @property
+    def at(self):
+        return _At(self)
 
 
 def _ready(x):
@@ -56,6 +82,27 @@ def _while_loop(cond, body, carry):
     while cond(carry):
         carry = body(carry)
     return carry
+
+
+def _vmap(fun, in_axes=0):
+    """``jax.vmap`` as a loop over the mapped axis, outputs stacked."""
+    def mapped(*args):
+        axes = in_axes if isinstance(in_axes, (list, tuple)) \
+            else (in_axes,) * len(args)
+        n = next(np.shape(a)[ax] for a, ax in zip(args, axes)
+                 if ax is not None)
+        outs = [fun(*[a if ax is None else np.take(a, i, axis=ax)
+                      for a, ax in zip(args, axes)]) for i in range(n)]
+        return _ready(np.stack(outs))
+    return mapped
+
+
+def _no_jacfwd(fun, argnums=0):
+    """Forward-mode autodiff is not part of the stand-in: the functions it
+    builds may be made, not called."""
+    def unavailable(*args, **kwargs):
+        raise NotImplementedError("jax.jacfwd is not available here")
+    return unavailable
 
 
 def _jax_modules():
@@ -75,6 +122,8 @@ def _jax_modules():
     def jit(fun=None, **kwargs):
         return fun if fun is not None else (lambda f: f)
     jax.jit = jit
+    jax.vmap = _vmap
+    jax.jacfwd = _no_jacfwd
     return {"jax": jax, "jax.numpy": jnp, "jax.lax": lax,
             "jax.tree_util": tree_util}
 
@@ -298,3 +347,52 @@ def reference_laplacian(num_x):
     domain, lap = _CACHE["lap"]
     return lap.Laplacian(domain.Domain(domain.DomainConfig(
         num_x=int(num_x), x_l=0.0, x_r=1.0)))
+
+
+def reference_flamelet_equations(sol, num_x, y_ox, y_fu):
+    """The reference's ``FlameletEquations`` (``equations.py``) for one
+    flamelet of *num_x* points over [0, 1], around the reference's generated
+    class (``oracle.refgen``) wrapped by its own ``make_pyro_object`` on the
+    stand-in ``jax.numpy``.  ``rhs``, ``source_terms`` and the vmapped
+    ``compressible_eos_rt`` run; the ``jax.jacfwd`` Jacobians do not."""
+    from .refgen import reference_class
+    state, _, _ = reference_flamelet_modules()
+    lap = reference_laplacian(num_x)
+    if "eqs" not in _CACHE:
+        names = ["jax", "jax.numpy", "jax.lax", "jax.tree_util", "pyrometheus",
+                 "pyrometheus.flamelets", "pyrometheus.flamelets.state",
+                 "pyrometheus.flamelets.make_pyro",
+                 "pyrometheus.flamelets.onedim_laplacian",
+                 "pyrometheus.flamelets.equations"]
+        saved = {k: sys.modules.get(k) for k in names}
+        try:
+            mods = _jax_modules()
+            sys.modules.update(mods)
+            for pkg in ("pyrometheus", "pyrometheus.flamelets"):
+                m = types.ModuleType(pkg)
+                m.__path__ = []
+                sys.modules[pkg] = m
+            sys.modules["pyrometheus.flamelets.state"] = state
+            sys.modules["pyrometheus.flamelets.onedim_laplacian"] = \
+                sys.modules.get("pyrometheus.flamelets.onedim_laplacian") \
+                or types.ModuleType("pyrometheus.flamelets.onedim_laplacian")
+            sys.modules["pyrometheus.flamelets.onedim_laplacian"].Laplacian \
+                = type(lap)
+            fl = "pyrometheus/flamelets/"
+            make_pyro = _exec("pyrometheus.flamelets.make_pyro",
+                              fl + "make_pyro.py")
+            eqs = _exec("pyrometheus.flamelets.equations",
+                        fl + "equations.py")
+        finally:
+            for k, v in saved.items():
+                if v is None:
+                    sys.modules.pop(k, None)
+                else:
+                    sys.modules[k] = v
+        # JAX arrays defer arithmetic with unknown types to them; numpy
+        # arrays do so for classes that opt out of ufuncs
+        state.StateContainer.__array_ufunc__ = None
+        _CACHE["eqs"] = (make_pyro, eqs, mods["jax.numpy"])
+    make_pyro, eqs, jnp = _CACHE["eqs"]
+    gas = make_pyro.make_pyro_object(reference_class(sol), jnp)
+    return eqs.FlameletEquations(gas, lap, _ready(y_ox), _ready(y_fu))

@@ -133,3 +133,35 @@ def test_oracle_laplacian_matches_the_reference(n, nv):
     np.testing.assert_array_equal(
         _arr(lap.apply_operator(refdriver.state_of(phi))),
         FlameletOracle.laplacian(phi, dx))
+
+
+@pytest.mark.parametrize("tag", ["s9", "s53"])
+def test_reference_flamelet_equations_live(tag):
+    """The reference's ``FlameletEquations.rhs`` (``equations.py:167-238``,
+    around its generated class and ``make_pyro_object``) run live: equal to
+    the golden residual bit for bit and to the oracle within 1e-12 of the
+    term magnitudes; its vmapped ``compressible_eos_rt`` against the
+    oracle's ``R T`` (per-point against batch-wide temperature iteration
+    stops: 1e-12 relative)."""
+    from oracle import refdriver
+    from oracle.flamelet_oracle import FlameletOracle
+    from test_flamelet import _golden, _resid_scale
+    np.seterr(all="ignore")
+    sol, d = _golden(tag)
+    n = d["h"].shape[0]
+    eq = refdriver.reference_flamelet_equations(sol, n, d["y_ox"],
+                                                d["y_fu"])
+    phi = np.vstack([d["h"], d["Y"]])
+    r = _arr(eq.rhs(refdriver.state_of(phi), refdriver._ready(d["chi"]),
+                    d["visc"], d["T_guess"], float(d["P"]),
+                    float(d["h_ox"]), float(d["h_fu"])))
+    np.testing.assert_array_equal(r, d["resid"])
+    fo = FlameletOracle(sol)
+    ref = fo.residual(d["h"], d["Y"], d["chi"], d["visc"], d["T_guess"],
+                      float(d["P"]), float(d["h_ox"]), float(d["h_fu"]),
+                      d["y_ox"], d["y_fu"], float(d["dx"]))
+    assert np.all(np.abs(r - ref) <= 1e-12 * _resid_scale(d))
+    rt = np.asarray(eq.compressible_eos_rt(phi, d["T_guess"],
+                                           float(d["P"])))
+    ort = fo.eos_rt(d["h"], d["Y"], d["T_guess"])
+    assert np.abs(rt - ort).max() <= 1e-12 * np.abs(ort).max()
