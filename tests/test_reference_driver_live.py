@@ -165,3 +165,22 @@ def test_reference_flamelet_equations_live(tag):
                                            float(d["P"])))
     ort = fo.eos_rt(d["h"], d["Y"], d["T_guess"])
     assert np.abs(rt - ort).max() <= 1e-12 * np.abs(ort).max()
+    # the pieces of rhs: source terms, equation of state, boundary values
+    src = _arr(eq.source_terms(refdriver.state_of(phi), d["visc"],
+                               d["T_guess"], float(d["P"])))
+    np.testing.assert_array_equal(src, d["src"])
+    osrc = fo.source(d["h"], d["Y"], d["visc"], d["T_guess"], float(d["P"]))
+    assert np.all(np.abs(src - osrc) <= 1e-12 * np.abs(osrc).max(
+        axis=1, keepdims=True))
+    rho, t = eq.equation_of_state(refdriver.state_of(phi), d["T_guess"],
+                                  float(d["P"]))
+    ot = fo.temperature(d["h"], d["Y"], d["T_guess"])
+    np.testing.assert_array_equal(np.asarray(t), ot)
+    # the generated class and the oracle sum 1/W_mix in different orders
+    np.testing.assert_allclose(np.asarray(rho), fo.th.get_density(
+        float(d["P"]), ot, d["Y"]), rtol=1e-15, atol=0)
+    bc = _arr(eq.boundary_conditions(float(d["h_ox"]), float(d["h_fu"])))
+    ref_bc = np.zeros_like(phi)
+    ref_bc[0, 0], ref_bc[0, -1] = d["h_ox"], d["h_fu"]
+    ref_bc[1:, 0], ref_bc[1:, -1] = d["y_ox"], d["y_fu"]
+    np.testing.assert_array_equal(bc, ref_bc)
