@@ -10,6 +10,8 @@ A numpy restatement, for one flamelet on a uniform grid, of
 * ``FlameletEquations.jac`` (``equations.py:240-298``): central blocks
   ``chi/2 Lap_c + dS/dphi`` (zero source blocks at the two boundary
   points), lower ``chi[1:]/2 Lap_l``, upper ``chi[:-1]/2 Lap_u``;
+* ``FlameletEquations.jacobian_action`` (``equations.py:411-450``):
+  ``chi/2 Lap(v) + dS/dphi v`` with every point's source Jacobian;
 * ``source_terms`` (``equations.py:340-385``): ``S = (v/rho, W w/rho)``
   with T from the enthalpy Newton of ``make_pyro.py:255-299`` and
   ``rho = get_density(p, T, Y)``;
@@ -102,6 +104,15 @@ class FlameletOracle:
             fm = self.source(xm[0], xm[1:], visc, t_guess, p)
             jac[:, :, q] = ((fp - fm) / (2.0 * step)).T
         return jac
+
+    def jacobian_action(self, v, h, y, chi, visc, t_guess, p, dx):
+        """``chi/2 Lap(v) + dS/dphi v`` per point, ``[S+1, N]``
+        (``FlameletEquations.jacobian_action``, ``equations.py:411-450``):
+        unlike :meth:`blocks`, the boundary points keep their source
+        Jacobians."""
+        sj = self.source_jacobian_fd(h, y, visc, t_guess, p)
+        return 0.5 * chi * self.laplacian(v, dx) + np.einsum("ijk,ki->ji",
+                                                             sj, v)
 
     @staticmethod
     def blocks(source_jac, chi, dx):

@@ -97,6 +97,27 @@ def _vmap(fun, in_axes=0):
     return mapped
 
 
+def _jacfwd_fd(fun, argnums=0, rel=1e-6):
+    """``jax.jacfwd`` with respect to a point's state vector (argument 0)
+    by central differences, the oracle's step rule: ``rel * max(|h|, 1)``
+    for the enthalpy, ``rel`` for the mass fractions."""
+    if argnums != 0:
+        return _no_jacfwd(fun, argnums)
+
+    def jac(x, *args):
+        x = np.asarray(x, dtype=np.float64)
+        cols = []
+        for q in range(x.shape[0]):
+            step = rel * max(abs(x[q]), 1.0) if q == 0 else rel
+            xp, xm = x.copy(), x.copy()
+            xp[q] += step
+            xm[q] -= step
+            cols.append((np.asarray(fun(_ready(xp), *args))
+                         - np.asarray(fun(_ready(xm), *args))) / (2 * step))
+        return np.stack(cols, axis=1)
+    return jac
+
+
 def _no_jacfwd(fun, argnums=0):
     """Forward-mode autodiff is not part of the stand-in: the functions it
     builds may be made, not called."""
@@ -349,12 +370,16 @@ def reference_laplacian(num_x):
         num_x=int(num_x), x_l=0.0, x_r=1.0)))
 
 
-def reference_flamelet_equations(sol, num_x, y_ox, y_fu):
+def reference_flamelet_equations(sol, num_x, y_ox, y_fu,
+                                 fd_jacobian=False):
     """The reference's ``FlameletEquations`` (``equations.py``) for one
     flamelet of *num_x* points over [0, 1], around the reference's generated
     class (``oracle.refgen``) wrapped by its own ``make_pyro_object`` on the
     stand-in ``jax.numpy``.  ``rhs``, ``source_terms`` and the vmapped
-    ``compressible_eos_rt`` run; the ``jax.jacfwd`` Jacobians do not."""
+    ``compressible_eos_rt`` run; the ``jax.jacfwd`` Jacobians do not, unless
+    *fd_jacobian* puts central differences in place of ``jax.jacfwd`` for
+    the source Jacobian (``vmap_jacobian``, used by ``jac`` and
+    ``jacobian_action``)."""
     from .refgen import reference_class
     state, _, _ = reference_flamelet_modules()
     lap = reference_laplacian(num_x)
@@ -395,4 +420,9 @@ def reference_flamelet_equations(sol, num_x, y_ox, y_fu):
         _CACHE["eqs"] = (make_pyro, eqs, mods["jax.numpy"])
     make_pyro, eqs, jnp = _CACHE["eqs"]
     gas = make_pyro.make_pyro_object(reference_class(sol), jnp)
-    return eqs.FlameletEquations(gas, lap, _ready(y_ox), _ready(y_fu))
+    if fd_jacobian:
+        eqs.jax.jacfwd = _jacfwd_fd
+    try:
+        return eqs.FlameletEquations(gas, lap, _ready(y_ox), _ready(y_fu))
+    finally:
+        eqs.jax.jacfwd = _no_jacfwd

@@ -184,3 +184,42 @@ def test_reference_flamelet_equations_live(tag):
     ref_bc[0, 0], ref_bc[0, -1] = d["h_ox"], d["h_fu"]
     ref_bc[1:, 0], ref_bc[1:, -1] = d["y_ox"], d["y_fu"]
     np.testing.assert_array_equal(bc, ref_bc)
+
+
+@pytest.mark.parametrize("tag", ["s9", "s53"])
+def test_oracle_jacobian_assembly_matches_the_reference(tag):
+    """The reference's ``jac`` and ``jacobian_action``
+    (``equations.py:228-282, 411-450``) with central differences standing
+    in for ``jax.jacfwd`` against the oracle's blocks and
+    ``jacobian_action``: L and U bit for bit, the central blocks and the
+    action within 1e-8 of each row's largest entry (the two difference
+    Jacobians differ only by where the temperature iterations stop, per
+    point in the reference, batch-wide in the oracle)."""
+    from oracle import refdriver
+    from oracle.flamelet_oracle import FlameletOracle
+    from test_flamelet import _golden
+    np.seterr(all="ignore")
+    sol, d = _golden(tag)
+    n = d["h"].shape[0]
+    eq = refdriver.reference_flamelet_equations(sol, n, d["y_ox"],
+                                                d["y_fu"], fd_jacobian=True)
+    phi = np.vstack([d["h"], d["Y"]])
+    args = (refdriver._ready(d["chi"]), d["visc"], d["T_guess"],
+            float(d["P"]))
+    fo = FlameletOracle(sol)
+    sj = fo.source_jacobian_fd(d["h"], d["Y"], d["visc"], d["T_guess"],
+                               float(d["P"]))
+    lo, c, up = (np.asarray(x) for x in eq.jac(refdriver.state_of(phi),
+                                               *args))
+    olo, oc, oup = fo.blocks(sj, d["chi"], float(d["dx"]))
+    np.testing.assert_array_equal(lo, olo)
+    np.testing.assert_array_equal(up, oup)
+    assert np.all(np.abs(c - oc)
+                  <= 1e-8 * np.abs(oc).max(axis=2, keepdims=True))
+    v = np.random.default_rng(1).standard_normal(phi.shape)
+    ja = _arr(eq.jacobian_action(refdriver.state_of(v),
+                                 refdriver.state_of(phi), *args))
+    ref = fo.jacobian_action(v, d["h"], d["Y"], d["chi"], d["visc"],
+                             d["T_guess"], float(d["P"]), float(d["dx"]))
+    assert np.all(np.abs(ja - ref)
+                  <= 1e-8 * np.abs(ref).max(axis=1, keepdims=True))
