@@ -9,7 +9,10 @@
  * Packed layout: system s owns rows [row_off[s], row_off[s+1]) of
  * C[rows][nv][nv] (diagonal blocks), L and U (sub/super-diagonal blocks;
  * the last row of each system is ignored), b[rows][nv] and x[rows][nv].
- * All pointers are device pointers; row-major blocks; FP64.
+ * Every system needs at least one row: a system whose row range is empty
+ * (row_off[s+1] <= row_off[s]) is skipped, its x left untouched, and bit 1
+ * of *status is set.  All pointers are device pointers; row-major blocks;
+ * FP64.
  */
 #ifndef PYRO_BLOCK_THOMAS_H
 #define PYRO_BLOCK_THOMAS_H
@@ -33,9 +36,9 @@ int64_t pyro_block_thomas_smem_bytes(int nv);
 /* Solve nsys systems (1 <= nv <= 64).  order: permutation of 0..nsys-1
  * (longest first balances best); work: pyro_block_thomas_work_doubles
  * doubles; counter: device int (zeroed by the call); status: device int,
- * bit 0 set on a zero pivot (may be NULL); threads: CTA size (multiple of
- * 32); ctas: grid size (0 = all resident).  Asynchronous on `stream`;
- * returns 0 or a PyroStatus error. */
+ * bit 0 set on a zero pivot, bit 1 on an empty system (may be NULL);
+ * threads: CTA size (multiple of 32); ctas: grid size (0 = all resident).
+ * Asynchronous on `stream`; returns 0 or a PyroStatus error. */
 int pyro_block_thomas(const double* L, const double* C, const double* U,
                       const double* b, double* x, const int64_t* row_off,
                       const int* order, int nsys, int nv, double* work,
@@ -55,8 +58,24 @@ int pyro_block_thomas_small(const double* L, const double* C, const double* U,
                             int nsys, int nv, double* work, int* status,
                             int threads, cudaStream_t stream);
 
-/* More right-hand sides for systems already solved: after pyro_block_thomas
- * or pyro_block_thomas_small, `work` holds every row's LU factors and
+/* pyro_block_thomas for blocks of size nv <= 16 with 32 / nv systems per
+ * warp (three at nv = 10), one lane per block row and the working rows in
+ * registers: every lane of every FP64 instruction works, and nothing
+ * synchronises beyond a warp.  Pivoting and the kept factors are getrf's,
+ * in the workspace layout of pyro_block_thomas (so
+ * pyro_block_thomas_resolve applies).  Same arguments as
+ * pyro_block_thomas without the CTA size (128 threads); ctas: persistent
+ * grid (0 = all resident).  Replaces the same reference function,
+ * pyrometheus/flamelets/linear_solver.py:6-103. */
+int pyro_block_thomas_seg(const double* L, const double* C, const double* U,
+                          const double* b, double* x, const int64_t* row_off,
+                          const int* order, int nsys, int nv, double* work,
+                          int* counter, int* status, int ctas,
+                          cudaStream_t stream);
+
+/* More right-hand sides for systems already solved: after pyro_block_thomas,
+ * pyro_block_thomas_small or pyro_block_thomas_seg, `work` holds every row's
+ * LU factors and
  * pivots of C'_i; for the same L, C, U this solves nrhs (1..4) further
  * systems, B[c][rows][nv] -> X[c][rows][nv] (the c-th at offset
  * c * rhs_stride), with the vector recurrences only (4 nv^2 FMAs per row
@@ -64,12 +83,13 @@ int pyro_block_thomas_small(const double* L, const double* C, const double* U,
  * block_thomas, pyrometheus/flamelets/linear_solver.py:6-103, including
  * the adjoint solves that share one operator in
  * pyrometheus/flamelets/thermodynamic_consistency.py:105-307.  order and
- * counter as for pyro_block_thomas; nv <= 64; B and X must not overlap. */
+ * counter as for pyro_block_thomas; status (may be NULL): bit 1 on an empty
+ * system; nv <= 64; B and X must not overlap. */
 int pyro_block_thomas_resolve(const double* L, const double* U,
                               const double* B, double* X, int nrhs,
                               int64_t rhs_stride, const int64_t* row_off,
                               const int* order, int nsys, int nv,
-                              const double* work, int* counter,
+                              const double* work, int* counter, int* status,
                               cudaStream_t stream);
 
 /* No counterpart in the reference (its block_thomas allocates through JAX

@@ -267,8 +267,13 @@ __global__ void k_block_thomas(const double* __restrict__ Lm,
     if (q >= nsys) break;
     const int s = order[q];
     const int64_t r0 = row_off[s];
-    const int N = (int)(row_off[s + 1] - r0);
-    solve_system(Lm, Cm, Um, B, X, r0, N, nv, work, smem, &s_sing);
+    const int64_t n64 = row_off[s + 1] - r0;
+    if (n64 <= 0) {  // an empty row range: skipped and flagged
+      if (threadIdx.x == 0 && status) atomicOr(status, 2);
+      __syncthreads();
+      continue;
+    }
+    solve_system(Lm, Cm, Um, B, X, r0, (int)n64, nv, work, smem, &s_sing);
     if (threadIdx.x == 0 && s_sing && status) atomicOr(status, 1);
     __syncthreads();
   }
@@ -311,7 +316,12 @@ __global__ void __launch_bounds__(64)
 #define EP(i, j) P[((i) * LD + (j)) * T]
   const int s = order[q];
   const int64_t r0 = row_off[s];
-  const int N = (int)(row_off[s + 1] - r0);
+  const int64_t n64 = row_off[s + 1] - r0;
+  if (n64 <= 0) {  // an empty row range: skipped and flagged
+    if (status) atomicOr(status, 2);
+    return;
+  }
+  const int N = (int)n64;
   constexpr int64_t WROW = (int64_t)NV * NV + 2 * NV;
   bool singular = false;
   for (int i = 0; i < N; ++i) {
@@ -502,8 +512,9 @@ PYRO_EXPORT int64_t pyro_block_thomas_smem_bytes(int nv) {
 // Solve nsys block-tridiagonal systems (packed as described above).
 // order: a permutation of 0..nsys-1 (longest first balances best); counter
 // and status: device ints (counter is zeroed here, status gets bit 0 set
-// for a zero pivot); threads: CTA size (multiple of 32, <= 1024); ctas:
-// grid size (0: as many as fit, resident).  Asynchronous on `stream`.
+// for a zero pivot and bit 1 for a system with an empty row range, which is
+// skipped); threads: CTA size (multiple of 32, <= 1024); ctas: grid size
+// (0: as many as fit, resident).  Asynchronous on `stream`.
 PYRO_EXPORT int pyro_block_thomas(const double* L, const double* C,
                                   const double* U, const double* b, double* x,
                                   const int64_t* row_off, const int* order,
@@ -572,6 +583,319 @@ PYRO_EXPORT int pyro_block_thomas_small(const double* L, const double* C,
     PYRO_BT_SMALL(9) PYRO_BT_SMALL(10) PYRO_BT_SMALL(11) PYRO_BT_SMALL(12)
     PYRO_BT_SMALL(13) PYRO_BT_SMALL(14) PYRO_BT_SMALL(15) PYRO_BT_SMALL(16)
 #undef PYRO_BT_SMALL
+    default:
+      return PYRO_ERR_ARGUMENT;
+  }
+}
+
+// ------------------------------------------------------------------------
+// Small blocks, several systems per warp (nv <= 16).
+//
+// A warp-wide FP64 instruction costs GB300's narrow FP64 pipe the same
+// however many of its lanes are active, so small blocks need every lane
+// busy, and the CTA-per-system kernel above, whose 10 x 10 steps keep a few
+// lanes busy between barriers, cannot.  Here a system takes a segment of NV
+// consecutive lanes (P = 32 / NV systems per warp: three at nv = 10) and
+// lane r of a segment holds row r of the system's working blocks in
+// registers; nothing synchronises beyond the warp.
+//
+// Forward sweep, per block row: C'_i | b'_i = (C_i | b_i) - L_{i-1}
+// (S_{i-1} | t_{i-1}) with S_{i-1} | t_{i-1} read from warp-private shared
+// memory; then one elimination pass over [C'_i | U_i | b'_i] with partial
+// pivoting.  Row interchanges are relabellings (a lane keeps its row and
+// tracks the position LAPACK's swaps would move it to); the pivot is the
+// largest |a| of the eligible rows, ties to the lowest position, as getrf
+// chooses it.  Below the pivot the pass is LU's elimination (its
+// multipliers and the pivot rows are exactly getrf's factors, kept in the
+// workspace in the layout of the kernels above); above the pivot it also
+// eliminates (Gauss-Jordan), which in SIMT costs nothing extra: the lanes
+// of rows above the pivot run the same instructions as the others.  Each
+// lane's right-hand-side row, scaled by its pivot's reciprocal, is then row
+// `pivot step` of S_i | t_i.  The backward sweep solves with the kept LU
+// factors, x_i = C'_i^-1 (b'_i - U_i x_{i+1}), as the reference does.
+
+namespace {
+
+constexpr int kSegWarps = 4;
+
+template <int NV>
+struct SegCfg {
+  static constexpr int P = 32 / NV;         // systems per warp
+  static constexpr int RS = NV + 1;         // shared row stride (S | t)
+  static constexpr int SMEM = P * NV * RS;  // doubles per warp
+  static constexpr int ROUNDS = NV <= 1 ? 0 : NV <= 2 ? 1 : NV <= 4 ? 2
+                                : NV <= 8 ? 3 : 4;
+};
+
+__device__ __forceinline__ long long abs_key(double v) {
+  // |v|'s bit pattern orders like |v|; NaN ranks below every number
+  const long long b = __double_as_longlong(v) & 0x7fffffffffffffffLL;
+  return b > 0x7ff0000000000000LL ? -1LL : b;
+}
+
+template <int NV>
+__global__ void __launch_bounds__(kSegWarps * 32)
+    k_block_thomas_seg(const double* __restrict__ Lm,
+                       const double* __restrict__ Cm,
+                       const double* __restrict__ Um,
+                       const double* __restrict__ B, double* __restrict__ X,
+                       const int64_t* __restrict__ row_off,
+                       const int* __restrict__ order, int nsys,
+                       double* __restrict__ work, int* __restrict__ counter,
+                       int* __restrict__ status) {
+  using Cfg = SegCfg<NV>;
+  constexpr int P = Cfg::P, RS = Cfg::RS, NC = 2 * NV + 1;
+  constexpr int64_t NN = (int64_t)NV * NV, WROW = NN + 2 * NV;
+  __shared__ double s_st[kSegWarps][Cfg::SMEM];
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int seg = lane / NV, r = lane - seg * NV, base = seg * NV;
+  // lanes past the last segment (32 mod NV of them) own no system and no
+  // shared rows; they read segment 0's rows and never write them
+  double* st = s_st[wid] + (seg < P ? seg : 0) * NV * RS;
+  for (;;) {
+    int q0 = 0;
+    if (lane == 0) q0 = atomicAdd(counter, P);
+    q0 = __shfl_sync(0xffffffffu, q0, 0);
+    if (q0 >= nsys) break;
+    const int q = q0 + seg;
+    const bool has = seg < P && q < nsys;
+    int64_t r0 = 0;
+    int N = 0;
+    if (has) {
+      const int s = order[q];
+      r0 = row_off[s];
+      const int64_t n64 = row_off[s + 1] - r0;
+      // an empty (or inverted) row range is skipped and flagged
+      N = n64 > 0 ? (int)n64 : 0;
+      if (n64 <= 0 && r == 0 && status) atomicOr(status, 2);
+    }
+    const int nmax = __reduce_max_sync(0xffffffffu, N);
+    bool singular = false;
+    double xlast = 0.0;
+    // ---- forward sweep
+    for (int i = 0; i < nmax; ++i) {
+      const bool act = i < N;
+      const int64_t row = r0 + i;
+      double a[NC], l[NV];
+      if (act) {
+        const double* __restrict__ Ci = Cm + row * NN + r * NV;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) a[j] = __ldg(Ci + j);
+        a[2 * NV] = __ldg(B + row * NV + r);
+        if (i + 1 < N) {
+          const double* __restrict__ Ui = Um + row * NN + r * NV;
+#pragma unroll
+          for (int j = 0; j < NV; ++j) a[NV + j] = __ldg(Ui + j);
+        } else {
+#pragma unroll
+          for (int j = 0; j < NV; ++j) a[NV + j] = 0.0;
+        }
+        if (i > 0) {
+          const double* __restrict__ Li = Lm + (row - 1) * NN + r * NV;
+#pragma unroll
+          for (int k = 0; k < NV; ++k) l[k] = __ldg(Li + k);
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < NC; ++j) a[j] = 0.0;
+      }
+      if (i > 0) {
+        // C' = C - L S_prev, b' = b - L t_prev (S | t in shared memory)
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          const double lk = act ? l[k] : 0.0;
+#pragma unroll
+          for (int j = 0; j < NV; ++j)
+            a[j] = fma(-lk, st[k * RS + j], a[j]);
+          a[2 * NV] = fma(-lk, st[k * RS + NV], a[2 * NV]);
+        }
+      }
+      double* __restrict__ w = work + row * WROW;
+      if (act) w[NN + r] = a[2 * NV];  // b'_i, original row order
+      __syncwarp();
+      // elimination with relabelled partial pivoting
+      int pos = r, myk = 0, mypiv = 0;
+      bool elig = true;
+      double myinv = 0.0, lu[NV];
+#pragma unroll
+      for (int k = 0; k < NV; ++k) {
+        long long bk = elig ? abs_key(a[k]) : -2LL;
+        int bp = pos, bl = lane;
+        // segmented argmax: after the rounds with offsets 1, 2, 4, 8 each
+        // lane holds the best of positions [r, r + 2^rounds) mod NV
+#pragma unroll
+        for (int o = 0, off = 1; o < Cfg::ROUNDS; ++o, off <<= 1) {
+          const int rr = r + off;
+          const int src = base + (rr >= NV ? rr - NV : rr);
+          const long long ok = __shfl_sync(0xffffffffu, bk, src);
+          const int op = __shfl_sync(0xffffffffu, bp, src);
+          const int ol = __shfl_sync(0xffffffffu, bl, src);
+          if (ok > bk || (ok == bk && op < bp)) {
+            bk = ok;
+            bp = op;
+            bl = ol;
+          }
+        }
+        if (bk == 0 && act) singular = true;
+        if (r == k) mypiv = bp;
+        const bool is_piv = lane == bl;
+        const double pv = __shfl_sync(0xffffffffu, a[k], bl);
+        const double inv = 1.0 / pv;
+        const double m = is_piv ? 0.0 : a[k] * inv;
+        if (elig && !is_piv) lu[k] = m;  // getrf's multiplier
+        if (is_piv) {
+#pragma unroll
+          for (int j = k; j < NV; ++j) lu[j] = a[j];  // getrf's U row
+          myinv = inv;
+          myk = k;
+        }
+#pragma unroll
+        for (int j = k + 1; j < NC; ++j) {
+          const double pj = __shfl_sync(0xffffffffu, a[j], bl);
+          a[j] = fma(-m, pj, a[j]);
+        }
+        if (pos == k) pos = bp;
+        if (is_piv) {
+          pos = k;
+          elig = false;
+        }
+      }
+      if (act) {
+        // factors in getrf's row order (position myk), pivots as swaps
+        double* __restrict__ wf = w + myk * NV;
+#pragma unroll
+        for (int j = 0; j < NV; ++j) wf[j] = lu[j];
+        w[NN + NV + r] = (double)mypiv;
+      }
+      // row myk of S_i | t_i, for the next row's update (and x_{N-1})
+      const double tk = a[2 * NV] * myinv;
+      if (seg < P) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) st[myk * RS + j] = a[NV + j] * myinv;
+        st[myk * RS + NV] = tk;
+      }
+      if (act && i == N - 1) X[row * NV + myk] = tk;
+      __syncwarp();
+      if (i == N - 1) xlast = st[r * RS + NV];  // x_{N-1}, variable order
+    }
+    // ---- backward sweep: x_i = C'_i^-1 (b'_i - U_i x_{i+1})
+    double x = xlast;
+    for (int i = nmax - 2; i >= 0; --i) {
+      const bool act = i <= N - 2;
+      const int64_t row = r0 + i;
+      const double* __restrict__ w = work + row * WROW;
+      double f[NV], v = 0.0, d = 1.0;
+      int perm_src = r;
+      if (act) {
+        v = w[NN + r];
+#pragma unroll
+        for (int j = 0; j < NV; ++j) f[j] = w[r * NV + j];
+        d = f[0];
+#pragma unroll
+        for (int j = 1; j < NV; ++j)
+          if (j == r) d = f[j];
+        // original row held at position r after getrf's swaps
+        int j = r;
+#pragma unroll
+        for (int k = NV - 1; k >= 0; --k) {
+          const int pk = (int)w[NN + NV + k];
+          if (j == k)
+            j = pk;
+          else if (j == pk)
+            j = k;
+        }
+        perm_src = j;
+      } else {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) f[j] = 0.0;
+      }
+      // v_r = b'_r - (U_i x_{i+1})_r in original order; every lane takes
+      // part in the shuffles
+      {
+        const double* __restrict__ Ui = Um + (act ? row : 0) * NN + r * NV;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          const double xk = __shfl_sync(0xffffffffu, x, base + k);
+          if (act) v = fma(-__ldg(Ui + k), xk, v);
+        }
+      }
+      double y = __shfl_sync(0xffffffffu, v, base + perm_src);
+      // unit lower: y_r -= L[r][k] y_k, k < r
+#pragma unroll
+      for (int k = 0; k < NV - 1; ++k) {
+        const double yk = __shfl_sync(0xffffffffu, y, base + k);
+        if (r > k) y = fma(-f[k], yk, y);
+      }
+      // upper: x_r = (y_r - sum_{k > r} U[r][k] x_k) / U[r][r]
+      const double inv = 1.0 / d;
+#pragma unroll
+      for (int k = NV - 1; k >= 0; --k) {
+        if (r == k) y *= inv;
+        const double xk = __shfl_sync(0xffffffffu, y, base + k);
+        if (r < k) y = fma(-f[k], xk, y);
+      }
+      x = y;
+      if (act) X[row * NV + r] = x;
+    }
+    if (singular && status) atomicOr(status, 1);
+  }
+}
+
+template <int NV>
+int launch_seg(const double* L, const double* C, const double* U,
+               const double* b, double* x, const int64_t* row_off,
+               const int* order, int nsys, double* work, int* counter,
+               int* status, int ctas, cudaStream_t stream) {
+  if (ctas <= 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, k_block_thomas_seg<NV>, kSegWarps * 32, 0) !=
+            cudaSuccess ||
+        per_sm < 1) {
+      (void)cudaGetLastError();
+      per_sm = 1;
+    }
+    ctas = per_sm * pyro_sm_count();
+  }
+  const int per_cta = kSegWarps * SegCfg<NV>::P;
+  const int need = (nsys + per_cta - 1) / per_cta;
+  if (ctas > need) ctas = need;
+  if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  k_block_thomas_seg<NV><<<ctas, kSegWarps * 32, 0, stream>>>(
+      L, C, U, b, x, row_off, order, nsys, work, counter, status);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+}  // namespace
+
+// pyro_block_thomas for blocks of size nv <= 16 with 32 / nv systems per
+// warp, one lane per block row (see above).  Same arguments and workspace
+// layout as pyro_block_thomas; the CTA size is fixed (128 threads); ctas:
+// persistent grid (0 = all resident).
+PYRO_EXPORT int pyro_block_thomas_seg(const double* L, const double* C,
+                                      const double* U, const double* b,
+                                      double* x, const int64_t* row_off,
+                                      const int* order, int nsys, int nv,
+                                      double* work, int* counter, int* status,
+                                      int ctas, cudaStream_t stream) {
+  if (nsys < 0 || nv < 1 || nv > 16) return PYRO_ERR_ARGUMENT;
+  if (nsys == 0) return PYRO_OK;
+  if (!L || !C || !U || !b || !x || !row_off || !order || !work || !counter)
+    return PYRO_ERR_ARGUMENT;
+  switch (nv) {
+#define PYRO_BT_SEG(NV)                                                      \
+  case NV:                                                                   \
+    return launch_seg<NV>(L, C, U, b, x, row_off, order, nsys, work,         \
+                          counter, status, ctas, stream);
+    PYRO_BT_SEG(1) PYRO_BT_SEG(2) PYRO_BT_SEG(3) PYRO_BT_SEG(4)
+    PYRO_BT_SEG(5) PYRO_BT_SEG(6) PYRO_BT_SEG(7) PYRO_BT_SEG(8)
+    PYRO_BT_SEG(9) PYRO_BT_SEG(10) PYRO_BT_SEG(11) PYRO_BT_SEG(12)
+    PYRO_BT_SEG(13) PYRO_BT_SEG(14) PYRO_BT_SEG(15) PYRO_BT_SEG(16)
+#undef PYRO_BT_SEG
     default:
       return PYRO_ERR_ARGUMENT;
   }
@@ -688,7 +1012,8 @@ __global__ void __launch_bounds__(32 * kResolveWarps)
                            const int64_t* __restrict__ row_off,
                            const int* __restrict__ order, int nsys, int nv,
                            const double* __restrict__ work,
-                           int* __restrict__ counter) {
+                           int* __restrict__ counter,
+                           int* __restrict__ status) {
   __shared__ double s_vec[kResolveWarps][2 * NRHS * 64 + 96];
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   double* y = s_vec[wid];            // current vector
@@ -702,7 +1027,12 @@ __global__ void __launch_bounds__(32 * kResolveWarps)
     if (q >= nsys) break;
     const int s = order[q];
     const int64_t r0 = row_off[s];
-    const int N = (int)(row_off[s + 1] - r0);
+    const int64_t n64 = row_off[s + 1] - r0;
+    if (n64 <= 0) {  // an empty row range: skipped and flagged
+      if (lane == 0 && status) atomicOr(status, 2);
+      continue;
+    }
+    const int N = (int)n64;
     // forward
     for (int i = 0; i < N; ++i) {
       const int64_t row = r0 + i;
@@ -761,12 +1091,13 @@ template <int NRHS>
 int launch_resolve(const double* L, const double* U, const double* B,
                    double* X, int64_t rhs_stride, const int64_t* row_off,
                    const int* order, int nsys, int nv, const double* work,
-                   int* counter, cudaStream_t stream) {
+                   int* counter, int* status, cudaStream_t stream) {
   int blocks = (nsys + kResolveWarps - 1) / kResolveWarps;
   const int cap = pyro_sm_count() * 16;
   if (blocks > cap) blocks = cap;
   k_block_thomas_resolve<NRHS><<<blocks, 32 * kResolveWarps, 0, stream>>>(
-      L, U, B, X, rhs_stride, row_off, order, nsys, nv, work, counter);
+      L, U, B, X, rhs_stride, row_off, order, nsys, nv, work, counter,
+      status);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
@@ -775,13 +1106,14 @@ int launch_resolve(const double* L, const double* U, const double* B,
 
 // nrhs (1..4) right-hand sides B[c][rows][nv] (c-th at B + c * rhs_stride)
 // -> X[c][rows][nv] for the systems whose factors a previous
-// pyro_block_thomas / pyro_block_thomas_small call with the same L, C, U
-// left in `work`.  order, counter as for pyro_block_thomas (counter zeroed
-// here); nv <= 64.  B and X must not overlap.  Asynchronous on `stream`.
+// pyro_block_thomas / _small / _seg call with the same L, C, U left in
+// `work`.  order, counter as for pyro_block_thomas (counter zeroed here);
+// status (may be NULL): bit 1 for an empty row range; nv <= 64.  B and X
+// must not overlap.  Asynchronous on `stream`.
 PYRO_EXPORT int pyro_block_thomas_resolve(
     const double* L, const double* U, const double* B, double* X,
     int nrhs, int64_t rhs_stride, const int64_t* row_off, const int* order,
-    int nsys, int nv, const double* work, int* counter,
+    int nsys, int nv, const double* work, int* counter, int* status,
     cudaStream_t stream) {
   if (nsys < 0 || nv < 1 || nv > 64 || nrhs < 1 || nrhs > 4)
     return PYRO_ERR_ARGUMENT;
@@ -794,16 +1126,16 @@ PYRO_EXPORT int pyro_block_thomas_resolve(
   switch (nrhs) {
     case 1:
       return launch_resolve<1>(L, U, B, X, rhs_stride, row_off, order, nsys,
-                               nv, work, counter, stream);
+                               nv, work, counter, status, stream);
     case 2:
       return launch_resolve<2>(L, U, B, X, rhs_stride, row_off, order, nsys,
-                               nv, work, counter, stream);
+                               nv, work, counter, status, stream);
     case 3:
       return launch_resolve<3>(L, U, B, X, rhs_stride, row_off, order, nsys,
-                               nv, work, counter, stream);
+                               nv, work, counter, status, stream);
     default:
       return launch_resolve<4>(L, U, B, X, rhs_stride, row_off, order, nsys,
-                               nv, work, counter, stream);
+                               nv, work, counter, status, stream);
   }
 }
 

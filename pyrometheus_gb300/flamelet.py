@@ -36,10 +36,11 @@ class BlockThomasSolver:
     ``nv x nv`` blocks.
 
     ``kernel``: ``"cta"`` (one CTA per system, threads over matrix
-    elements; any nv <= 64) or ``"small"`` (one thread per system, nv <=
+    elements; any nv <= 64), ``"seg"`` (32 // nv systems per warp, one lane
+    per block row; nv <= 16) or ``"small"`` (one thread per system, nv <=
     16); ``threads``: CTA size (``"cta"``: a multiple of 32; ``"small"``:
-    32 or 64 systems per CTA); both ``None`` pick from the autotuner cache
-    or a size rule.  ``ctas``: persistent grid of the ``"cta"`` kernel (0:
+    32 or 64 systems per CTA; ``"seg"``: fixed at 128); both ``None`` pick
+    from the autotuner cache or a size rule.  ``ctas``: persistent grid of the ``"cta"`` kernel (0:
     all resident CTAs); ``use_graph``: capture the launch in a CUDA graph on
     the first :meth:`solve` with given buffers and replay it afterwards.
     """
@@ -71,13 +72,16 @@ class BlockThomasSolver:
         if kernel is None and threads is None:
             kernel, threads = default_plan(self.nv)
         self.kernel = kernel or "cta"
-        if self.kernel not in ("cta", "small"):
+        if self.kernel not in ("cta", "small", "seg"):
             raise ValueError(f"unknown block-Thomas kernel {kernel!r}")
-        if self.kernel == "small" and self.nv > 16:
-            raise ValueError("the one-thread-per-system kernel takes nv <= 16")
-        self.threads = int(threads) if threads else (
-            _small_threads(self.nv) if self.kernel == "small"
-            else default_threads(self.nv))
+        if self.kernel in ("small", "seg") and self.nv > 16:
+            raise ValueError(f"the {self.kernel!r} kernel takes nv <= 16")
+        if self.kernel == "seg":
+            self.threads = 128
+        else:
+            self.threads = int(threads) if threads else (
+                _small_threads(self.nv) if self.kernel == "small"
+                else default_threads(self.nv))
         self.ctas = int(ctas)
         self.use_graph = bool(use_graph)
         self._graph = None
@@ -85,6 +89,15 @@ class BlockThomasSolver:
         self._factored = False
 
     def _launch(self, L, C, U, b, x, stream):
+        if self.kernel == "seg":
+            _check(self.lib.pyro_block_thomas_seg(
+                L.data_ptr(), C.data_ptr(), U.data_ptr(), b.data_ptr(),
+                x.data_ptr(), self.offsets.data_ptr(), self.order.data_ptr(),
+                self.nsys, self.nv, self.work.data_ptr(),
+                self.counter.data_ptr(), self.status.data_ptr(), self.ctas,
+                ctypes.c_void_p(stream.cuda_stream)),
+                "pyro_block_thomas_seg")
+            return
         if self.kernel == "small":
             _check(self.lib.pyro_block_thomas_small(
                 L.data_ptr(), C.data_ptr(), U.data_ptr(), b.data_ptr(),
@@ -169,21 +182,25 @@ class BlockThomasSolver:
                 L.data_ptr(), U.data_ptr(), Bv[c0].data_ptr(),
                 Xv[c0].data_ptr(), k, rows * nv, self.offsets.data_ptr(),
                 self.order.data_ptr(), self.nsys, nv, self.work.data_ptr(),
-                self.counter.data_ptr(), ctypes.c_void_p(stream.cuda_stream)),
+                self.counter.data_ptr(), self.status.data_ptr(),
+                ctypes.c_void_p(stream.cuda_stream)),
                 "pyro_block_thomas_resolve")
         return X
 
     def check_status(self):
-        if int(self.status.item()) != 0:
+        st = int(self.status.item())
+        if st != 0:
             self.status.zero_()
-            raise RuntimeError("block-Thomas: singular diagonal block")
+            if st & 1:
+                raise RuntimeError("block-Thomas: singular diagonal block")
+            raise RuntimeError("block-Thomas: a system with no rows")
 
 
 def default_threads(nv: int) -> int:
     """CTA size of the one-CTA-per-system kernel: from the autotuner cache
     when it holds one, else the sizes the autotuner picks on GB300."""
     best = _tuned().get(str(nv))
-    if best and not str(best).startswith("small"):
+    if best and str(best).startswith("cta:"):
         return int(str(best).split(":")[-1])
     # the autotuner's choices on GB300 for 4,096 systems of 64..1024 rows:
     # 128 threads at nv = 10, 256 at nv = 54
@@ -225,8 +242,9 @@ def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
              candidates=(32, 64, 96, 128, 192, 256, 384, 512),
              seed: int = 0, device=None, repeats: int = 3, lengths=None):
     """Time the solve for each kernel and CTA size (the CTA kernel at each
-    of *candidates*, and for nv <= 16 the one-thread-per-system kernel at 32
-    and 64 systems per CTA) on a seeded sample of systems of the given
+    of *candidates*, and for nv <= 16 the several-systems-per-warp kernel
+    and the one-thread-per-system kernel at 32 and 64 systems per CTA) on a
+    seeded sample of systems of the given
     shape (or on systems of the given *lengths*); store the fastest in the
     build directory's tuning file and return ``{"kernel:threads": ms}``."""
     rng = np.random.default_rng(seed)
@@ -250,6 +268,7 @@ def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
     plans = [("cta", th) for th in candidates
              if not (nv > th and th < 64) and not (nv <= 24 and th > 256)]
     if nv <= 16:
+        plans += [("seg", 128)]
         plans += [("small", th) for th in (32, 64)
                   if 3 * nv * (nv + 1) * 8 * th <= 227 * 1024]
     times = {}

@@ -147,9 +147,12 @@ def block_thomas_lib() -> ctypes.CDLL:
     lib.pyro_block_thomas_small.restype = I
     lib.pyro_block_thomas_small.argtypes = [P, P, P, P, P, P, P, I, I, P, P,
                                             I, P]
+    lib.pyro_block_thomas_seg.restype = I
+    lib.pyro_block_thomas_seg.argtypes = [P, P, P, P, P, P, P, I, I, P, P, P,
+                                          I, P]
     lib.pyro_block_thomas_resolve.restype = I
     lib.pyro_block_thomas_resolve.argtypes = [P, P, P, P, I, I64, P, P, I, I,
-                                              P, P, P]
+                                              P, P, P, P]
     return lib
 
 

@@ -60,7 +60,7 @@ def _solve_cuda(lengths, L, C, U, b, threads=None, use_graph=False,
 
 
 PLANS = [("cta", 32), ("cta", 64), ("cta", 128), ("small", 32),
-         ("small", 64)]
+         ("small", 64), ("seg", 128)]
 
 
 @pytest.mark.gpu
@@ -70,8 +70,8 @@ def test_cuda_block_thomas_golden(tag, plan):
     _cuda()
     lengths, L, C, U, b, x = _golden(tag)
     kernel, threads = plan
-    if kernel == "small" and C.shape[1] > 16:
-        pytest.skip("one thread per system takes nv <= 16")
+    if kernel in ("small", "seg") and C.shape[1] > 16:
+        pytest.skip(f"the {kernel!r} kernel takes nv <= 16")
     got, _, _ = _solve_cuda(lengths, L, C, U, b, threads=threads,
                             kernel=kernel)
     assert _rel(got, x) < 1e-12
@@ -92,6 +92,8 @@ def _residual(L, C, U, b, x):
 
 @pytest.mark.gpu
 @pytest.mark.parametrize("nv,kernel", [(10, "cta"), (10, "small"),
+                                       (10, "seg"), (1, "seg"), (3, "seg"),
+                                       (8, "seg"), (16, "seg"),
                                        (54, "cta")])
 def test_cuda_block_thomas_uneven_batch(nv, kernel):
     """Against the reference algorithm on long systems.  The two round
@@ -135,3 +137,92 @@ def test_cuda_graph_replay_and_single_system_api():
     n = int(lengths[0])
     xs = bt_gpu(L[:n - 1], C[:n], U[:n - 1], b[:n]).cpu().numpy()
     assert _rel(xs, ref[:n]) < 1e-12
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", ["cta", "small", "seg"])
+def test_empty_systems_are_skipped_and_flagged(kernel):
+    """A system with an empty row range is skipped with status bit 1 and
+    writes nothing.  The empty systems sit right after non-empty ones in
+    the packing (offsets 0, 5, 5, 12, 12, 20), so a kernel that ran their
+    backward sweep anyway would overwrite the last row of the system before
+    them, inside the buffers: that row must still hold its solution.  The
+    re-solve with the kept factors skips them the same way."""
+    _cuda()
+    import ctypes
+
+    from pyrometheus_gb300 import native
+    lib = native.block_thomas_lib()
+    nv = 10
+    real = np.array([5, 7, 8])
+    lengths = np.array([5, 0, 7, 0, 8])
+    rows = int(real.sum())
+    rng = np.random.default_rng(18)
+    L, C, U = (rng.standard_normal((rows, nv, nv)) for _ in range(3))
+    C += 10.0 * np.eye(nv)
+    b = rng.standard_normal((rows, nv))
+    ref = solve_packed(real, L, C, U, b)
+    dev = torch.device("cuda")
+    t = [torch.as_tensor(a, device=dev).contiguous() for a in (L, C, U, b)]
+    offs = torch.as_tensor(np.concatenate([[0], np.cumsum(lengths)]),
+                           dtype=torch.int64, device=dev)
+    # the empty systems first, where a longest-first order would not put
+    # them
+    order = torch.as_tensor([1, 3, 4, 2, 0], dtype=torch.int32, device=dev)
+    work = torch.empty(int(lib.pyro_block_thomas_work_doubles(nv, rows)),
+                       dtype=torch.float64, device=dev)
+    counter = torch.zeros(1, dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    x = torch.full_like(t[3], float("nan"))
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    args = [a.data_ptr() for a in t] + [x.data_ptr(), offs.data_ptr(),
+                                        order.data_ptr(), 5, nv,
+                                        work.data_ptr()]
+    if kernel == "cta":
+        st = lib.pyro_block_thomas(*args, counter.data_ptr(),
+                                   status.data_ptr(), 64, 0, sp)
+    elif kernel == "small":
+        st = lib.pyro_block_thomas_small(*args, status.data_ptr(), 32, sp)
+    else:
+        st = lib.pyro_block_thomas_seg(*args, counter.data_ptr(),
+                                       status.data_ptr(), 0, sp)
+    assert st == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 2
+    assert _rel(x.cpu().numpy(), ref) < 1e-12
+    # re-solve with the kept factors: the same skip and flag
+    b2 = torch.as_tensor(rng.standard_normal((rows, nv)), device=dev)
+    x2 = torch.full_like(b2, float("nan"))
+    status.zero_()
+    assert lib.pyro_block_thomas_resolve(
+        t[0].data_ptr(), t[2].data_ptr(), b2.data_ptr(), x2.data_ptr(), 1,
+        0, offs.data_ptr(), order.data_ptr(), 5, nv, work.data_ptr(),
+        counter.data_ptr(), status.data_ptr(), sp) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 2
+    ref2 = solve_packed(real, L, C, U, b2.cpu().numpy())
+    assert _rel(x2.cpu().numpy(), ref2) < 1e-12
+
+
+@pytest.mark.gpu
+def test_seg_kernel_workspace_serves_resolve_and_matches_cta():
+    """The several-systems-per-warp kernel keeps getrf's factors and pivots
+    in the shared workspace layout: re-solves from its workspace equal
+    fresh solves, and its solution equals the CTA kernel's to rounding."""
+    _cuda()
+    from pyrometheus_gb300.flamelet import BlockThomasSolver
+    lengths, L, C, U, b = make_systems(97, 10, 1, 90, seed=23)
+    dev = torch.device("cuda")
+    t = [torch.as_tensor(a, device=dev).contiguous() for a in (L, C, U, b)]
+    seg = BlockThomasSolver(10, lengths, kernel="seg")
+    cta = BlockThomasSolver(10, lengths, kernel="cta", threads=64)
+    xs = seg.solve(*t).cpu().numpy()
+    xc = cta.solve(*t).cpu().numpy()
+    seg.check_status()
+    assert _rel(xs, xc) < 1e-13
+    rng = np.random.default_rng(24)
+    B = torch.as_tensor(rng.standard_normal((3,) + b.shape), device=dev)
+    X = seg.resolve(t[0], t[2], B).cpu().numpy()
+    for c in range(3):
+        ref = solve_packed(lengths, L, C, U, B[c].cpu().numpy())
+        assert _rel(X[c], ref) < 1e-12

@@ -96,3 +96,36 @@ def test_noalloc_rejects_sizes_beyond_its_scratch():
     st = lib.pyro_block_thomas_noalloc(1, 1, 1, 1, 1, 1, 1, 1, nv, too_many,
                                        None, 128, 0, None)
     assert st == PYRO_ERR_CAPACITY
+
+
+def test_noalloc_skips_systems_past_the_stated_rows():
+    """If the host's total_rows is smaller than the packed offsets say, the
+    systems reaching past it are skipped (status bit 1) instead of writing
+    past the static scratch; the others still match the allocating entry
+    point and the skipped rows of x keep what they held."""
+    lib = _lib()
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    nv, nsys = 10, 6
+    lengths, (L, C, U, b), offs, order = _device_systems(nsys, nv, 31)
+    rows = int(lengths.sum())
+    head = rows - int(lengths[-1])
+    work = torch.empty(int(lib.pyro_block_thomas_work_doubles(nv, rows)),
+                       dtype=torch.float64, device="cuda")
+    counter = torch.zeros(1, dtype=torch.int32, device="cuda")
+    x_ref = torch.empty_like(b)
+    assert lib.pyro_block_thomas(
+        L.data_ptr(), C.data_ptr(), U.data_ptr(), b.data_ptr(),
+        x_ref.data_ptr(), offs.data_ptr(), order.data_ptr(), nsys, nv,
+        work.data_ptr(), counter.data_ptr(), None, 32, 0, sp) == 0
+    st = torch.zeros(1, dtype=torch.int32, device="cuda")
+    x = torch.full_like(b, float("nan"))
+    assert lib.pyro_block_thomas_noalloc(
+        L.data_ptr(), C.data_ptr(), U.data_ptr(), b.data_ptr(),
+        x.data_ptr(), offs.data_ptr(), order.data_ptr(), nsys, nv, head,
+        st.data_ptr(), 32, 0, sp) == 0
+    torch.cuda.synchronize()
+    assert int(st.item()) == 2
+    xr, xn = x_ref.cpu().numpy(), x.cpu().numpy()
+    assert np.abs(xn[:head] - xr[:head]).max() <= \
+        1e-12 * np.abs(xr[:head]).max()
+    assert np.isnan(xn[head:]).all()
