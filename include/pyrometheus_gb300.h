@@ -151,6 +151,18 @@ int pyro_reactor_jacobian(const double* p, int64_t p_inc, const double* T,
                           double* J, int64_t ldj, int64_t n,
                           cudaStream_t stream);
 
+/* The source and its Jacobian in one pass: F[S+1][ldf] as
+ * pyro_reactor_source and J as pyro_reactor_jacobian, from the rates the
+ * Jacobian kernel forms anyway.  Replaces the primal-and-tangent pair that
+ * jax.jacfwd(rhs) yields in one trace (examples/free_flame/reactors.py:
+ * 115-125, flamelets/equations.py:124-129) -- and the two separate calls
+ * a caller of the generated class would otherwise make. */
+int pyro_reactor_source_jacobian(const double* p, int64_t p_inc,
+                                 const double* T, int64_t t_inc,
+                                 const double* Y, int64_t ldy, double* F,
+                                 int64_t ldf, double* J, int64_t ldj,
+                                 int64_t n, cudaStream_t stream);
+
 /* Vector-Jacobian product v^T df/d(T, Y) and v^T df/dp for cotangents
  * V[S+1][ldv]: gT[n], gY[S][ldg], gp[n] (gp may be NULL); the reverse-mode
  * counterpart of jax.vjp over the same function. */

@@ -422,11 +422,15 @@ __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
 // doubles of shared memory per warp (JW_DOUBLES, from the tables):
 //   c, h, g, cp, w, jt, a, u, shj [NS each]; q, dq/dT, Hq, Qc [NR each];
 //   D = dq/dc per slot [NSLOT], dq/dM per reaction [NR], one zero.
+// With F non-null the kernel also writes the source f = (dT/dt, dY/dt)
+// [S+1][ldf] from the rates it forms anyway (the primal jacfwd returns with
+// the tangents, flamelets/equations.py:124-129): one pass for both.
 __global__ void __launch_bounds__(JWARPS * 32)
     k_reactor_jacobian(const double* __restrict__ Pp, int64_t p_inc,
                        const double* __restrict__ Tp, int64_t t_inc,
                        const double* __restrict__ Y, int64_t ldy,
-                       double* __restrict__ J, int64_t ldj, int64_t n) {
+                       double* __restrict__ J, int64_t ldj,
+                       double* __restrict__ F, int64_t ldf, int64_t n) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -553,6 +557,13 @@ __global__ void __launch_bounds__(JWARPS * 32)
     const double rcp = rho * cpm;
     const double inv_rcp = 1.0 / rcp;
     const double qr2 = Q * inv_rcp * inv_rcp;
+    if (F != nullptr) {
+      // dT/dt = -Q / (rho cp), dY_k/dt = W_k w_k / rho (the lane that
+      // formed w_k stores it)
+      if (lane == 0) F[i] = -Q * inv_rcp;
+      for (int k = lane; k < NS; k += 32)
+        F[(int64_t)(k + 1) * ldf + i] = __ldg(jg_mw + k) * sw[k] / rho;
+    }
     __syncwarp();
     // rows 1..S, columns 1..S: d(dY_k/dt)/dY_m = W_k/rho ((Jc + a_k) rho
     //   / W_m + (w_k - u_k) / (sigma W_m)) = (W_k Jc_km + B_k) / W_m with

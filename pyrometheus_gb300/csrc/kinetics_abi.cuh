@@ -298,6 +298,25 @@ PYRO_EXPORT int pyro_reactor_source_dp(const double* p, int64_t p_inc,
   return PYRO_OK;
 }
 
+namespace {
+int launch_reactor_jacobian(const double* p, int64_t p_inc, const double* T,
+                            int64_t t_inc, const double* Y, int64_t ldy,
+                            double* F, int64_t ldf, double* J, int64_t ldj,
+                            int64_t n, cudaStream_t stream) {
+  const size_t sm = (size_t)JWARPS * JW_DOUBLES * sizeof(double);
+  if (prepare_smem((const void*)k_reactor_jacobian, sm) != PYRO_OK)
+    return PYRO_ERR_LAUNCH;
+  const int64_t blocks = (n + JWARPS - 1) / JWARPS;
+  const int grid =
+      (int)(blocks < (int64_t)pyro_sm_count() * 8 ? blocks
+                                                   : (int64_t)pyro_sm_count() * 8);
+  k_reactor_jacobian<<<grid, JWARPS * 32, sm, stream>>>(
+      p, p_inc, T, t_inc, Y, ldy, J, ldj, F, ldf, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+}  // namespace
+
 PYRO_EXPORT int pyro_reactor_jacobian(const double* p, int64_t p_inc,
                                       const double* T, int64_t t_inc,
                                       const double* Y, int64_t ldy, double* J,
@@ -308,17 +327,21 @@ PYRO_EXPORT int pyro_reactor_jacobian(const double* p, int64_t p_inc,
   if (!p || !T || !Y || !J || ldy < n ||
       ldj < (int64_t)(NS + 1) * (NS + 1))
     return PYRO_ERR_ARGUMENT;
-  const size_t sm = (size_t)JWARPS * JW_DOUBLES * sizeof(double);
-  if (prepare_smem((const void*)k_reactor_jacobian, sm) != PYRO_OK)
-    return PYRO_ERR_LAUNCH;
-  const int64_t blocks = (n + JWARPS - 1) / JWARPS;
-  const int grid =
-      (int)(blocks < (int64_t)pyro_sm_count() * 8 ? blocks
-                                                   : (int64_t)pyro_sm_count() * 8);
-  k_reactor_jacobian<<<grid, JWARPS * 32, sm, stream>>>(p, p_inc, T, t_inc, Y,
-                                                        ldy, J, ldj, n);
-  PYRO_CHECK_LAUNCH();
-  return PYRO_OK;
+  return launch_reactor_jacobian(p, p_inc, T, t_inc, Y, ldy, nullptr, 0, J,
+                                 ldj, n, stream);
+}
+
+PYRO_EXPORT int pyro_reactor_source_jacobian(
+    const double* p, int64_t p_inc, const double* T, int64_t t_inc,
+    const double* Y, int64_t ldy, double* F, int64_t ldf, double* J,
+    int64_t ldj, int64_t n, cudaStream_t stream) {
+  if (n < 0) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  if (!p || !T || !Y || !F || !J || ldy < n || ldf < n ||
+      ldj < (int64_t)(NS + 1) * (NS + 1))
+    return PYRO_ERR_ARGUMENT;
+  return launch_reactor_jacobian(p, p_inc, T, t_inc, Y, ldy, F, ldf, J, ldj,
+                                 n, stream);
 }
 
 PYRO_EXPORT int pyro_reactor_vjp(const double* p, int64_t p_inc,

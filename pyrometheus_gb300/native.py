@@ -60,6 +60,9 @@ def peaks_lib() -> ctypes.CDLL:
     lib.pyro_measure_fp64.restype = ctypes.c_int
     lib.pyro_measure_fp64.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
                                       ctypes.c_int]
+    lib.pyro_measure_dmma.restype = ctypes.c_int
+    lib.pyro_measure_dmma.argtypes = [ctypes.c_void_p, ctypes.c_void_p,
+                                      ctypes.c_int]
     return lib
 
 
@@ -77,6 +80,17 @@ def measure_fp64(scratch, repeats: int = 3):
     if st != 0:
         raise RuntimeError(f"pyro_measure_fp64 failed (status {st})")
     return res[0], res[1], res[2]
+
+
+def measure_dmma(scratch, repeats: int = 3):
+    """(FP64 FLOP/s of ``mma.sync`` m8n8k4, of m16n8k16) on the current
+    device; *scratch* as for :func:`measure_fp64`."""
+    res = (ctypes.c_double * 2)()
+    st = peaks_lib().pyro_measure_dmma(ctypes.c_void_p(scratch.data_ptr()),
+                                       res, int(repeats))
+    if st != 0:
+        raise RuntimeError(f"pyro_measure_dmma failed (status {st})")
+    return res[0], res[1]
 
 
 def measure_fp64_rcp(scratch, repeats: int = 3) -> float:

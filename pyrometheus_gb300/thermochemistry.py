@@ -71,6 +71,8 @@ _SIGNATURES = {
                               _P],
     "pyro_reactor_source_dp": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _I64,
                                _P],
+    "pyro_reactor_source_jacobian": [_P, _I64, _P, _I64, _P, _I64, _P, _I64,
+                                     _P, _I64, _I64, _P],
     "pyro_reactor_vjp": [_P, _I64, _P, _I64, _P, _I64, _P, _I64, _P, _P,
                          _I64, _P, _I64, _P],
     "pyro_reactor_bdf2": [_P, _P, _P, _I64] + [_P] * 18 + [_I64, _INT, _D,
@@ -725,6 +727,38 @@ class CudaThermochemistryBase:
             out.data_ptr(), out.stride(0) if n > 1 else nc * nc, n,
             self._stream), "reactor Jacobian")
         return out[0] if single and n == 1 else out
+
+    def get_reactor_source_and_jacobian(self, pressure, temperature,
+                                        mass_fractions, out=None):
+        """``(f, J)``: the reactor source ``[S+1, N]`` (as
+        :meth:`get_reactor_source`) and its Jacobian ``[N, S+1, S+1]`` (as
+        :meth:`get_reactor_jacobian`) from one pass of the Jacobian kernel
+        -- the primal and tangents ``jax.jacfwd`` yields together
+        (``flamelets/equations.py:124-129``).  *out*: optional ``(f, J)``
+        tensors to fill (``f`` with unit stride along N)."""
+        pv, tv, ym, n, single = self._reactor_args(pressure, temperature,
+                                                   mass_fractions)
+        nc = self.num_species + 1
+        if out is None:
+            f = self._out(nc, n)
+            jac = torch.empty((n, nc, nc), dtype=torch.float64,
+                              device=self.device)
+        else:
+            f, jac = out
+        if (tuple(jac.shape) != (n, nc, nc) or jac.stride(2) != 1
+                or jac.stride(1) != nc):
+            raise ValueError("J must be a [N, S+1, S+1] row-major tensor")
+        if tuple(f.shape) != (nc, n) or f.stride(1) != 1:
+            raise ValueError("f must be a [S+1, N] tensor with unit stride "
+                             "along N")
+        _check(self._lib.pyro_reactor_source_jacobian(
+            pv.ptr, pv.inc, tv.ptr, tv.inc, ym.data_ptr(), ym.stride(0),
+            f.data_ptr(), max(f.stride(0), n), jac.data_ptr(),
+            jac.stride(0) if n > 1 else nc * nc, n, self._stream),
+            "reactor source and Jacobian")
+        if single and n == 1:
+            return self._shape_rows(f, True), jac[0]
+        return f, jac
 
     def get_reactor_vjp(self, pressure, temperature, mass_fractions,
                         cotangent):

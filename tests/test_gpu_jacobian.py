@@ -55,6 +55,34 @@ def test_source_and_jacobian_against_reference_autodiff(name):
         not np.isfinite(g["jac"]).all()
 
 
+@pytest.mark.parametrize("name", GOLDEN_SETS)
+def test_fused_source_and_jacobian(name):
+    """One pass for the source and its Jacobian (the primal and tangents of
+    the reference's jacfwd): the same Jacobian as the Jacobian-only entry
+    point bit for bit, and the source against the reference's golden one
+    and the source kernel."""
+    sol, g = load_golden(name)
+    th = _cls(sol)()
+    n = g["jac"].shape[0]
+    p, t, y = g["P"][:n], g["T"][:n], g["Y"][:, :n]
+    f, jac = th.get_reactor_source_and_jacobian(p, t, y)
+    assert torch.equal(jac, th.get_reactor_jacobian(p, t, y))
+    ref = g["reactor_source"]
+    f = f.cpu().numpy()
+    assert np.abs(f - ref).max() <= 1e-12 * np.abs(ref).max()
+    f_sep = th.get_reactor_source(p, t, y).cpu().numpy()
+    assert np.abs(f - f_sep).max() <= 1e-13 * np.abs(f_sep).max()
+    # into caller buffers, with a leading dimension beyond N
+    nc = sol.n_species + 1
+    fb = torch.full((nc, n + 5), float("nan"), dtype=torch.float64,
+                    device="cuda")
+    jb = torch.empty((n, nc, nc), dtype=torch.float64, device="cuda")
+    th.get_reactor_source_and_jacobian(p, t, y, out=(fb[:, :n], jb))
+    assert np.array_equal(fb[:, :n].cpu().numpy(), f)
+    assert torch.isnan(fb[:, n:]).all()
+    assert torch.equal(jb, jac)
+
+
 def test_jacobian_order_of_convergence_like_reference():
     """Central differences of the oracle source converge to the CUDA
     Jacobian at second order (test/test.py:360-374)."""
