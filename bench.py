@@ -268,6 +268,46 @@ def run_reference(args):
 # }}}
 
 
+PARITY_REL = 1e-12
+PARITY_T_K = 1e-10
+
+
+def headline_parity(sol, t, p, y, e, w, tn, m=8192):
+    """The timed step's own output, checked: *m* seeded random states of
+    the last timed step's ``wdot`` and ``T`` against the CPU oracle (net
+    production rates at the creation + destruction scale, 1e-12; the
+    temperature within 1e-10 K of the oracle's Newton, which also recovers
+    the states' own temperatures, the energies having been computed from
+    them)."""
+    import numpy as np
+    import torch
+
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    n = t.shape[0]
+    idx = np.sort(np.random.default_rng(4242).choice(n, size=min(m, n),
+                                                     replace=False))
+    orc = Oracle(sol)
+    ts, ps, ys, es = t[idx], p[idx], y[:, idx], e[idx]
+    rho = orc.get_density(ps, ts, ys)
+    w_ref = orc.get_net_production_rates(rho, ts, ys)
+    cd, dd = orc.get_creation_destruction_rates(rho, ts, ys)
+    t_ref = orc.get_temperature(es, 1500.0, ys, do_energy=True)
+    ii = torch.as_tensor(idx, device=w.device)
+    wg = w[:, ii].cpu().numpy()
+    tg = tn[ii].cpu().numpy()
+    d = np.abs(wg - w_ref)
+    scale = np.maximum(np.abs(w_ref), cd + dd)
+    rel = float(np.where(d == 0, 0.0, d / np.where(scale == 0, 1.0,
+                                                   scale)).max())
+    dT = float(np.abs(tg - t_ref).max())
+    return {"states": int(idx.size), "max_rel": rel, "max_dT_K": dT,
+            "max_dT_vs_state_K": float(np.abs(tg - ts).max()),
+            "tol_rel": PARITY_REL, "tol_T_K": PARITY_T_K,
+            "scale": "max(|x_ref|, creation + destruction)",
+            "checked": "last timed step's wdot and T against the oracle",
+            "pass": bool(rel <= PARITY_REL and dT <= PARITY_T_K)}
+
+
 def newton_iterations(sol, t, y, e, t0=1500.0, tol=1e-6):
     """Mean per-state Newton iterations of the fused step on a sample
     (the same update as the kernel)."""
@@ -450,7 +490,7 @@ def secondary_legs(sol, th, dev, dfma):
     import numpy as np
     import torch
 
-    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300 import opcount, synthetic
     from pyrometheus_gb300.flamelet import BlockThomasSolver, autotune
     out = {}
     n = 1 << 20
@@ -459,19 +499,49 @@ def secondary_legs(sol, th, dev, dfma):
     P = torch.as_tensor(p, device=dev)
     Y = torch.as_tensor(y, device=dev)
     nc = sol.n_species + 1
-    J = torch.empty((n, nc, nc), dtype=torch.float64, device=dev)
-    ms_j = _event_ms(lambda: th.get_reactor_jacobian(P, T, Y, out=J), 2)
-    del J
-    V = torch.randn((nc, n), dtype=torch.float64, device=dev,
-                    generator=torch.Generator(device=dev).manual_seed(1))
-    ms_v = _event_ms(lambda: th.get_reactor_vjp(P, T, Y, V), 2)
-    out["jacobian"] = {
-        "states": n, "ms": ms_j, "states_per_s": n / ms_j * 1e3,
-        "output_bytes_per_state": nc * nc * 8,
-        "output_gbs": n * nc * nc * 8 / ms_j / 1e6}
+    f64 = dict(dtype=torch.float64, device=dev)
+    J = torch.empty((n, nc, nc), **f64)
+    F = torch.empty((nc, n), **f64)
+    ms_fused = _event_ms(lambda: th.get_reactor_source_and_jacobian(
+        P, T, Y, out=(F, J)), 3)
+    jac_parity = source_jacobian_parity(sol, t, p, y, F, J)
+
+    def plain():
+        # the plain per-call path: the source and the Jacobian as two
+        # separate calls of the class (two launches)
+        th.get_reactor_source(P, T, Y)
+        th.get_reactor_jacobian(P, T, Y, out=J)
+
+    ms_plain = _event_ms(plain, 3)
+    ms_j = _event_ms(lambda: th.get_reactor_jacobian(P, T, Y, out=J), 3)
+    del J, F
+    V = torch.randn((nc, n), generator=torch.Generator(
+        device=dev).manual_seed(1), **f64)
+    ms_v = _event_ms(lambda: th.get_reactor_vjp(P, T, Y, V), 3)
+    fl_j = opcount.weighted_flops(opcount.jacobian_counts(sol),
+                                  opcount.FIXED_WEIGHTS)
+    fl_v = opcount.weighted_flops(opcount.vjp_counts(sol),
+                                  opcount.FIXED_WEIGHTS)
+    out["source_jacobian"] = {
+        "states": n, "ms": ms_fused, "states_per_s": n / ms_fused * 1e3,
+        "what": "f = (dT/dt, dY/dt) [S+1, N] and J = df/d(T, Y) "
+                "[N, S+1, S+1] in one pass (pyro_reactor_source_jacobian)",
+        "plain_per_call_ms": ms_plain,
+        "plain_per_call": "get_reactor_source then get_reactor_jacobian "
+                          "(two launches)",
+        "fused_over_plain": ms_plain / ms_fused,
+        "jacobian_only_ms": ms_j,
+        "roofline": _fp64_roofline(fl_j, n, ms_fused, dfma,
+                                   "opcount.jacobian_counts"),
+        "hbm": {"bytes_per_state": (nc * nc + 2 * nc + 1) * 8,
+                "achieved_gbs": n * (nc * nc + 2 * nc + 1) * 8
+                / ms_fused / 1e6},
+        "parity": jac_parity}
     out["vjp"] = {"states": n, "ms": ms_v, "states_per_s": n / ms_v * 1e3,
-                  "cotangents": "N(0,1), seeded"}
-    out["jacobian"]["cpu_baseline"], out["vjp"]["cpu_baseline"] = \
+                  "cotangents": "N(0,1), seeded",
+                  "roofline": _fp64_roofline(fl_v, n, ms_v, dfma,
+                                             "opcount.vjp_counts")}
+    out["source_jacobian"]["cpu_baseline"], out["vjp"]["cpu_baseline"] = \
         jacobian_cpu_baseline(sol, t, p, y)
     del V
     out["transport"] = transport_leg(sol, th, dev, dfma, t, p, y, T, P, Y)
@@ -516,6 +586,45 @@ def secondary_legs(sol, th, dev, dfma):
     out["flamelet_newton"] = flamelet_newton_legs(dev, dfma)
     out["eos_adjoint"] = eos_adjoint_legs(dev)
     return out
+
+
+def _fp64_roofline(flops_per_state, n, ms, dfma, model):
+    """FP64 roofline of a rate-type leg: the fixed-weight algorithmic flops
+    (transcendentals at opcount.FIXED_WEIGHTS) per state times the states,
+    over the CUDA-event time, against the live DFMA peak."""
+    achieved = flops_per_state * n / (ms * 1e-3)
+    return {"bound": "fp64", "achieved": achieved / 1e12,
+            "peak": dfma / 1e12, "unit": "TFLOP/s", "frac": achieved / dfma,
+            "flops_per_state": flops_per_state,
+            "flop_model": model + " (exp/log/log10/10^x 20 flops, pow 40)",
+            "peak_source": "DFMA throughput measured live by bench.py"}
+
+
+def source_jacobian_parity(sol, t, p, y, F, J, m=256):
+    """The fused leg's output, checked on *m* seeded states: the source
+    against the oracle's (row-scaled, 1e-12) and the Jacobian against the
+    oracle's central differences (relative steps 1e-7; row-scaled, within
+    the differences' own accuracy, 1e-6)."""
+    import numpy as np
+    import torch
+
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    n = t.shape[0]
+    idx = np.sort(np.random.default_rng(77).choice(n, size=m,
+                                                   replace=False))
+    ii = torch.as_tensor(idx, device=F.device)
+    o = Oracle(sol)
+    f_ref = o.reactor_source(p[idx], t[idx], y[:, idx])
+    f = F[:, ii].cpu().numpy()
+    fs = np.abs(f_ref).max(axis=1, keepdims=True)
+    f_err = float((np.abs(f - f_ref) / np.where(fs == 0, 1, fs)).max())
+    j_ref = o.reactor_jacobian_fd(p[idx], t[idx], y[:, idx])
+    j = J[ii].cpu().numpy()
+    js = np.abs(j_ref).max(axis=2, keepdims=True)
+    j_err = float((np.abs(j - j_ref) / np.where(js == 0, 1, js)).max())
+    return {"states": m, "source_max_rel_row": f_err, "source_tol": 1e-12,
+            "jacobian_max_rel_row_vs_fd": j_err, "jacobian_tol": 1e-6,
+            "pass": bool(f_err <= 1e-12 and j_err <= 1e-6)}
 
 
 def transport_leg(sol, th, dev, dfma, t, p, y, T, P, Y):
@@ -867,6 +976,8 @@ def run_gb300(args):
     if rank != 0:
         return
 
+    parity = headline_parity(sol, t, p, y, E_h.numpy(), w, tn)
+
     # roofline: FP64 pipe (the bound) and HBM (for context)
     scratch = torch.empty(int(native.peaks_scratch_doubles()),
                           dtype=torch.float64, device=dev)
@@ -878,6 +989,8 @@ def run_gb300(args):
     counts = opcount.fused_step_counts(sol, iters)
     flops_state = opcount.weighted_flops(counts, weights)
     achieved = flops_state * n / (ms_per_step * 1e-3)
+    fixed_state = opcount.weighted_flops(counts, opcount.FIXED_WEIGHTS)
+    fixed_achieved = fixed_state * n / (ms_per_step * 1e-3)
     bps = opcount.bytes_per_state(sol)
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -918,6 +1031,15 @@ def run_gb300(args):
             "peak_source": "DFMA throughput measured live by bench.py "
                            "(MEASURED_PEAKS.json has no FP64 figure)",
             "flops_per_state": flops_state,
+            "algorithmic": {
+                "flops_per_state": fixed_state,
+                "achieved": fixed_achieved / 1e12,
+                "frac": fixed_achieved / dfma,
+                "weights": "every exp/log/log10/10^x 20 flops, pow 40, "
+                           "whatever the kernel's own implementation "
+                           "costs (frac above counts each transcendental "
+                           "at the FP64 work of the kernel's table "
+                           "methods: an FP64-pipe utilisation)"},
             "flop_model": {"arith_flops": counts["flops"],
                            "transcendentals": {k: counts[k] for k in
                                                opcount.TRANSCENDENTALS},
@@ -928,11 +1050,16 @@ def run_gb300(args):
                 "peak_gbs": hbm_peak, "frac": hbm_achieved / hbm_peak,
                 "peak_source": hbm_src},
         "cpu_baseline": base,
+        "parity": parity,
         "clocks": clk,
     }
     if extra is not None:
         out["secondary"] = extra
-    print(json.dumps(out))
+    print(json.dumps(out), flush=True)
+    if not parity["pass"]:
+        raise SystemExit("bench: the timed output disagrees with the oracle "
+                         f"(max rel {parity['max_rel']:.3g}, max |dT| "
+                         f"{parity['max_dT_K']:.3g} K)")
 
 
 def main():

@@ -214,3 +214,72 @@ def bytes_per_state(sol) -> int:
     """HBM bytes per state of the fused step: p, T, Y, e in; wdot, T out."""
     S = sol.n_species
     return 8 * (2 + S + 1) + 8 * (S + 1)
+
+
+#: Constant per-call weights (flops) of the transcendentals for the
+#: implementation-independent algorithmic count: every exp, log, log10 and
+#: 10^x is charged 20 flops, pow 40 (a log and an exp), whatever the
+#: kernels' own implementations cost, so a faster exp or log does not lower
+#: the counted work.
+FIXED_WEIGHTS = {"exp": 20.0, "exp10": 20.0, "log": 20.0, "log10": 20.0,
+                 "pow": 40.0}
+
+
+def _rate_derivative_counts(sol, c: Counter):
+    """Per-reaction work shared by the Jacobian and the VJP: d ln kf/dT and
+    d ln K/dT (2 flops per species slot + 4), dq/dT and dq/d[M] (10), the
+    Troe blending's T and Pr derivatives (30 and one log10 per Troe
+    reaction) and dq/dc per slot (the product of the other slots and a
+    multiply); returns the slot counts per reaction."""
+    m = _tables(sol)
+    slots = []
+    for r in m.rx:
+        ns = len(r.nu_r) + len(r.nu_p)
+        c["flops"] += 2 * ns + 4 + 10 + ns * (ns + 1)
+        if r.kind == "falloff" and r.ftype == "Troe":
+            c["flops"] += 30
+            c["log10"] += 1
+        slots.append((r, ns))
+    return slots
+
+
+def jacobian_counts(sol) -> Counter:
+    """Per-state algorithmic work of the analytic reactor Jacobian
+    ``d(dT/dt, dY/dt)/d(T, Y)`` as ``k_reactor_jacobian`` forms it: the
+    rates of progress (:func:`production_rates_counts`) and their
+    derivatives, species thermo with d(cp/R)/dT (40 flops per species), one
+    FMA per (element, contribution) of the S x S block of dw/dc (the slot
+    pairs of every reaction and its third-body entries), the chain rule
+    through c(T, Y) and rho(T, Y) per element (3 flops), the per-species
+    sums (10 flops per slot incidence) and the dT/dt row (12 flops per
+    column) and column (5 per row)."""
+    m = _tables(sol)
+    S = m.S
+    c = Counter(production_rates_counts(sol))
+    entries = 0
+    for r, ns in _rate_derivative_counts(sol, c):
+        entries += ns * ns
+        if r.kind != "elementary":
+            entries += ns * sum(1 for e in r.eff.values()
+                                if e != r.default_eff)
+        c["flops"] += 10 * ns
+    c["flops"] += 40 * S + 2 * entries + 3 * S * S + 12 * (S + 1) + 5 * S
+    return c
+
+
+def vjp_counts(sol) -> Counter:
+    """Per-state algorithmic work of the reactor VJP ``v^T df/d(T, Y)``
+    (``k_reactor_vjp``, reverse accumulation): the rates and their
+    derivatives as for :func:`jacobian_counts` without the S x S block,
+    plus per slot the adjoint weight and the scatter of ``mu dq/dc`` (8
+    flops), per third-body entry one FMA, and per species the thermo and
+    closing sums (70 flops)."""
+    m = _tables(sol)
+    c = Counter(production_rates_counts(sol))
+    for r, ns in _rate_derivative_counts(sol, c):
+        c["flops"] += 8 * ns
+        if r.kind != "elementary":
+            c["flops"] += 2 * sum(1 for e in r.eff.values()
+                                  if e != r.default_eff) + 2
+    c["flops"] += 70 * m.S
+    return c
