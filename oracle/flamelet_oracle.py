@@ -5,14 +5,14 @@ imports it.
 
 A numpy restatement, for one flamelet on a uniform grid, of
 
-* ``FlameletEquations.rhs`` (``pyrometheus/flamelets/equations.py:193-238``):
+* ``FlameletEquations.rhs`` (``pyrometheus/flamelets/equations.py:167-227``):
   ``R = chi/2 Lap(phi) + S(phi) m - BC``;
-* ``FlameletEquations.jac`` (``equations.py:240-298``): central blocks
+* ``FlameletEquations.jac`` (``equations.py:228-282``): central blocks
   ``chi/2 Lap_c + dS/dphi`` (zero source blocks at the two boundary
   points), lower ``chi[1:]/2 Lap_l``, upper ``chi[:-1]/2 Lap_u``;
 * ``FlameletEquations.jacobian_action`` (``equations.py:411-450``):
   ``chi/2 Lap(v) + dS/dphi v`` with every point's source Jacobian;
-* ``source_terms`` (``equations.py:340-385``): ``S = (v/rho, W w/rho)``
+* ``source_terms`` (``equations.py:313-359``): ``S = (v/rho, W w/rho)``
   with T from the enthalpy Newton of ``make_pyro.py:255-299`` and
   ``rho = get_density(p, T, Y)``;
 * ``Laplacian.assemble_block_form`` / ``apply_operator``
@@ -24,7 +24,7 @@ and, for the compressible-EOS consistency layer,
 * ``FlameletEquations.adjoint_operator`` (``equations.py:451-516``):
   central blocks ``Lap_c`` inside plus ``(2/chi) dS/dphi^T``, boundary
   blocks ``chi/2 Lap_c``, the Laplacian's own lower/upper blocks;
-* ``local_compressible_eos_rt`` (``equations.py:517-535``): ``R T / W_mix``
+* ``local_compressible_eos_rt`` (``equations.py:518-535``): ``R T / W_mix``
   at T(h, Y), and its gradient (central differences here);
 * the pressure gradient of the source (``source_gradient_wrt_pressure``,
   ``equations.py:124-134``; fourth-order central differences here);

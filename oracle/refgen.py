@@ -38,12 +38,14 @@ import types
 
 import numpy as np
 
-REFERENCE_ROOT = os.environ.get("PYRO_REFERENCE_ROOT", "/root/reference")
+# The reference checkout is found through PYRO_REFERENCE_ROOT alone; with
+# it unset, everything that runs the reference is skipped.
+REFERENCE_ROOT = os.environ.get("PYRO_REFERENCE_ROOT", "")
 
 
 def reference_available() -> bool:
-    return os.path.isfile(os.path.join(REFERENCE_ROOT, "pyrometheus",
-                                       "codegen", "python.py"))
+    return bool(REFERENCE_ROOT) and os.path.isfile(os.path.join(
+        REFERENCE_ROOT, "pyrometheus", "codegen", "python.py"))
 
 
 # {{{ pymbolic stand-in
@@ -500,8 +502,8 @@ def reference_generator():
     if _REF is not None:
         return _REF
     if not reference_available():
-        raise RuntimeError("reference checkout not found at "
-                           f"{REFERENCE_ROOT}")
+        raise RuntimeError("reference checkout not found (set "
+                           "PYRO_REFERENCE_ROOT to its root)")
     mods = _install_stubs()
     saved = {k: sys.modules.get(k) for k in mods}
     saved.update({k: sys.modules.get(k) for k in

@@ -16,24 +16,25 @@ def main(argv=None):
     generators = get_code_generators()
     parser = argparse.ArgumentParser(
         prog="pyrometheus_gb300",
-        description="Code generation for combustion thermochemistry "
-                    "(GB300 CUDA target).")
+        description="Generate thermochemistry code for a mechanism; the "
+                    "cuda target emits a GB300 (sm_103a) translation "
+                    "unit.")
     parser.add_argument("--version", action="version",
                         version=f"%(prog)s {__version__}")
     parser.add_argument("-l", "--lang", "--language",
-                        help="Language to generate code for.",
+                        help="target language of the generated code",
                         choices=generators.keys(), required=True)
     parser.add_argument("-m", "--mech", "--mechanism",
-                        help="Path to the mechanism file.", required=True)
-    parser.add_argument("-o", "--output", help="Path to the output file.",
+                        help="mechanism file (Cantera YAML)", required=True)
+    parser.add_argument("-o", "--output", help="file to write the generated code to",
                         required=True)
     parser.add_argument("-n", "--name", "--namespace",
-                        help="Namespace to use for the generated code.",
+                        help="name of the generated class or namespace",
                         required=True)
     parser.add_argument("-p", "--phase",
-                        help="Phase name to use for the generated code.")
+                        help="phase of the mechanism file to read")
     parser.add_argument("--build", action="store_true",
-                        help="Also compile the output to a shared library.")
+                        help="also compile the output into a shared library")
     args = parser.parse_args(argv)
 
     gen = generators[args.lang]

@@ -65,15 +65,16 @@ class CompressibleEOS:
     def update_config_option(self, option_path: str, option_val):
         """``config[a][b][c] = option_val`` for ``option_path = "a/b/c"``,
         creating missing levels (``thermodynamic_consistency.py:81-104``)."""
-        keys = option_path.split("/")
-        current = self.config
-        for k in keys[:-1]:
-            if k not in current:
-                current[k] = {}
-            if not isinstance(current[k], dict):
-                raise TypeError(f"Path segment {k} is not a dict")
-            current = current[k]
-        current[keys[-1]] = option_val
+        *parents, leaf = option_path.split("/")
+        node = self.config
+        for name in parents:
+            child = node.setdefault(name, {})
+            if not isinstance(child, dict):
+                # the reference raises TypeError here too
+                raise TypeError(f"config entry {name!r} on the path "
+                                f"{option_path!r} is not a dict")
+            node = child
+        node[leaf] = option_val
 
     # {{{ gradients (whole batch; thermodynamic_consistency.py:105-307)
 

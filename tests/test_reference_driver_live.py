@@ -194,7 +194,11 @@ def test_oracle_jacobian_assembly_matches_the_reference(tag):
     ``jacobian_action``: L and U bit for bit, the central blocks and the
     action within 1e-8 of each row's largest entry (the two difference
     Jacobians differ only by where the temperature iterations stop, per
-    point in the reference, batch-wide in the oracle)."""
+    point in the reference, batch-wide in the oracle).  Both sides use the
+    same central-difference source Jacobian, so this checks the assembly
+    (Laplacian, per-point contraction, boundary handling), not dS/dphi
+    itself; the device jacobian_action is checked against the oracle's in
+    the GPU flamelet tests."""
     from oracle import refdriver
     from oracle.flamelet_oracle import FlameletOracle
     from test_flamelet import _golden
