@@ -1,12 +1,12 @@
 """Small seeded cases of each kernel, for profiler captures.
 
-    python -m pyrometheus_gb300.profile_cases jacobian [states]
-    python -m pyrometheus_gb300.profile_cases vjp [states]
-    python -m pyrometheus_gb300.profile_cases block_thomas [nv] [systems] [n_min] [n_max]
-    python -m pyrometheus_gb300.profile_cases batched_lu [nv] [cells]
-    python -m pyrometheus_gb300.profile_cases transport [states]
-    python -m pyrometheus_gb300.profile_cases serving [cells] [launches]
-    python -m pyrometheus_gb300.profile_cases flamelet_solve [copies]
+    python profile_cases.py jacobian [states]
+    python profile_cases.py vjp [states]
+    python profile_cases.py block_thomas [nv] [systems] [n_min] [n_max]
+    python profile_cases.py batched_lu [nv] [cells]
+    python profile_cases.py transport [states]
+    python profile_cases.py serving [cells] [launches]
+    python profile_cases.py flamelet_solve [copies]
 
 Each case builds its inputs on the current CUDA device (inputs larger than
 the 129 MB L2 at the default sizes, a few GB at most), runs the kernel three
@@ -18,7 +18,12 @@ blocks.
 
 from __future__ import annotations
 
+import os
 import sys
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
 
 import numpy as np
 
@@ -33,7 +38,7 @@ def _dev():
 def jacobian(states: int = 1 << 15, vjp: bool = False):
     import torch
 
-    from . import get_thermochem_class, synthetic
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
     dev = _dev()
     sol = synthetic.config2_mechanism()
     th = get_thermochem_class(sol)(device=dev)
@@ -59,7 +64,7 @@ def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
                  n_max: int = 1024):
     import torch
 
-    from .flamelet import BlockThomasSolver
+    from pyrometheus_gb300.flamelet import BlockThomasSolver
     dev = _dev()
     lengths = np.random.default_rng(0).integers(n_min, n_max + 1,
                                                 size=systems)
@@ -82,7 +87,7 @@ def batched_lu(nv: int = 54, cells: int = 1 << 16):
 
     import torch
 
-    from . import native
+    from pyrometheus_gb300 import native
     dev = _dev()
     lib = native.batched_lu_lib()
     g = torch.Generator(device=dev).manual_seed(nv)
@@ -112,7 +117,7 @@ def transport(states: int = 1 << 18):
     (``k_transport_mixavg``); prints the mean of the timed launches."""
     import torch
 
-    from . import get_thermochem_class, synthetic
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
     dev = _dev()
     sol = synthetic.config2_mechanism()
     th = get_thermochem_class(sol)(device=dev)
@@ -140,8 +145,8 @@ def serving(cells: int = 1 << 16, launches: int = 3):
     attempts per cell; prints the time per launch."""
     import torch
 
-    from . import get_thermochem_class, synthetic
-    from .serving import CudaReactorBackend, ReactorPool, poisson_requests
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
+    from pyrometheus_gb300.serving import CudaReactorBackend, ReactorPool, poisson_requests
     dev = _dev()
     sol = synthetic.config1_mechanism()
     th = get_thermochem_class(sol)(device=dev)
@@ -170,8 +175,8 @@ def flamelet_solve(copies: int = 256):
 
     import torch
 
-    from . import get_thermochem_class, synthetic
-    from .flamelet_solver import FlameletSolver
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
+    from pyrometheus_gb300.flamelet_solver import FlameletSolver
     dev = _dev()
     sol = synthetic.scaled_rates(synthetic.config1_mechanism(), 1e-12)
     th = get_thermochem_class(sol)(device=dev)
