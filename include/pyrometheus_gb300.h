@@ -198,8 +198,8 @@ int pyro_reactor_bdf2(double* y, double* y_prev, double* f_n, int64_t ld,
  * for flamelets packed along rows (system s owns rows [row_off[s],
  * row_off[s+1]), at least 3; sys_of_row[rows] gives s; uniform grid with
  * inv_dx2[s] = 1/dx^2): FlameletEquations.rhs,
- * pyrometheus/flamelets/equations.py:193-238, with the Laplacian of
- * onedim_laplacian.py:182-212 and source_terms equations.py:340-385.
+ * pyrometheus/flamelets/equations.py:167-227, with the Laplacian of
+ * onedim_laplacian.py:182-212 and source_terms equations.py:313-359.
  * Inputs: T[rows] (from get_temperature_from_enthalpy), h[rows],
  * Y[S][ldy], F[S+1][ldf] the reactor source at (p, T, Y) (rows 1.. are
  * W_k w_k / rho), chi and visc [rows], h_ox/h_fu [nsys], y_ox/y_fu
@@ -215,7 +215,7 @@ int pyro_flamelet_residual(const double* p, int64_t p_inc, const double* T,
                            cudaStream_t stream);
 
 /* Block-tridiagonal Jacobian of that residual w.r.t. (h, Y):
- * FlameletEquations.jac, equations.py:240-298, and
+ * FlameletEquations.jac, equations.py:228-282, and
  * Laplacian.assemble_block_form, onedim_laplacian.py:144-180.  On entry
  * C[rows][nv][nv] holds pyro_reactor_jacobian at (p, T, Y); it is turned in
  * place into the central blocks (chain rule through T(h, Y), viscous
@@ -228,6 +228,24 @@ int pyro_flamelet_blocks(const double* p, int64_t p_inc, const double* T,
                          const int* sys_of_row, const double* inv_dx2,
                          double* L, double* C, double* U, int64_t rows,
                          cudaStream_t stream);
+
+/* Matrix-free Jacobian action A v = chi/2 Lap(v) + dS/dphi v per point,
+ * A[S+1][lda] for directions V[S+1][ldv]: FlameletEquations.jacobian_action,
+ * pyrometheus/flamelets/equations.py:411-450.  Every point keeps its source
+ * Jacobian (the boundary points included, unlike the blocks) and the
+ * Laplacian's boundary rows are v / dx^2.  J[rows][nv][nv] holds
+ * pyro_reactor_jacobian at (p, T, Y) (read only); other arguments as for
+ * pyro_flamelet_blocks. */
+int pyro_flamelet_jacobian_action(const double* p, int64_t p_inc,
+                                  const double* T, const double* Y,
+                                  int64_t ldy, const double* J,
+                                  const double* V, int64_t ldv,
+                                  const double* chi, const double* visc,
+                                  const int64_t* row_off,
+                                  const int* sys_of_row,
+                                  const double* inv_dx2, double* A,
+                                  int64_t lda, int64_t rows,
+                                  cudaStream_t stream);
 
 /* dF/dp [S+1][ldf] of the reactor source at fixed (T, Y), in forward mode
  * (the concentrations and [M] scale with p): the pressure derivative the

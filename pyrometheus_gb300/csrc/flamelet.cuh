@@ -1,6 +1,6 @@
 // Steady-flamelet residual and block-tridiagonal Jacobian on the device
 // (FP64, sm_103a): the assembly of pyrometheus/flamelets/equations.py
-// (FlameletEquations.rhs :193-238, jac :240-298, source_terms :340-385)
+// (FlameletEquations.rhs :167-227, jac :228-282, source_terms :313-359)
 // with the Laplacian block form of onedim_laplacian.py:144-180, for many
 // flamelets at once.
 //
@@ -325,6 +325,111 @@ PYRO_EXPORT int pyro_flamelet_residual(
   k_flamelet_residual<<<(int)blocks, 128, 0, stream>>>(
       p, p_inc, T, h, Y, ldy, F, ldf, chi, visc, row_off, sys_of_row,
       inv_dx2, h_ox, h_fu, y_ox, y_fu, ldb, R, ldr, rows);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
+// one warp per row: the matrix-free flamelet Jacobian action
+// A v = chi / 2 Lap(v) + dS/dphi v (FlameletEquations.jacobian_action,
+// equations.py:411-450), with every point's source Jacobian -- the two
+// boundary points included, unlike the blocks -- and the Laplacian's
+// boundary rows v / dx^2.  dS/dphi v comes from the reactor Jacobian J at
+// (T, Y, p) without forming dS/dphi: with a = (v_h - sum_m h_m v_m) / cp
+// (the temperature change along v), the species rows are J (a, v_Y) and
+// the enthalpy row (v / rho) (a / T + sum_m v_m / (sigma W_m)).
+__global__ void __launch_bounds__(128)
+    k_flamelet_jacobian_action(
+        const double* __restrict__ Pp, int64_t p_inc,
+        const double* __restrict__ Tt, const double* __restrict__ Y,
+        int64_t ldy, const double* __restrict__ J,
+        const double* __restrict__ V, int64_t ldv,
+        const double* __restrict__ chi, const double* __restrict__ visc,
+        const int64_t* __restrict__ row_off,
+        const int* __restrict__ sys_of_row,
+        const double* __restrict__ inv_dx2, double* __restrict__ A,
+        int64_t lda, int64_t rows) {
+  const int lane = threadIdx.x & 31;
+  constexpr int NB = FNV * FNV;
+  __shared__ double s_z[4][FNV];
+  double* z = s_z[threadIdx.x >> 5];
+  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+       r < rows; r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
+    const int s = sys_of_row[r];
+    const int64_t r0 = row_off[s], r1 = row_off[s + 1];
+    const bool interior = r != r0 && r != r1 - 1;
+    const double idx2 = inv_dx2[s];
+    const double T = Tt[r];
+    const double invT = 1.0 / T;
+    double sig = 0.0, cpp = 0.0, hv = 0.0, wv = 0.0;
+    for (int k = lane; k < NS; k += 32) {
+      const double wk = __ldg(Y + (int64_t)k * ldy + r) * k_inv_mw[k];
+      const pyro::Nasa a(k, T > k_tmid[k]);
+      const double cpk =
+          fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
+      const double hrt =
+          fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
+                            a[2] * (1.0 / 3.0)),
+                    a[1] * 0.5),
+              a[0]) +
+          a[5] * invT;
+      const double vk = __ldg(V + (int64_t)(k + 1) * ldv + r);
+      sig += wk;
+      cpp = fma(wk, cpk, cpp);
+      hv = fma(GAS_CONSTANT * T * hrt * k_inv_mw[k], vk, hv);
+      wv = fma(k_inv_mw[k], vk, wv);
+      z[k + 1] = vk;
+    }
+    const double sigma = pyro::warp_sum(sig);
+    const double cp = GAS_CONSTANT * pyro::warp_sum(cpp);
+    const double hvs = pyro::warp_sum(hv), wvs = pyro::warp_sum(wv);
+    const double vh = __ldg(V + r);
+    const double a = (vh - hvs) / cp;
+    if (lane == 0) z[0] = a;
+    __syncwarp();
+    const double rho = pyro_ld(Pp, p_inc, r) / (GAS_CONSTANT * T * sigma);
+    const double* __restrict__ Jr = J + r * NB;
+    const double half_chi = 0.5 * chi[r];
+    // chi / 2 Lap(v) for component q at this row
+    auto lap = [&](int q) {
+      const double vc = __ldg(V + (int64_t)q * ldv + r);
+      if (!interior) return vc * idx2;
+      return (__ldg(V + (int64_t)q * ldv + r - 1) - 2.0 * vc +
+              __ldg(V + (int64_t)q * ldv + r + 1)) * idx2;
+    };
+    for (int k = 0; k < NS; ++k) {
+      const double* __restrict__ row = Jr + (int64_t)(k + 1) * FNV;
+      double acc = 0.0;
+      for (int m = lane; m < FNV; m += 32) acc = fma(__ldg(row + m), z[m], acc);
+      acc = pyro::warp_sum(acc);
+      if (lane == 0)
+        A[(int64_t)(k + 1) * lda + r] = fma(half_chi, lap(k + 1), acc);
+    }
+    if (lane == 0) {
+      const double vr = visc[r] / rho;
+      A[r] = fma(half_chi, lap(0), vr * (a * invT + wvs / sigma));
+    }
+    __syncwarp();
+  }
+}
+
+PYRO_EXPORT int pyro_flamelet_jacobian_action(
+    const double* p, int64_t p_inc, const double* T, const double* Y,
+    int64_t ldy, const double* J, const double* V, int64_t ldv,
+    const double* chi, const double* visc, const int64_t* row_off,
+    const int* sys_of_row, const double* inv_dx2, double* A, int64_t lda,
+    int64_t rows, cudaStream_t stream) {
+  if (rows < 0 || ldy < rows || ldv < rows || lda < rows)
+    return PYRO_ERR_ARGUMENT;
+  if (rows == 0) return PYRO_OK;
+  if (!p || !T || !Y || !J || !V || !chi || !visc || !row_off ||
+      !sys_of_row || !inv_dx2 || !A)
+    return PYRO_ERR_ARGUMENT;
+  int64_t blocks = (rows * 32 + 127) / 128;
+  const int64_t cap = (int64_t)pyro_sm_count() * 32;
+  if (blocks > cap) blocks = cap;
+  k_flamelet_jacobian_action<<<(int)blocks, 128, 0, stream>>>(
+      p, p_inc, T, Y, ldy, J, V, ldv, chi, visc, row_off, sys_of_row, inv_dx2,
+      A, lda, rows);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }

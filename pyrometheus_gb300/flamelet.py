@@ -318,7 +318,7 @@ class FlameletEquations:
     """Steady-flamelet residual and block-tridiagonal Jacobian for many
     flamelets at once, on the GPU: the counterpart of
     ``pyrometheus.flamelets.equations.FlameletEquations`` (``rhs``
-    ``equations.py:193-238``, ``jac`` :240-298, ``source_terms`` :340-385)
+    ``equations.py:167-227``, ``jac`` :228-282, ``source_terms`` :313-359)
     with the Laplacian of ``onedim_laplacian.py:144-180``.
 
     Flamelets are packed along rows as for :class:`BlockThomasSolver`:
@@ -414,7 +414,7 @@ class FlameletEquations:
 
     def temperature(self, h, Y, temp_guess, check=True):
         """T with h_mix(T, Y) = h (``equation_of_state``,
-        ``equations.py:320-338``).  ``check=False`` returns the last
+        ``equations.py:284-311``).  ``check=False`` returns the last
         iterate of states whose iteration did not converge (nan for nan
         states) instead of raising."""
         if check:
@@ -422,6 +422,72 @@ class FlameletEquations:
                 h, Y, self._rowvec(temp_guess))
         return self.th._temperature(h, self._rowvec(temp_guess), Y, False,
                                     1.0e-10, 500, check=False)
+
+    def equation_of_state(self, h, Y, temp_guess, pressure):
+        """``(density [rows], temperature [rows])`` from the state:
+        T(h, Y) by the enthalpy Newton, then the ideal-gas density
+        (``equation_of_state``, ``equations.py:284-311``)."""
+        h, Y = self._state(h, Y)
+        T = self.temperature(h, Y, temp_guess)
+        p, _ = self._pressure(pressure)
+        return self.th.get_density(p, T, Y), T
+
+    def source_terms(self, h, Y, viscous_diss, temp_guess, pressure,
+                     temperature=None):
+        """``(S_h [rows], S_Y [S, rows])``: the point-wise source
+        ``(v / rho, W w / rho)`` (``source_terms``,
+        ``equations.py:313-359``)."""
+        h, Y = self._state(h, Y)
+        T = temperature if temperature is not None else \
+            self.temperature(h, Y, temp_guess)
+        p, _ = self._pressure(pressure)
+        F = self.th.get_reactor_source(p, T, Y)
+        rho = self.th.get_density(p, T, Y)
+        return self._rowvec(viscous_diss) / rho, F[1:]
+
+    def boundary_conditions(self, h_ox, h_fu):
+        """``(BC_h [rows], BC_Y [S, rows])``: ``h_ox``/``y_ox`` at each
+        flamelet's first point, ``h_fu``/``y_fu`` at its last, zero inside
+        (``boundary_conditions``, ``equations.py:391-409``)."""
+        f64 = dict(dtype=torch.float64, device=self.device)
+        bh = torch.zeros(self.rows, **f64)
+        by = torch.zeros((self.S, self.rows), **f64)
+        first, last = self.row_off[:-1], self.row_off[1:] - 1
+        bh[first] = self._sysvec(h_ox)
+        bh[last] = self._sysvec(h_fu)
+        by[:, first] = self.y_ox
+        by[:, last] = self.y_fu
+        return bh, by
+
+    def jacobian_action(self, v, h, Y, diss_rate, viscous_diss, temp_guess,
+                        pressure, temperature=None):
+        """``chi/2 Lap(v) + dS/dphi v`` per point, ``[S+1, rows]`` for a
+        direction ``v`` ``[S+1, rows]`` (row 0 enthalpy): the matrix-free
+        product of ``jacobian_action`` (``equations.py:411-450``), with
+        every point's source Jacobian (the boundary points keep theirs,
+        unlike :meth:`jac`'s blocks)."""
+        h, Y = self._state(h, Y)
+        T = temperature if temperature is not None else \
+            self.temperature(h, Y, temp_guess)
+        p, p_inc = self._pressure(pressure)
+        v = v.to(device=self.device, dtype=torch.float64) if \
+            torch.is_tensor(v) else torch.as_tensor(
+                np.asarray(v, dtype=np.float64), device=self.device)
+        if tuple(v.shape) != (self.nv, self.rows):
+            raise ValueError(f"v must have shape {(self.nv, self.rows)}")
+        v = v.contiguous()
+        J = self.th.get_reactor_jacobian(p, T, Y)
+        chi, visc = self._rowvec(diss_rate), self._rowvec(viscous_diss)
+        A = torch.empty((self.nv, self.rows), dtype=torch.float64,
+                        device=self.device)
+        _check(self.th._lib.pyro_flamelet_jacobian_action(
+            p.data_ptr(), p_inc, T.data_ptr(), Y.data_ptr(), Y.stride(0),
+            J.data_ptr(), v.data_ptr(), v.stride(0), chi.data_ptr(),
+            visc.data_ptr(), self.row_off.data_ptr(),
+            self.sys_of_row.data_ptr(), self.inv_dx2.data_ptr(),
+            A.data_ptr(), A.stride(0), self.rows, self._stream()),
+            "flamelet Jacobian action")
+        return A
 
     def rhs(self, h, Y, diss_rate, viscous_diss, temp_guess, pressure,
             h_ox, h_fu, temperature=None):

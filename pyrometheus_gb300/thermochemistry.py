@@ -87,6 +87,9 @@ _SIGNATURES = {
     "pyro_flamelet_adjoint_blocks": [_P, _I64, _P, _P, _I64, _P, _P, _P, _P,
                                      _P, _P, _P, _P, _I64, _P],
     "pyro_flamelet_eos_rt": [_P, _P, _I64, _P, _P, _I64, _I64, _P],
+    "pyro_flamelet_jacobian_action": [_P, _I64, _P, _P, _I64, _P, _P, _I64,
+                                      _P, _P, _P, _P, _P, _P, _I64, _I64,
+                                      _P],
     "pyro_flamelet_residual": [_P, _I64, _P, _P, _P, _I64, _P, _I64, _P, _P,
                                _P, _P, _P, _P, _P, _P, _P, _I64, _P, _I64,
                                _I64, _P],

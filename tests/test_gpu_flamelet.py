@@ -106,3 +106,80 @@ def test_newton_correction_solves_the_linear_system():
         assert np.abs(ax - bs).max() <= 1e-11 * scale
     # both copies of the flamelet get the same correction
     assert np.allclose(x[:n_x], x[n_x:], rtol=1e-12, atol=0)
+
+
+def _lap(v, dx):
+    lap = np.empty_like(v)
+    lap[:, 0] = v[:, 0] / dx ** 2
+    lap[:, -1] = v[:, -1] / dx ** 2
+    lap[:, 1:-1] = (v[:, :-2] - 2.0 * v[:, 1:-1] + v[:, 2:]) / dx ** 2
+    return lap
+
+
+@pytest.mark.parametrize("tag", ["s9", "s53", "s9slow", "s53slow"])
+def test_jacobian_action_against_reference_autodiff(tag):
+    """The device ``jacobian_action`` (``equations.py:411-450``) against
+    chi/2 Lap(v) + dS/dphi v with the golden per-point source Jacobians of
+    every point -- jacfwd through the reference's generated class and its
+    enthalpy Newton, the boundary points included -- and against the
+    oracle's ``jacobian_action`` (central differences)."""
+    import os
+
+    from conftest import GOLDEN
+    from oracle.flamelet_oracle import FlameletOracle
+    from pyrometheus_gb300.yaml_mech import load_mechanism
+    g = np.load(os.path.join(GOLDEN, "eos_adjoint.npz"))
+    d = {k[len(tag) + 1:]: g[k] for k in g.files
+         if k.startswith(tag + "_")}
+    sol = load_mechanism(f"{tag}.yaml", text=str(d["mech_yaml"]))
+    n_x = d["h"].shape[0]
+    dx = float(d["dx"])
+    eq = _eqs(sol, [n_x], dx, d["y_ox"], d["y_fu"])
+    v = np.random.default_rng(3).standard_normal((sol.n_species + 1, n_x))
+    args = (d["h"], torch.as_tensor(d["Y"]), d["chi"], d["visc"],
+            d["T_guess"], float(d["P"]))
+    A = eq.jacobian_action(torch.as_tensor(v), *args).cpu().numpy()
+    sj = d["src_jac_all"]
+    terms = np.abs(0.5 * d["chi"] * _lap(v, dx)) + np.einsum(
+        "ijk,ki->ji", np.abs(sj), np.abs(v))
+    ref = 0.5 * d["chi"] * _lap(v, dx) + np.einsum("ijk,ki->ji", sj, v)
+    # at the scale of the terms summed (the source Jacobian's rows span
+    # many decades), as for the blocks
+    assert np.all(np.abs(A - ref) <= 1e-10 * terms.max(axis=1,
+                                                       keepdims=True))
+    # boundary points keep their source Jacobians: the action there is
+    # not just chi/2 v/dx^2
+    assert np.abs(A[:, [0, -1]] - (0.5 * d["chi"] * _lap(v, dx))[:, [0, -1]]
+                  ).max() > 0
+    if tag.endswith("slow"):
+        # central differences resolve the slow-chemistry source Jacobians
+        # (the stiff ones, entries to 1e14, only the autodiff pins)
+        fo = FlameletOracle(sol)
+        ref_fd = fo.jacobian_action(v, d["h"], d["Y"], d["chi"], d["visc"],
+                                    d["T_guess"], float(d["P"]), dx)
+        assert np.all(np.abs(A - ref_fd) <= 1e-6 * terms.max(
+            axis=1, keepdims=True))
+
+
+@pytest.mark.parametrize("tag", TAGS)
+def test_public_source_terms_eos_and_boundary_conditions(tag):
+    """``equation_of_state``, ``source_terms`` and ``boundary_conditions``
+    (``equations.py:284-409``) against the golden values from the
+    reference's generated class."""
+    sol, d = _golden(tag)
+    n_x = d["h"].shape[0]
+    eq = _eqs(sol, [n_x], float(d["dx"]), d["y_ox"], d["y_fu"])
+    Y = torch.as_tensor(d["Y"])
+    rho, T = eq.equation_of_state(d["h"], Y, d["T_guess"], float(d["P"]))
+    assert np.abs(T.cpu().numpy() - d["T_solved"]).max() < 1e-10
+    sh, sy = eq.source_terms(d["h"], Y, d["visc"], d["T_guess"],
+                             float(d["P"]))
+    src = np.vstack([sh.cpu().numpy()[None], sy.cpu().numpy()])
+    scale = np.abs(d["src"]).max(axis=1, keepdims=True)
+    assert np.all(np.abs(src - d["src"]) <= 1e-12 * scale)
+    bh, by = eq.boundary_conditions(float(d["h_ox"]), float(d["h_fu"]))
+    bh, by = bh.cpu().numpy(), by.cpu().numpy()
+    assert bh[0] == float(d["h_ox"]) and bh[-1] == float(d["h_fu"])
+    assert not bh[1:-1].any() and not by[:, 1:-1].any()
+    assert np.array_equal(by[:, 0], d["y_ox"])
+    assert np.array_equal(by[:, -1], d["y_fu"])
