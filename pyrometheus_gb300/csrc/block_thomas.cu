@@ -834,8 +834,12 @@ __global__ void __launch_bounds__(kSegWarps * 32)
         const double xk = __shfl_sync(0xffffffffu, y, base + k);
         if (r < k) y = fma(-f[k], xk, y);
       }
-      x = y;
-      if (act) X[row * NV + r] = x;
+      // a segment whose system is shorter than the warp's longest idles
+      // through the first rows of this loop and keeps x_{N-1} meanwhile
+      if (act) {
+        x = y;
+        X[row * NV + r] = x;
+      }
     }
     if (singular && status) atomicOr(status, 1);
   }
