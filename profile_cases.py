@@ -3,6 +3,7 @@
     python profile_cases.py jacobian [states]
     python profile_cases.py vjp [states]
     python profile_cases.py block_thomas [nv] [systems] [n_min] [n_max]
+    python profile_cases.py block_thomas_seg [nv] [systems] [n_min] [n_max]
     python profile_cases.py batched_lu [nv] [cells]
     python profile_cases.py transport [states]
     python profile_cases.py serving [cells] [launches]
@@ -61,7 +62,7 @@ def jacobian(states: int = 1 << 15, vjp: bool = False):
 
 
 def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
-                 n_max: int = 1024):
+                 n_max: int = 1024, kernel=None):
     import torch
 
     from pyrometheus_gb300.flamelet import BlockThomasSolver
@@ -76,7 +77,7 @@ def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
     L = torch.randn((rows, nv, nv), generator=g, **f64)
     U = torch.randn((rows, nv, nv), generator=g, **f64)
     b = torch.randn((rows, nv), generator=g, **f64)
-    solver = BlockThomasSolver(nv, lengths, device=dev)
+    solver = BlockThomasSolver(nv, lengths, device=dev, kernel=kernel)
     for _ in range(3):
         solver.solve(L, C, U, b)
     torch.cuda.synchronize()
@@ -227,6 +228,8 @@ def main(argv=None):
         jacobian(*rest, vjp=True)
     elif case == "block_thomas":
         block_thomas(*rest)
+    elif case == "block_thomas_seg":
+        block_thomas(*rest, kernel="seg")
     elif case == "batched_lu":
         batched_lu(*rest)
     elif case == "transport":
