@@ -25,7 +25,13 @@ def load_golden(name):
     return sol, g
 
 
-GOLDEN_SETS = ["synthetic9", "synthetic53", "quirks9"]
+# seeded synthetic mechanisms (the benchmark shapes and one with
+# irreversible reactions, fractional orders and a zero default efficiency)
+# and the reference's own test fixtures (test/mechs/*.yaml, the set
+# test/CMakeLists.txt:9 runs every backend on), all with golden vectors
+# from the reference's generated class
+FIXTURE_SETS = ["ref_uiuc", "ref_sandiego", "ref_hong", "ref_uconn32"]
+GOLDEN_SETS = ["synthetic9", "synthetic53", "quirks9"] + FIXTURE_SETS
 
 
 def rel_err(x, ref, scale=None):

@@ -1,14 +1,17 @@
 """Generate the golden vectors in this folder from the reference itself.
 
-Run in a checkout that has the reference next to it (the default location is
-``/root/reference``; override with ``PYRO_REFERENCE_ROOT``)::
+Run with ``PYRO_REFERENCE_ROOT`` set to the root of a reference checkout::
 
-    python tests/golden/make_golden.py
+    PYRO_REFERENCE_ROOT=<checkout> python tests/golden/make_golden.py [fixtures]
 
 For each mechanism below it
 
-1. builds the mechanism with :mod:`pyrometheus_gb300.synthetic` and stores
-   its Cantera-YAML text (so the tests rebuild exactly the same mechanism);
+1. builds the mechanism -- seeded synthetic ones with
+   :mod:`pyrometheus_gb300.synthetic`, and the reference's own test
+   fixtures (``test/mechs/{uiuc,sandiego,hong,uconn32,gri30}.yaml``, the
+   set ``test/CMakeLists.txt:9`` runs every backend on) through the YAML
+   loader -- and stores its Cantera-YAML text in SI units (so the tests
+   rebuild exactly the same mechanism without the checkout);
 2. renders the reference's ``PythonCodeGenerator`` class for it
    (``oracle/refgen.py``: the reference's generator with stand-ins for its
    uninstalled Cantera/pymbolic/mako dependencies);
@@ -125,10 +128,85 @@ def reactor_jacobian(cls, p, t, y):
     return jac.numpy(), val.numpy().T
 
 
-def golden(sol, n, seed, n_jac, fname):
+def reactor_states(sol, fuel, stoich_ratio, n_samples, t_end):
+    """States along an adiabatic constant-pressure ignition from 1500 K and
+    one atmosphere, with the fuel/O2/N2 mole fractions of the reference's
+    kinetics tests (``test/test.py:228-238``: equivalence ratio 1,
+    oxidizer-to-diluent ratio 0.21), sampled at the first integrator steps
+    where the temperature has risen by 0, 1/n, ..., (n-1)/n of its rise up
+    to *t_end*.  The trajectory comes from SciPy's BDF on the oracle's
+    source terms (vectorised over the difference Jacobian's columns); it
+    only supplies realistic compositions (radical pools, near-equilibrium
+    products)."""
+    from scipy.integrate import solve_ivp
+
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    orc = Oracle(sol)
+    S = sol.n_species
+    x = np.zeros(S)
+    i_fu, i_ox = sol.species_index(fuel), sol.species_index("O2")
+    i_di = sol.species_index("N2")
+    x[i_fu] = 0.21 / (stoich_ratio + 0.21)
+    x[i_ox] = stoich_ratio * x[i_fu]
+    x[i_di] = (1.0 - 0.21) * x[i_ox] / 0.21
+    x /= x.sum()
+    mw = np.asarray(sol.molecular_weights, dtype=np.float64)
+    y0 = x * mw / np.dot(x, mw)
+    p0 = 101325.0
+
+    def rhs(_, s):
+        s = s.reshape(S + 1, -1)
+        t, y = s[0], np.maximum(s[1:], 0.0)
+        rho = orc.get_density(p0, t, y)
+        w = orc.get_net_production_rates(rho, t, y)
+        h = orc.get_species_enthalpies_rt(t) * gas_constant * t
+        cp = orc.get_mixture_specific_heat_cp_mass(t, y)
+        return np.vstack([-(h * w).sum(axis=0) / (rho * cp),
+                          mw[:, None] * w / rho])
+
+    traj = solve_ivp(rhs, (0.0, t_end), np.concatenate([[1500.0], y0]),
+                     method="BDF", rtol=1e-7, atol=1e-13, vectorized=True)
+    if traj.status != 0:
+        raise RuntimeError(f"ignition on {sol.source}: {traj.message}")
+    rise = traj.y[0] - traj.y[0, 0]
+    picks = [int(np.argmax(rise >= k / n_samples * rise[-1]))
+             for k in range(n_samples)]
+    states = traj.y[:, picks]
+    y = np.maximum(states[1:], 0.0)
+    y /= y.sum(axis=0, keepdims=True)
+    return states[0].copy(), np.full(n_samples, p0), y
+
+
+def fixture_states(sol, fuel, stoich_ratio, t_end, n_reactor, n_random,
+                   seed):
+    """The state families of the reference's tests (``test/test.py``):
+    ignition-trajectory states, seeded random states with edge cases
+    (T = Tmid, 300 K, 3000 K, exact zeros), equal mass fractions at ten
+    temperatures in [500, 3000] K (``:56-60``), and every pure species at
+    those temperatures (``:191-200``); pressure one atmosphere except for
+    the random states."""
+    S = sol.n_species
+    t_r, p_r, y_r = reactor_states(sol, fuel, stoich_ratio, n_reactor,
+                                   t_end)
+    t_e, p_e, y_e = edge_states(sol, n_random, seed)
+    temps = np.linspace(500.0, 3000.0, 10)
+    t_u, y_u = temps.copy(), np.full((S, 10), 1.0 / S)
+    t_p = np.tile(temps, S)
+    y_p = np.repeat(np.eye(S), 10, axis=1)
+    t = np.concatenate([t_r, t_e, t_u, t_p])
+    p = np.concatenate([p_r, p_e, np.full(10 + 10 * S, 101325.0)])
+    y = np.ascontiguousarray(np.concatenate([y_r, y_e, y_u, y_p], axis=1))
+    return t, p, y
+
+
+def golden(sol, n, seed, n_jac, fname, states=None):
     cls = refgen.reference_class(sol)
     ref = cls()
-    t, p, y = edge_states(sol, n, seed)
+    if states is None:
+        t, p, y = edge_states(sol, n, seed)
+    else:
+        t, p, y = states
+        n = t.size
     mmw = ref.get_mixture_molecular_weight(y)
     rho = p * mmw / (gas_constant * t)
     c = np.array(list(ref.get_concentrations(rho, y)))
@@ -165,6 +243,9 @@ def golden(sol, n, seed, n_jac, fname):
     h = out["h_mass"]
     out["T_from_e"] = np.asarray(ref.get_temperature(e, 1500.0, y, True))
     out["T_from_h"] = np.asarray(ref.get_temperature(h, 1500.0, y, False))
+    # the reference's own guess in its temperature test (test/test.py:197)
+    out["T_from_e_guess09"] = np.asarray(
+        ref.get_temperature(e, 0.9 * t, y, True))
     jac, src = reactor_jacobian(cls, p[:n_jac], t[:n_jac], y[:, :n_jac])
     out["jac"] = jac
     out["reactor_source"] = src
@@ -483,9 +564,43 @@ def golden_transport(fname="transport.npz"):
     print(f"wrote {fname}")
 
 
+# the reference's fixture mechanisms with the fuel and O2/fuel mole ratio
+# its kinetics tests use for each (test/test.py:212-217, 377-383), the end
+# of the ignition run (s; past 99 % of the temperature rise) and how many
+# golden states go to the Jacobian
+FIXTURES = (("uiuc", "C2H4", 3.0, 1e-3, 16),
+            ("sandiego", "H2", 0.5, 1e-3, 16),
+            ("hong", "H2", 0.5, 1e-3, 16),
+            ("uconn32", "C2H4", 3.0, 1e-3, 12),
+            ("gri30", "CH4", 2.0, 2e-3, 12))
+
+
+def load_fixture(name):
+    from pyrometheus_gb300.yaml_mech import load_mechanism
+    path = os.path.join(refgen.REFERENCE_ROOT, "test", "mechs",
+                        f"{name}.yaml")
+    try:
+        return load_mechanism(path, "gas")
+    except ValueError:
+        return load_mechanism(path)
+
+
+def golden_fixtures(names=None):
+    for k, (name, fuel, stoich, t_end, n_jac) in enumerate(FIXTURES):
+        if names and name not in names:
+            continue
+        sol = load_fixture(name)
+        states = fixture_states(sol, fuel, stoich, t_end, n_jac, 32, 60 + k)
+        golden(sol, 0, 0, n_jac, f"ref_{name}.npz", states)
+
+
 def main():
     if not refgen.reference_available():
-        raise SystemExit("reference checkout not found")
+        raise SystemExit("reference checkout not found: set "
+                         "PYRO_REFERENCE_ROOT")
+    if sys.argv[1:2] == ["fixtures"]:
+        golden_fixtures(sys.argv[2:])
+        return
     golden(synthetic.config1_mechanism(), 256, 11, 24, "synthetic9.npz")
     golden(synthetic.config2_mechanism(), 48, 12, 6, "synthetic53.npz")
     golden(quirks_mechanism(), 128, 13, 12, "quirks9.npz")
@@ -493,6 +608,7 @@ def main():
     golden_flamelet()
     golden_transport()
     golden_eos_adjoint()
+    golden_fixtures()
 
 
 if __name__ == "__main__":

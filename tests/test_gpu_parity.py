@@ -94,6 +94,11 @@ def test_temperature(golden_cuda):
     th_ = _np(th.get_temperature(g["h_mass"], 1500.0, y, False))
     assert np.abs(te - g["T_from_e"]).max() < TOL_T
     assert np.abs(th_ - g["T_from_h"]).max() < TOL_T
+    if "T_from_e_guess09" in g:
+        # the reference's temperature test starts from 0.9 T
+        # (test/test.py:196-199)
+        t9 = _np(th.get_temperature(g["e_mass"], 0.9 * g["T"], y, True))
+        assert np.abs(t9 - g["T_from_e_guess09"]).max() < TOL_T
 
 
 def test_falloff_rates_in_place(golden_cuda):
