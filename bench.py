@@ -808,48 +808,97 @@ def eos_adjoint_legs(dev):
     return res
 
 
-def serving_leg(dev, window, t_end, budget_bytes=48e9):
-    """Reactor serving: seeded Poisson arrivals at 2,000 req/s for *window*
-    seconds, each request 1..65,536 cells (log-uniform) on the 9- or
-    53-species mechanism, T0 ~ U[900, 1800] K, p = 1e5 Pa, H2/O2/N2 between
-    stoichiometric and lean, BDF2 to *t_end* at rtol 1e-8; pools sized from
-    an HBM budget.  Latency = completion - arrival on the server clock."""
+# the start mixtures of the serving requests: H2/O2/N2 on the 9-species
+# mechanism; C2H4/O2/N2 on the 53-species one, where H2/O2/N2 barely reacts
+# (SciPy BDF on the oracle: max |dY| below 1e-11 by 1 ms from 900-1800 K)
+# while C2H4 takes 900-2,900 steps and heats the cell by 50-290 K
+SERVING_FUELS = {"s9": ("H2", 2.0), "s53": ("C2H4", 1.0 / 3.0)}
+
+
+def _serve(server, reqs, time_limit):
+    """Serve *reqs*; per-mechanism cells, cell-steps, engine steps and
+    latency percentiles."""
     import numpy as np
 
+    from pyrometheus_gb300.serving import latency_stats
+    steps0 = {k: p.engine_steps for k, p in server.pools.items()}
+    t0 = time.perf_counter()
+    done = list(server.run(reqs, time_limit=time_limit))
+    wall = time.perf_counter() - t0
+    server.done.clear()
+    ok = [r for r in done if r.status == "done"]
+    out = {"requests": len(reqs), "completed": len(ok),
+           "failed": sum(1 for r in done if r.status.startswith("failed")),
+           "wall_s": wall,
+           "cells": int(sum(r.n for r in reqs)),
+           "cell_steps_per_s": int(sum(int(np.sum(r.steps)) for r in ok))
+           / wall}
+    out.update(latency_stats(done))
+    per = {}
+    for name, pool in server.pools.items():
+        mine = [r for r in reqs if r.mech == name]
+        fin = [r for r in ok if r.mech == name]
+        cs = int(sum(int(np.sum(r.steps)) for r in fin))
+        d = {"requests": len(mine), "completed": len(fin),
+             "cells": int(sum(r.n for r in mine)), "cell_steps": cs,
+             "mean_steps_per_cell": cs / max(1, sum(r.n for r in fin)),
+             "engine_steps": pool.engine_steps - steps0[name]}
+        d.update(latency_stats(fin))
+        per[name] = d
+    out["per_mechanism"] = per
+    return out
+
+
+def serving_leg(dev, window, t_end, budget_bytes=48e9):
+    """Reactor serving, two loads.  (1) The configuration's offered load:
+    seeded Poisson arrivals at 2,000 req/s for *window* seconds, each
+    request 1..65,536 cells (log-uniform) on the 9- or 53-species
+    mechanism, T0 ~ U[900, 1800] K, p = 1e5 Pa, fuel/O2/N2 between
+    stoichiometric and lean (SERVING_FUELS), BDF2 to *t_end* at rtol 1e-8;
+    pools sized from an HBM budget.  That load is far beyond what the
+    server completes, so its latencies are backlog-drain times; the run
+    gives the capacity (completed requests per second while backlogged).
+    (2) A sustainable load: Poisson arrivals at 70 % of that capacity for
+    about eight requests, whose latencies are service latencies.  Latency =
+    completion - arrival on the server clock."""
     from pyrometheus_gb300 import get_thermochem_class, synthetic
-    from pyrometheus_gb300.serving import (ReactorServer, latency_stats,
-                                           poisson_requests)
+    from pyrometheus_gb300.serving import ReactorServer, poisson_requests
     mechs = {"s9": synthetic.config1_mechanism(),
              "s53": synthetic.config2_mechanism()}
     th = {k: get_thermochem_class(v)(device=dev) for k, v in mechs.items()}
     server = ReactorServer.from_thermos(th, budget_bytes)
     # warm-up (kernel loading, allocator): one small request per mechanism
     warm = poisson_requests(1e4, 1e-3, mechs, seed=1, cells=(4, 4),
-                            t_end=1e-7)
+                            t_end=1e-7, fuels=SERVING_FUELS)
     for r in warm:
         r.arrival = 0.0
     server.run(warm, time_limit=120.0)
     server.done.clear()
-    reqs = poisson_requests(2000.0, window, mechs, seed=2026, t_end=t_end)
-    steps0 = {k: p.engine_steps for k, p in server.pools.items()}
-    t0 = time.perf_counter()
-    done = server.run(reqs, time_limit=600.0)
-    wall = time.perf_counter() - t0
-    ok = [r for r in done if r.status == "done"]
-    cells = int(sum(r.n for r in ok))
-    cell_steps = int(sum(int(np.sum(r.steps)) for r in ok))
-    out = {"offered_req_per_s": 2000.0, "window_s": window,
-           "requests": len(reqs), "completed": len(ok),
-           "failed": sum(1 for r in done if r.status.startswith("failed")),
-           "cells": int(sum(r.n for r in reqs)), "t_end_s": t_end,
-           "rtol": 1e-8, "wall_s": wall,
-           "cells_per_s": cells / wall, "cell_steps_per_s": cell_steps / wall,
-           "engine_steps": {k: p.engine_steps - steps0[k]
-                            for k, p in server.pools.items()},
+    reqs = poisson_requests(2000.0, window, mechs, seed=2026, t_end=t_end,
+                            fuels=SERVING_FUELS)
+    offered = _serve(server, reqs, 600.0)
+    capacity = offered["completed"] / offered["wall_s"]
+    rate = 0.7 * capacity
+    reqs = poisson_requests(rate, 8.0 / rate, mechs, seed=2027, t_end=t_end,
+                            fuels=SERVING_FUELS)
+    sustained = _serve(server, reqs, 600.0)
+    out = {"t_end_s": t_end, "rtol": 1e-8,
+           "fuels": {k: v[0] for k, v in SERVING_FUELS.items()},
            "pool_capacity_cells": {k: p.cap for k, p in
                                    server.pools.items()},
-           "hbm_budget_bytes": budget_bytes}
-    out.update(latency_stats(done))
+           "hbm_budget_bytes": budget_bytes,
+           "offered": dict(offered, offered_req_per_s=2000.0,
+                           window_s=window,
+                           note="offered load far above capacity: "
+                                "latencies are backlog-drain times"),
+           "capacity_req_per_s": capacity,
+           "sustained": dict(sustained, offered_req_per_s=rate,
+                             note="70 % of the measured capacity")}
+    # the summary figures of the offered run, kept at the top level
+    for k in ("p50_ms", "p99_ms", "cell_steps_per_s", "completed",
+              "requests"):
+        if k in offered:
+            out[k] = offered[k]
     del server, th
     return out
 

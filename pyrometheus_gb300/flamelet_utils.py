@@ -41,3 +41,45 @@ def stoichiometric_mixture_fraction(sol, y_ox, y_fu):
     beta_ox = bilger.dot(elem.dot(np.asarray(y_ox, dtype=np.float64)))
     beta_fu = bilger.dot(elem.dot(np.asarray(y_fu, dtype=np.float64)))
     return -beta_ox / (beta_fu - beta_ox)
+
+
+def burke_schumann(sol, z, y_ox, y_fu, fuel=None):
+    """Mass fractions ``[S, len(z)]`` of the Burke-Schumann flamelet
+    (infinitely fast, complete one-step combustion) over the mixture
+    fraction *z*: the mixing line ``(1 - z) y_ox + z y_fu`` with the fuel
+    and O2 consumed together -- ``fuel + nu O2 -> a CO2 + b/2 H2O`` for a
+    fuel C_a H_b O_c, ``nu = a + b/4 - c/2`` -- as far as the scarcer of the
+    two allows (all the fuel on the lean side, all the O2 on the rich
+    side).  *fuel* defaults to the fuel stream's most abundant species
+    other than N2, Ar, He and O2.  The customary starting guess of a
+    burning steady flamelet (the reference's notebook starts from
+    equilibrium compositions, which need Cantera's solver)."""
+    names = list(sol.species_names)
+    w = np.asarray(sol.molecular_weights, dtype=np.float64)
+    y_ox = np.asarray(y_ox, dtype=np.float64)
+    y_fu = np.asarray(y_fu, dtype=np.float64)
+    if fuel is None:
+        skip = {"N2", "AR", "Ar", "HE", "He", "O2"}
+        cand = [(y_fu[k], k) for k, n in enumerate(names) if n not in skip]
+        fuel = names[max(cand)[1]]
+    kf = names.index(fuel)
+    ko = names.index("O2")
+    el = list(sol.element_names)
+
+    def atoms(e):
+        return sol.n_atoms(kf, el.index(e)) if e in el else 0.0
+
+    a, b, c = atoms("C"), atoms("H"), atoms("O")
+    nu = a + b / 4.0 - c / 2.0
+    z = np.asarray(z, dtype=np.float64)
+    y = (1.0 - z)[None, :] * y_ox[:, None] + z[None, :] * y_fu[:, None]
+    # moles per unit mass of fuel and O2 available, and how much burns
+    n_f = y[kf] / w[kf]
+    n_o = y[ko] / w[ko]
+    burnt = np.minimum(n_f, n_o / nu)
+    y[kf] -= burnt * w[kf]
+    y[ko] -= nu * burnt * w[ko]
+    for name, count in (("CO2", a), ("H2O", b / 2.0)):
+        if count:
+            y[names.index(name)] += count * burnt * w[names.index(name)]
+    return np.maximum(y, 0.0)

@@ -663,13 +663,16 @@ def latency_stats(done: List[Request]) -> Dict[str, float]:
 
 def poisson_requests(rate: float, duration: float, mechs: Dict[str, object],
                      seed: int = 0, cells=(1, 65536), t_end: float = 1e-3,
-                     pressure: float = 1e5, fuel_lean=(0.5, 1.0)):
+                     pressure: float = 1e5, fuel_lean=(0.5, 1.0),
+                     fuels: Dict[str, tuple] = None):
     """Seeded Poisson arrivals: exponential gaps of mean 1/rate over
     *duration* s; cells log-uniform in *cells*; mechanism chosen uniformly;
-    T0 ~ U[900, 1800] K; Y from an H2/O2/N2-type fuel-oxidiser-diluent
-    mix between stoichiometric and lean (equivalence ratio in
-    *fuel_lean*), read from the mechanism's species (``mechs`` maps names
-    to Solution objects)."""
+    T0 ~ U[900, 1800] K; Y from a fuel/O2/N2 mix (air-like 3.76 N2 per O2)
+    between stoichiometric and lean (equivalence ratio in *fuel_lean*).
+    ``mechs`` maps names to Solution objects; ``fuels`` maps a mechanism
+    name to ``(fuel species, fuel moles per O2 at stoichiometric)``,
+    H2 (2 per O2) where not given."""
+    fuels = dict(fuels or {})
     rng = np.random.default_rng(seed)
     out = []
     t = 0.0
@@ -687,15 +690,16 @@ def poisson_requests(rate: float, duration: float, mechs: Dict[str, object],
         Y0 = np.zeros((sol.n_species, n))
         phi = rng.uniform(fuel_lean[0], fuel_lean[1], size=n)
         idx = sol.species_index
-        # H2 + 0.5 O2 with air-like dilution by mass-ish fractions
-        x_f, x_o = 2.0 * phi, np.ones(n)
+        fuel, nu_f = fuels.get(name, ("H2", 2.0))
+        # fuel + O2 with air-like dilution, as mole numbers per O2
+        x_f, x_o = nu_f * phi, np.ones(n)
         x_n = 3.76 * x_o
         w = sol.molecular_weights
-        m_f = x_f * w[idx("H2")]
+        m_f = x_f * w[idx(fuel)]
         m_o = x_o * w[idx("O2")]
         m_n = x_n * w[idx("N2")]
         tot = m_f + m_o + m_n
-        Y0[idx("H2")] = m_f / tot
+        Y0[idx(fuel)] = m_f / tot
         Y0[idx("O2")] = m_o / tot
         Y0[idx("N2")] = m_n / tot
         out.append(Request(rid, name, T0, Y0, pressure, t_end, arrival=t))
