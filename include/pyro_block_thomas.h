@@ -64,8 +64,8 @@ int pyro_block_thomas_small(const double* L, const double* C, const double* U,
  * synchronises beyond a warp.  Pivoting and the kept factors are getrf's,
  * in the workspace layout of pyro_block_thomas (so
  * pyro_block_thomas_resolve applies).  Same arguments as
- * pyro_block_thomas without the CTA size (128 threads); ctas: persistent
- * grid (0 = all resident).  Replaces the same reference function,
+ * pyro_block_thomas without the CTA size (one warp per CTA); ctas: grid
+ * size (0 = all resident).  Replaces the same reference function,
  * pyrometheus/flamelets/linear_solver.py:6-103. */
 int pyro_block_thomas_seg(const double* L, const double* C, const double* U,
                           const double* b, double* x, const int64_t* row_off,

@@ -616,7 +616,12 @@ PYRO_EXPORT int pyro_block_thomas_small(const double* L, const double* C,
 
 namespace {
 
-constexpr int kSegWarps = 4;
+// one warp per CTA: the CTAs (one work item of 32 / nv systems each) are
+// all resident at once, and the hardware spreads them over the SMs round
+// robin, so every SM gets long and short systems alike (with four-warp
+// CTAs of consecutive longest-first items, SM loads differed 1.7-fold and
+// the FP64 pipe of the busiest SM was the only one kept busy)
+constexpr int kSegWarps = 1;
 
 template <int NV>
 struct SegCfg {
@@ -878,8 +883,8 @@ int launch_seg(const double* L, const double* C, const double* U,
 
 // pyro_block_thomas for blocks of size nv <= 16 with 32 / nv systems per
 // warp, one lane per block row (see above).  Same arguments and workspace
-// layout as pyro_block_thomas; the CTA size is fixed (128 threads); ctas:
-// persistent grid (0 = all resident).
+// layout as pyro_block_thomas; the CTA size is fixed (one warp); ctas:
+// grid size (0 = all resident).
 PYRO_EXPORT int pyro_block_thomas_seg(const double* L, const double* C,
                                       const double* U, const double* b,
                                       double* x, const int64_t* row_off,

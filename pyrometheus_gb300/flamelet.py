@@ -39,7 +39,7 @@ class BlockThomasSolver:
     elements; any nv <= 64), ``"seg"`` (32 // nv systems per warp, one lane
     per block row; nv <= 16) or ``"small"`` (one thread per system, nv <=
     16); ``threads``: CTA size (``"cta"``: a multiple of 32; ``"small"``:
-    32 or 64 systems per CTA; ``"seg"``: fixed at 128); both ``None`` pick
+    32 or 64 systems per CTA; ``"seg"``: fixed at 32); both ``None`` pick
     from the autotuner cache or a size rule.  ``ctas``: persistent grid of the ``"cta"`` kernel (0:
     all resident CTAs); ``use_graph``: capture the launch in a CUDA graph on
     the first :meth:`solve` with given buffers and replay it afterwards.
@@ -77,7 +77,7 @@ class BlockThomasSolver:
         if self.kernel in ("small", "seg") and self.nv > 16:
             raise ValueError(f"the {self.kernel!r} kernel takes nv <= 16")
         if self.kernel == "seg":
-            self.threads = 128
+            self.threads = 32
         else:
             self.threads = int(threads) if threads else (
                 _small_threads(self.nv) if self.kernel == "small"
@@ -268,7 +268,7 @@ def autotune(nv: int, n_systems: int = 304, n_min: int = 64,
     plans = [("cta", th) for th in candidates
              if not (nv > th and th < 64) and not (nv <= 24 and th > 256)]
     if nv <= 16:
-        plans += [("seg", 128)]
+        plans += [("seg", 32)]
         plans += [("small", th) for th in (32, 64)
                   if 3 * nv * (nv + 1) * 8 * th <= 227 * 1024]
     times = {}

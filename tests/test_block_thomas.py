@@ -60,7 +60,7 @@ def _solve_cuda(lengths, L, C, U, b, threads=None, use_graph=False,
 
 
 PLANS = [("cta", 32), ("cta", 64), ("cta", 128), ("small", 32),
-         ("small", 64), ("seg", 128)]
+         ("small", 64), ("seg", 32)]
 
 
 @pytest.mark.gpu
