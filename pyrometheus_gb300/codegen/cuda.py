@@ -296,8 +296,9 @@ class _Emitter:
         D holds per slot the partial derivative of the rate of progress
         with respect to that slot's concentration and, after the slots, the
         third-body derivative of each reaction.  Entries are sorted by
-        output element and split into 32 contiguous, equally long runs, one
-        per lane, so each element is summed by one lane in a fixed order
+        output element and split into JGROUP contiguous, equally long runs,
+        one per thread of the state's group (a warp, or two warps for large
+        mechanisms), so each element is summed by one thread in a fixed order
         and stored once (no atomics, no divergent trip counts); elements
         without contributions are listed separately and zeroed with plain
         stores.  Species -> third-body entries give the column sums the
@@ -349,18 +350,25 @@ class _Emitter:
                 groups[-1].append(e)
             else:
                 groups.append([e])
-        # contiguous split of the groups into 32 runs of nearly equal length
-        lanes: List[List[Tuple[int, int, float]]] = [[] for _ in range(32)]
+        # threads per state: two warps where the per-state shared memory
+        # would hold an SM to fewer than 24 warps (so twice the warps fit
+        # beside the same shared memory), else one
+        jw_doubles = 9 * S + 4 * R + nslot + R + 1
+        jgroup = 64 if 8 * jw_doubles > 8192 else 32
+        # contiguous split of the groups into jgroup runs of nearly equal
+        # length, one per thread of the state's group
+        lanes: List[List[Tuple[int, int, float]]] = [[] for _ in
+                                                     range(jgroup)]
         total, done, lane = len(entries), 0, 0
         for g in groups:
-            if lane < 31 and done >= (lane + 1) * total / 32.0:
+            if lane < jgroup - 1 and done >= (lane + 1) * total / jgroup:
                 lane += 1
             lanes[lane].extend(g)
             done += len(g)
         iters = max(len(x) for x in lanes)
         u_off, u_src, u_coef = [], [], []
         for it in range(iters):
-            for ln in range(32):
+            for ln in range(jgroup):
                 if it < len(lanes[ln]):
                     o, s, c = lanes[ln][it]
                 else:
@@ -369,9 +377,10 @@ class _Emitter:
                 u_src.append(s)
                 u_coef.append(c)
         # elements of dw/dc without contributions: plain zero stores
-        ziters = max(1, -(-len(zero_offs) // 32))
-        z_off = [zero_offs[it * 32 + ln] if it * 32 + ln < len(zero_offs)
-                 else 0xFFFF for it in range(ziters) for ln in range(32)]
+        ziters = max(1, -(-len(zero_offs) // jgroup))
+        z_off = [zero_offs[it * jgroup + ln]
+                 if it * jgroup + ln < len(zero_offs) else 0xFFFF
+                 for it in range(ziters) for ln in range(jgroup)]
         # species -> third-body entries (permuted reaction, e - default)
         stinc: List[List[Tuple[int, float]]] = [[] for _ in range(S)]
         for qq, j in enumerate(perm):
@@ -401,8 +410,10 @@ class _Emitter:
         nf = max(1, len(fo_low))
         nasa = [[m.tmid[k]] + list(m.hi[k]) + list(m.lo[k]) + [0.0]
                 for k in range(S)]
-        jw_doubles = 9 * S + 4 * R + nslot + R + 1
-        jwarps = max(1, min(16, (227 * 1024 - 16384) // (8 * jw_doubles)))
+        # states per CTA: as many as fit their shared memory beside the
+        # exp table, at most 512 threads
+        jgroups = max(1, min(512 // jgroup,
+                             (227 * 1024 - 16384) // (8 * jw_doubles)))
 
         def arr(ctype, name, dims, vals):
             return _table(qual, ctype, name, dims, vals)
@@ -415,7 +426,8 @@ class _Emitter:
         w(f"#define JZ_ITERS {ziters}")
         w(f"#define JD_ZERO {zero_src}")
         w(f"#define JW_DOUBLES {jw_doubles}")
-        w(f"#define JWARPS {jwarps}")
+        w(f"#define JGROUP {jgroup}")
+        w(f"#define JGROUPS {jgroups}")
         w(arr("int", "jq_flags", [R], [_cint(flags[j]) for j in perm]))
         w(arr("int", "jq_slot0", [R + 1], [_cint(v) for v in slot0]))
         w(arr("int", "jq_nr", [R], [_cint(v) for v in q_nr]))
@@ -457,13 +469,13 @@ class _Emitter:
               [_cint(v) for v in (st_q or [0])]))
         w(arr("double", "jg_st_de", [max(1, len(st_de))],
               [_hexd(v) for v in (st_de or [0.0])]))
-        w(arr("unsigned short", "jz_off", [32 * ziters],
+        w(arr("unsigned short", "jz_off", [jgroup * ziters],
               [_cint(v) for v in z_off]))
-        w(arr("unsigned short", "ju_off", [32 * iters],
+        w(arr("unsigned short", "ju_off", [jgroup * iters],
               [_cint(v) for v in u_off]))
-        w(arr("unsigned short", "ju_src", [32 * iters],
+        w(arr("unsigned short", "ju_src", [jgroup * iters],
               [_cint(v) for v in u_src]))
-        w(arr("double", "ju_coef", [32 * iters],
+        w(arr("double", "ju_coef", [jgroup * iters],
               [_hexd(v) for v in u_coef]))
         if zero_src > 0xFFFE or (S + 1) * nc > 0xFFFE:
             raise NotImplementedError("mechanism too large for the "

@@ -419,13 +419,50 @@ __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
 
 }  // namespace pyro
 
-// doubles of shared memory per warp (JW_DOUBLES, from the tables):
+// A state is handled by a group of JGROUP threads (one warp, or two for
+// large mechanisms: the per-state shared memory then holds an SM to half
+// the states but still 16 warps, which the FP64 pipe needs to stay busy).
+// Group-wide sums reduce within each warp, then across the group's warps
+// through shared memory in a fixed order, behind a named barrier.
+namespace pyro {
+
+__device__ __forceinline__ void group_sync(int gid) {
+#if JGROUP == 32
+  (void)gid;
+  __syncwarp();
+#else
+  asm volatile("bar.sync %0, %1;" ::"r"(1 + gid), "r"(JGROUP) : "memory");
+#endif
+}
+
+__device__ __forceinline__ double group_sum(double v, int gid, int t,
+                                            double* red) {
+  v = warp_sum(v);
+#if JGROUP == 32
+  (void)gid;
+  (void)t;
+  (void)red;
+  return v;
+#else
+  if ((t & 31) == 0) red[t >> 5] = v;
+  group_sync(gid);
+  double r = red[0];
+#pragma unroll
+  for (int h = 1; h < JGROUP / 32; ++h) r += red[h];
+  group_sync(gid);  // before the slots are written again
+  return r;
+#endif
+}
+
+}  // namespace pyro
+
+// doubles of shared memory per group (JW_DOUBLES, from the tables):
 //   c, h, g, cp, w, jt, a, u, shj [NS each]; q, dq/dT, Hq, Qc [NR each];
 //   D = dq/dc per slot [NSLOT], dq/dM per reaction [NR], one zero.
 // With F non-null the kernel also writes the source f = (dT/dt, dY/dt)
 // [S+1][ldf] from the rates it forms anyway (the primal jacfwd returns with
 // the tangents, flamelets/equations.py:124-129): one pass for both.
-__global__ void __launch_bounds__(JWARPS * 32)
+__global__ void __launch_bounds__(JGROUPS * JGROUP)
     k_reactor_jacobian(const double* __restrict__ Pp, int64_t p_inc,
                        const double* __restrict__ Tp, int64_t t_inc,
                        const double* __restrict__ Y, int64_t ldy,
@@ -433,8 +470,10 @@ __global__ void __launch_bounds__(JWARPS * 32)
                        double* __restrict__ F, int64_t ldf, int64_t n) {
   extern __shared__ double smem[];
   PEXP_PRELOAD();
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  double* sc = smem + (size_t)wid * JW_DOUBLES;
+  const int t = threadIdx.x % JGROUP, gid = threadIdx.x / JGROUP;
+  __shared__ double s_red[JGROUPS][JGROUP / 32];
+  double* red = s_red[gid];
+  double* sc = smem + (size_t)gid * JW_DOUBLES;
   double* sh = sc + NS;
   double* sg = sh + NS;   // g/RT, later the row constants B_k
   double* scp = sg + NS;
@@ -451,16 +490,16 @@ __global__ void __launch_bounds__(JWARPS * 32)
   using LC = pyro::LocalCols;
   const LC c{sc}, g{sg}, h{sh};
   constexpr int NC = NS + 1;
-  if (lane == 0) D[JD_ZERO] = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * JWARPS + wid; i < n;
-       i += (int64_t)gridDim.x * JWARPS) {
+  if (t == 0) D[JD_ZERO] = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * JGROUPS + gid; i < n;
+       i += (int64_t)gridDim.x * JGROUPS) {
     double* Ji = J + i * ldj;
     const double T = pyro_ld(Tp, t_inc, i);
     const double P = pyro_ld(Pp, p_inc, i);
     const double lnT = log(T), invT = 1.0 / T;
-    // species thermo, sigma, cp, dcp/dT (lanes over species)
+    // species thermo, sigma, cp, dcp/dT (threads over species)
     double sig = 0.0, cpp = 0.0, dcpp = 0.0;
-    for (int k = lane; k < NS; k += 32) {
+    for (int k = t; k < NS; k += JGROUP) {
       const double* nk = &jg_nasa[k][0];
       const bool up = T > __ldg(nk);
       const double* a = nk + (up ? 1 : 8);
@@ -490,12 +529,12 @@ __global__ void __launch_bounds__(JWARPS * 32)
       cpp = fma(wk, cpk, cpp);
       dcpp = fma(wk, dcpk, dcpp);
     }
-    const double sigma = pyro::warp_sum(sig);
-    const double cpm = GAS_CONSTANT * pyro::warp_sum(cpp);
-    const double dcpm = GAS_CONSTANT * pyro::warp_sum(dcpp);
+    const double sigma = pyro::group_sum(sig, gid, t, red);
+    const double cpm = GAS_CONSTANT * pyro::group_sum(cpp, gid, t, red);
+    const double dcpm = GAS_CONSTANT * pyro::group_sum(dcpp, gid, t, red);
     const double rho = P / (GAS_CONSTANT * T * sigma);
     double ct = 0.0;
-    for (int k = lane; k < NS; k += 32) {
+    for (int k = t; k < NS; k += JGROUP) {
       const double v =
           __ldg(jg_invmw + k) * rho * __ldg(Y + (int64_t)k * ldy + i);
       sc[k] = v;
@@ -506,12 +545,12 @@ __global__ void __launch_bounds__(JWARPS * 32)
     s.lnT = lnT;
     s.invT = invT;
     s.c0 = LOG_P0_OVER_R - lnT;
-    s.ctot = pyro::warp_sum(ct);
-    __syncwarp();
-    // per reaction (lanes over the kind-sorted numbering)
-    for (int qq = lane; qq < NR; qq += 32)
+    s.ctot = pyro::group_sum(ct, gid, t, red);
+    pyro::group_sync(gid);
+    // per reaction (threads over the kind-sorted numbering)
+    for (int qq = t; qq < NR; qq += JGROUP)
       pyro::jac_reaction(qq, s, c, g, h, D, Dq, DdT, Hq, Qc);
-    __syncwarp();
+    pyro::group_sync(gid);
     // per species k: w_k, dw_k/dT|c, the rank-1 third-body vector a_k,
     // u_k = sum_m dw_k/dc_m c_m and the column sum
     // shj_k = RT sum_j h_j dw_j/dc_k, from per-reaction sums; then the
@@ -519,7 +558,7 @@ __global__ void __launch_bounds__(JWARPS * 32)
     const double RT = GAS_CONSTANT * T;
     const double inv_sig = 1.0 / sigma;
     double pQ = 0.0, pHA = 0.0, pHU = 0.0, pdQ = 0.0;
-    for (int k = lane; k < NS; k += 32) {
+    for (int k = t; k < NS; k += JGROUP) {
       double w = 0.0, jt = 0.0, a = 0.0, u = 0.0, hj = 0.0;
       const int t1 = __ldg(jg_si0 + k + 1);
       for (int t = __ldg(jg_si0 + k); t < t1; ++t) {
@@ -552,26 +591,28 @@ __global__ void __launch_bounds__(JWARPS * 32)
       sg[k] = wk_rho * fma(a, rho, (w - u) * inv_sig);  // B_k
       sjt[k] = wk_rho * (jt - u * invT + w * invT);     // column 0
     }
-    const double Q = pyro::warp_sum(pQ), HA = pyro::warp_sum(pHA);
-    const double HU = pyro::warp_sum(pHU), dQdT = pyro::warp_sum(pdQ);
+    const double Q = pyro::group_sum(pQ, gid, t, red);
+    const double HA = pyro::group_sum(pHA, gid, t, red);
+    const double HU = pyro::group_sum(pHU, gid, t, red);
+    const double dQdT = pyro::group_sum(pdQ, gid, t, red);
     const double rcp = rho * cpm;
     const double inv_rcp = 1.0 / rcp;
     const double qr2 = Q * inv_rcp * inv_rcp;
     if (F != nullptr) {
-      // dT/dt = -Q / (rho cp), dY_k/dt = W_k w_k / rho (the lane that
+      // dT/dt = -Q / (rho cp), dY_k/dt = W_k w_k / rho (the thread that
       // formed w_k stores it)
-      if (lane == 0) F[i] = -Q * inv_rcp;
-      for (int k = lane; k < NS; k += 32)
+      if (t == 0) F[i] = -Q * inv_rcp;
+      for (int k = t; k < NS; k += JGROUP)
         F[(int64_t)(k + 1) * ldf + i] = __ldg(jg_mw + k) * sw[k] / rho;
     }
-    __syncwarp();
+    pyro::group_sync(gid);
     // rows 1..S, columns 1..S: d(dY_k/dt)/dY_m = W_k/rho ((Jc + a_k) rho
     //   / W_m + (w_k - u_k) / (sigma W_m)) = (W_k Jc_km + B_k) / W_m with
     // Jc = dw/dc.  Elements of dw/dc without contributions are B_k / W_m;
     // the others are summed by the lane that owns them (its run of the
     // update list) and stored once, transformed, with no read-back.
     for (int it = 0; it < JZ_ITERS; ++it) {
-      const int off = __ldg(jz_off + it * 32 + lane);
+      const int off = __ldg(jz_off + it * JGROUP + t);
       if (off != 0xFFFF) {
         const int k = off / NC - 1, m = off - (k + 1) * NC - 1;
         Ji[off] = __ldg(jg_invmw + m) * sg[k];
@@ -581,7 +622,7 @@ __global__ void __launch_bounds__(JWARPS * 32)
       int cur = -1;
       double acc = 0.0;
       for (int it = 0; it < JU_ITERS; ++it) {
-        const int e = it * 32 + lane;
+        const int e = it * JGROUP + t;
         const int off = __ldg(ju_off + e);
         const double cf = __ldg(ju_coef + e);
         const double dv = D[__ldg(ju_src + e)];
@@ -601,7 +642,7 @@ __global__ void __launch_bounds__(JWARPS * 32)
       }
     }
     // row 0: d(dT/dt)/dx
-    for (int col = lane; col < NC; col += 32) {
+    for (int col = t; col < NC; col += JGROUP) {
       double v;
       if (col == 0) {
         v = -dQdT * inv_rcp + qr2 * (-rcp * invT + rho * dcpm);
@@ -616,8 +657,8 @@ __global__ void __launch_bounds__(JWARPS * 32)
       Ji[col] = v;
     }
     // column 0 of rows 1..S
-    for (int k = lane; k < NS; k += 32) Ji[(int64_t)(k + 1) * NC] = sjt[k];
-    __syncwarp();
+    for (int k = t; k < NS; k += JGROUP) Ji[(int64_t)(k + 1) * NC] = sjt[k];
+    pyro::group_sync(gid);
   }
 }
 

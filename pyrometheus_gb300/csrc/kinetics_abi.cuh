@@ -303,14 +303,14 @@ int launch_reactor_jacobian(const double* p, int64_t p_inc, const double* T,
                             int64_t t_inc, const double* Y, int64_t ldy,
                             double* F, int64_t ldf, double* J, int64_t ldj,
                             int64_t n, cudaStream_t stream) {
-  const size_t sm = (size_t)JWARPS * JW_DOUBLES * sizeof(double);
+  const size_t sm = (size_t)JGROUPS * JW_DOUBLES * sizeof(double);
   if (prepare_smem((const void*)k_reactor_jacobian, sm) != PYRO_OK)
     return PYRO_ERR_LAUNCH;
-  const int64_t blocks = (n + JWARPS - 1) / JWARPS;
+  const int64_t blocks = (n + JGROUPS - 1) / JGROUPS;
   const int grid =
       (int)(blocks < (int64_t)pyro_sm_count() * 8 ? blocks
                                                    : (int64_t)pyro_sm_count() * 8);
-  k_reactor_jacobian<<<grid, JWARPS * 32, sm, stream>>>(
+  k_reactor_jacobian<<<grid, JGROUPS * JGROUP, sm, stream>>>(
       p, p_inc, T, t_inc, Y, ldy, J, ldj, F, ldf, n);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
