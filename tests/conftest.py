@@ -30,7 +30,8 @@ def load_golden(name):
 # and the reference's own test fixtures (test/mechs/*.yaml, the set
 # test/CMakeLists.txt:9 runs every backend on), all with golden vectors
 # from the reference's generated class
-FIXTURE_SETS = ["ref_uiuc", "ref_sandiego", "ref_hong", "ref_uconn32"]
+FIXTURE_SETS = ["ref_uiuc", "ref_sandiego", "ref_hong", "ref_uconn32",
+                "ref_gri30"]
 GOLDEN_SETS = ["synthetic9", "synthetic53", "quirks9"] + FIXTURE_SETS
 
 
