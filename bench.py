@@ -428,32 +428,6 @@ def _cpu_flamelet(sol, prof, h, lengths):
     return FlameletOracle(sol), d
 
 
-def flamelet_cpu_baseline(sol, prof, h, lengths):
-    """One flamelet Newton step (enthalpy Newton, residual, central-
-    difference source Jacobian, blocks, numpy block_thomas) of a flamelet
-    of about the mean length, on the oracle; flamelet steps/s."""
-    import numpy as np
-
-    from oracle.block_thomas_oracle import block_thomas
-    fo, d = _cpu_flamelet(sol, prof, h, lengths)
-    visc = np.zeros(d["n"])
-
-    def step():
-        r = fo.residual(d["h"], d["Y"], d["chi"], visc, d["T"], 1e5,
-                        d["h"][0], d["h"][-1], d["Y"][:, 0], d["Y"][:, -1],
-                        d["dx"])
-        sj = fo.source_jacobian_fd(d["h"], d["Y"], visc, d["T"], 1e5)
-        lo, c, up = fo.blocks(sj, d["chi"], d["dx"])
-        block_thomas(lo, c, up, -r.T)
-
-    dt = _cpu_timed(step)
-    return {"value": 1.0 / dt, "unit": "flamelet Newton steps/s",
-            "cores": _blas_threads(), "kind": "port",
-            "sample": f"one {d['n']}-point flamelet of the workload (oracle "
-                      "numpy restatement, central-difference source "
-                      "Jacobian)"}
-
-
 def eos_cpu_baseline(sol, prof, h, lengths, pdf):
     """``eos_gradient`` of a flamelet of about the mean length on the
     oracle (central-difference source Jacobian, R T gradient and dS/dp;
@@ -583,7 +557,7 @@ def secondary_legs(sol, th, dev, dfma):
         torch.cuda.empty_cache()
     out["block_thomas"] = bt
     torch.cuda.empty_cache()
-    out["flamelet_newton"] = flamelet_newton_legs(dev, dfma)
+    out["flamelet_solve"] = flamelet_solve_leg(dev)
     out["eos_adjoint"] = eos_adjoint_legs(dev)
     return out
 
@@ -673,78 +647,153 @@ def transport_leg(sol, th, dev, dfma, t, p, y, T, P, Y):
                                    "numpy restatement)"}}
 
 
-def flamelet_newton_legs(dev, dfma):
-    """One steady-flamelet Newton step over 4,096 flamelets (N ~ U[64,
-    1024], seeded profiles) for the 9- and 53-species mechanisms: T from
-    the enthalpy by Newton, the residual, the source Jacobian through the
-    analytic reactor Jacobian and the block assembly on the device, then
-    the batched block-Thomas solve (the solver's CUDA graph)."""
+def _sandiego():
+    """The reference's flamelet-notebook mechanism (sandiego: 9 species,
+    24 reactions), from the golden vectors generated by the reference's own
+    code on its test fixture (stored there in SI units)."""
+    import numpy as np
+
+    from pyrometheus_gb300.yaml_mech import load_mechanism
+    g = np.load(os.path.join(ROOT, "tests", "golden", "ref_sandiego.npz"))
+    return load_mechanism("sandiego.yaml", text=str(g["mech_yaml"]))
+
+
+def flamelet_problem(sol, th, lengths, chi_st, dev):
+    """Steady H2/air flamelets as the reference's notebook sets them up
+    (``examples/flamelet/flamelet.ipynb``): oxidizer O2:0.21/N2:0.79 at
+    500 K, fuel H2:0.5/N2:0.5 at 300 K, one atmosphere, enthalpy linear in
+    the mixture fraction, dissipation rate ``chi_st bell(Z)/bell(Z_st)``
+    inside and ``2 dx^2`` at the two boundary points, no viscous heating.
+    The start is the Burke-Schumann composition (the notebook starts from
+    Cantera equilibrium compositions)."""
     import numpy as np
     import torch
 
-    from pyrometheus_gb300 import get_thermochem_class, synthetic
-    from pyrometheus_gb300.flamelet import (BlockThomasSolver,
-                                            FlameletEquations)
-    res = {}
-    for tag, sol in (("s9", synthetic.config1_mechanism()),
-                     ("s53", synthetic.config2_mechanism())):
-        lengths = np.random.default_rng(3).integers(64, 1025, size=4096)
-        prof = synthetic.flamelet_profiles(sol, lengths, seed=4)
-        th = get_thermochem_class(sol)(device=dev)
-        eq = FlameletEquations(th, lengths, prof["dx"], prof["y_ox"],
-                               prof["y_fu"], device=dev)
-        Y = torch.as_tensor(prof["Y"], device=dev)
-        T0 = torch.as_tensor(prof["T"], device=dev)
-        h = th.get_mixture_enthalpy_mass(T0, Y)
-        chi = torch.as_tensor(prof["chi"], device=dev)
-        visc = torch.zeros_like(chi)
-        offs = np.concatenate([[0], np.cumsum(lengths)])
-        h_ox, h_fu = h[offs[:-1]], h[offs[1:] - 1]
-        nv, rows = sol.n_species + 1, int(offs[-1])
-        f64 = dict(dtype=torch.float64, device=dev)
-        blocks = tuple(torch.empty((rows, nv, nv), **f64) for _ in range(3))
-        solver = BlockThomasSolver(nv, lengths, device=dev, use_graph=True)
-        x = torch.empty((rows, nv), **f64)
-        b = torch.empty((rows, nv), **f64)
+    from pyrometheus_gb300.flamelet_utils import (
+        bell_profile, burke_schumann, stoichiometric_mixture_fraction)
+    S = sol.n_species
+    W = np.asarray(sol.molecular_weights)
+    idx = sol.species_index
 
-        def assemble():
-            T = eq.temperature(h, Y, T0)
-            R = eq.rhs(h, Y, chi, visc, None, 1e5, h_ox, h_fu, temperature=T)
-            eq.jac(h, Y, chi, visc, None, 1e5, temperature=T, out=blocks)
-            b.copy_((-R).T)
-            return R
+    def from_x(d):
+        x = np.zeros(S)
+        for k, v in d.items():
+            x[idx(k)] = v
+        return x * W / np.dot(x, W)
 
-        def solve():
-            solver.solve(*blocks, b, out=x)
+    y_ox = from_x({"O2": 0.21, "N2": 0.79})
+    y_fu = from_x({"H2": 0.5, "N2": 0.5})
+    z_st = stoichiometric_mixture_fraction(sol, y_ox, y_fu)
 
-        R0 = assemble()
-        solve()
-        torch.cuda.synchronize()
-        ms_a = _event_ms(assemble, 2)
-        ms_s = _event_ms(solve, 2)
-        solver.check_status()
-        # residual after applying the correction once (a full, undamped
-        # step from these synthetic profiles may leave the state where the
-        # enthalpy Newton cannot follow; that is reported, not raised)
-        try:
-            r_after = float(eq.rhs(h + x[:, 0], Y + x[:, 1:].T, chi, visc,
-                                   T0, 1e5, h_ox, h_fu).abs().max())
-        except RuntimeError as exc:
-            r_after = f"not evaluated: {exc}"
-        flops = rows * (14.0 / 3.0) * nv ** 3
-        res[tag] = {
-            "flamelets": len(lengths), "points": rows, "nv": nv,
-            "assembly_ms": ms_a, "solve_ms": ms_s,
-            "newton_steps_per_s": len(lengths) / (ms_a + ms_s) * 1e3,
-            "points_per_s_assembly": rows / ms_a * 1e3,
-            "solve_fp64_frac": flops / ms_s / 1e9 / (dfma / 1e12),
-            "residual_inf_before": float(R0.abs().max()),
-            "residual_inf_after": r_after,
-            "block_thomas": f"{solver.kernel}:{solver.threads}",
-            "cpu_baseline": flamelet_cpu_baseline(sol, prof, h, lengths)}
-        del blocks, solver, x, b, eq, th, Y, h, R0
-        torch.cuda.empty_cache()
-    return res
+    def f64(x):
+        return torch.as_tensor(np.asarray(x, dtype=np.float64), device=dev)
+
+    h_ox = float(th.get_mixture_enthalpy_mass(f64([500.0]),
+                                              f64(y_ox[:, None]))[0])
+    h_fu = float(th.get_mixture_enthalpy_mass(f64([300.0]),
+                                              f64(y_fu[:, None]))[0])
+    hs, ys, chis, dxs = [], [], [], []
+    for n, cs in zip(lengths, chi_st):
+        n = int(n)
+        z = np.linspace(0.0, 1.0, n)
+        dx = 1.0 / (n - 1)
+        chi = cs * bell_profile(np.clip(z, 1e-12, 1.0 - 1e-12)) \
+            / bell_profile(z_st)
+        chi[0] = chi[-1] = 2.0 * dx ** 2
+        hs.append(h_ox + (h_fu - h_ox) * z)
+        ys.append(burke_schumann(sol, z, y_ox, y_fu))
+        chis.append(chi)
+        dxs.append(dx)
+    h = f64(np.concatenate(hs))
+    Y = f64(np.hstack(ys))
+    T = th.get_temperature_from_enthalpy(h, Y, torch.full_like(h, 1500.0))
+    return dict(h=h, Y=Y, chi=f64(np.concatenate(chis)), T=T, dx=dxs,
+                y_ox=y_ox, y_fu=y_fu, h_ox=h_ox, h_fu=h_fu, z_st=z_st)
+
+
+# the reference notebook's solver settings (newton maxiter/tol, bdf newton
+# maxiter/tol, bdf time step, bdf maxsteps, try newton first, max attempts)
+FLAMELET_CONFIG = (10, 1e-8, 20, 1e-9, 1e-5, 10, False, 10)
+
+
+def flamelet_solve_leg(dev, n_flamelets=4096):
+    """Converged steady flamelets: ``FlameletSolver.solve`` (the reference's
+    ``solver.py:476-600`` control flow per flamelet) on *n_flamelets*
+    H2/air flamelets of the real sandiego mechanism (:func:`flamelet_problem`)
+    with seeded grid lengths U[64, 1024] and stoichiometric dissipation
+    rates U[10, 100] 1/s, timed on the second of two identical solves (the
+    first builds the sub-batch plans); flamelet solves/s counts converged
+    flamelets.  The CPU baseline is the oracle driver on the notebook's own
+    101-point, chi_st = 100 flamelet."""
+    import numpy as np
+    import torch
+
+    from pyrometheus_gb300 import get_thermochem_class
+    from pyrometheus_gb300.flamelet_solver import FlameletSolver
+    sol = _sandiego()
+    th = get_thermochem_class(sol)(device=dev)
+    rng = np.random.default_rng(11)
+    lengths = rng.integers(64, 1025, size=n_flamelets)
+    chi_st = rng.uniform(10.0, 100.0, size=n_flamelets)
+    pb = flamelet_problem(sol, th, lengths, chi_st, dev)
+    fs = FlameletSolver(th, lengths, pb["dx"], (pb["y_ox"], pb["y_fu"]))
+    args = (False,) + FLAMELET_CONFIG + (
+        pb["chi"], torch.zeros_like(pb["chi"]), pb["T"], 101325.0,
+        pb["h_ox"], pb["h_fu"], (pb["h"], pb["Y"]))
+    fs.solve(*args)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    _, temp = fs.solve(*args)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    ls = fs.last_solve
+    conv = np.asarray(ls["converged"], dtype=bool)
+    stages = np.bincount(np.asarray(ls["stage"]) + 1, minlength=12)
+    offs = np.concatenate([[0], np.cumsum(lengths)])
+    tmax = np.array([float(temp[offs[i]:offs[i + 1]].max())
+                     for i in range(0, n_flamelets, 256)])
+    out = {"flamelets": n_flamelets, "points": int(offs[-1]), "nv": 10,
+           "mechanism": "sandiego (the reference notebook's), H2/air, "
+                        "Burke-Schumann start",
+           "chi_st": "U[10, 100] 1/s, seeded",
+           "wall_s": wall, "converged": int(conv.sum()),
+           "converged_solves_per_s": float(conv.sum()) / wall,
+           "stage_counts": {"none": int(stages[0]),
+                            **{str(k): int(stages[k + 1])
+                               for k in range(11) if stages[k + 1]}},
+           "T_max_sampled_K": [float(tmax.min()), float(tmax.max())],
+           "solver_config": "newton 10 / 1e-8, time march dt 1e-5 s x 10 "
+                            "steps (Newton 20 / 1e-9), up to 10 attempts "
+                            "(the notebook's)"}
+    out["cpu_baseline"] = flamelet_solve_cpu_baseline(sol, th, dev)
+    del fs, pb, th
+    torch.cuda.empty_cache()
+    return out
+
+
+def flamelet_solve_cpu_baseline(sol, th, dev, cap_s=60.0):
+    """The oracle driver (one flamelet, numpy, central-difference source
+    Jacobian, numpy block-Thomas) on the reference notebook's flamelet: 101
+    points, chi_st = 100; flamelet solves/s."""
+    import numpy as np
+
+    from oracle.flamelet_solver_oracle import FlameletSolverOracle
+    pb = flamelet_problem(sol, th, [101], [100.0], dev)
+    orc = FlameletSolverOracle(sol, pb["dx"][0], pb["y_ox"], pb["y_fu"])
+    phi = np.vstack([pb["h"].cpu().numpy(), pb["Y"].cpu().numpy()])
+    chi = pb["chi"].cpu().numpy()
+    with np.errstate(all="ignore"):
+        t0 = time.perf_counter()
+        _, _, rec = orc.solve(*FLAMELET_CONFIG, chi, np.zeros(101),
+                              pb["T"].cpu().numpy(), 101325.0, pb["h_ox"],
+                              pb["h_fu"], phi)
+        dt = time.perf_counter() - t0
+    return {"value": 1.0 / dt, "unit": "flamelet solves/s",
+            "cores": _blas_threads(), "kind": "port",
+            "stage": int(rec["stage"]),
+            "sample": "the reference notebook's flamelet (sandiego, 101 "
+                      "points, chi_st = 100), oracle driver (numpy, "
+                      "central-difference source Jacobian)"}
 
 
 def eos_adjoint_legs(dev):
