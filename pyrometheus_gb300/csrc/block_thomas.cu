@@ -725,7 +725,7 @@ __global__ void __launch_bounds__(kSegWarps * 32)
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
         long long bk = elig ? abs_key(a[k]) : -2LL;
-        int bp = pos, bl = lane;
+        int bpl = (pos << 8) | lane;  // position, then lane, in one int
         // segmented argmax: after the rounds with offsets 1, 2, 4, 8 each
         // lane holds the best of positions [r, r + 2^rounds) mod NV
 #pragma unroll
@@ -733,19 +733,18 @@ __global__ void __launch_bounds__(kSegWarps * 32)
           const int rr = r + off;
           const int src = base + (rr >= NV ? rr - NV : rr);
           const long long ok = __shfl_sync(0xffffffffu, bk, src);
-          const int op = __shfl_sync(0xffffffffu, bp, src);
-          const int ol = __shfl_sync(0xffffffffu, bl, src);
-          if (ok > bk || (ok == bk && op < bp)) {
-            bk = ok;
-            bp = op;
-            bl = ol;
-          }
+          const int opl = __shfl_sync(0xffffffffu, bpl, src);
+          // larger |a| first, then the lower position
+          const bool take = ok > bk || (ok == bk && opl < bpl);
+          bk = take ? ok : bk;
+          bpl = take ? opl : bpl;
         }
+        const int bp = bpl >> 8, bl = bpl & 0xff;
         if (bk == 0 && act) singular = true;
         if (r == k) mypiv = bp;
         const bool is_piv = lane == bl;
         const double pv = __shfl_sync(0xffffffffu, a[k], bl);
-        const double inv = 1.0 / pv;
+        const double inv = pyro_rcp(pv);
         const double m = is_piv ? 0.0 : a[k] * inv;
         if (elig && !is_piv) lu[k] = m;  // getrf's multiplier
         if (is_piv) {
@@ -832,7 +831,7 @@ __global__ void __launch_bounds__(kSegWarps * 32)
         if (r > k) y = fma(-f[k], yk, y);
       }
       // upper: x_r = (y_r - sum_{k > r} U[r][k] x_k) / U[r][r]
-      const double inv = 1.0 / d;
+      const double inv = pyro_rcp(d);
 #pragma unroll
       for (int k = NV - 1; k >= 0; --k) {
         if (r == k) y *= inv;

@@ -59,3 +59,30 @@ PYRO_EXPORT int pyro_log_check(const double* x, double* mine, double* ref,
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
+
+namespace {
+
+__global__ void k_rcpcheck(const double* __restrict__ x, double* mine,
+                           double* ref, int64_t n) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x) {
+    const double v = x[i];
+    mine[i] = pyro_rcp(v);
+    ref[i] = 1.0 / v;
+  }
+}
+
+}  // namespace
+
+// mine[i] = pyro_rcp(x[i]), ref[i] = CUDA's 1.0 / x[i].  Device pointers;
+// asynchronous on stream.
+PYRO_EXPORT int pyro_rcp_check(const double* x, double* mine, double* ref,
+                               int unused, int64_t n, cudaStream_t stream) {
+  (void)unused;
+  if (n < 0 || (n > 0 && (!x || !mine || !ref))) return PYRO_ERR_ARGUMENT;
+  if (n == 0) return PYRO_OK;
+  k_rcpcheck<<<pyro_grid(n, 256, pyro_sm_count() * 4), 256, 0, stream>>>(
+      x, mine, ref, n);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}

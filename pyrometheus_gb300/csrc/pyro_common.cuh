@@ -57,3 +57,20 @@ __device__ __forceinline__ double pyro_ld(const double* __restrict__ p,
                                           int64_t inc, int64_t i) {
   return __ldg(p + inc * i);
 }
+
+// 1/x by Newton-Raphson (Markstein, IBM J. Res. Dev. 34(1), 1990): the
+// hardware approximation rcp.approx.ftz.f64 as the seed, then two steps of
+// r <- r + r (1 - x r), each roughly doubling the correct bits; within an
+// ulp of the correctly rounded reciprocal for normal x whose reciprocal is
+// normal, and branch-free (so the scheduler can overlap it with
+// independent work), unlike the IEEE division.  x = 0 or a subnormal x
+// gives nan, not inf; callers use it on pivots they flag as singular when
+// zero.
+__device__ __forceinline__ double pyro_rcp(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  r = fma(r, e, r);
+  e = fma(-x, r, 1.0);
+  return fma(r, e, r);
+}

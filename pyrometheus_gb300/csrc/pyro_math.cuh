@@ -117,3 +117,4 @@ __device__ __forceinline__ double pyro_log(double x) {
 __device__ __forceinline__ double pyro_log10(double x) {
   return pyro_log(x) * PYRO_LOG_INV_LN10;
 }
+

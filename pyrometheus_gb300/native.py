@@ -113,6 +113,9 @@ def mathcheck_lib() -> ctypes.CDLL:
     lib.pyro_log_check.restype = ctypes.c_int
     lib.pyro_log_check.argtypes = [ctypes.c_void_p] * 3 + [
         ctypes.c_int, ctypes.c_int64, ctypes.c_void_p]
+    lib.pyro_rcp_check.restype = ctypes.c_int
+    lib.pyro_rcp_check.argtypes = [ctypes.c_void_p] * 3 + [
+        ctypes.c_int, ctypes.c_int64, ctypes.c_void_p]
     return lib
 
 

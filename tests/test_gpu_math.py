@@ -1,6 +1,6 @@
-"""The table-driven exponential (Tang 1989) and logarithm (Tang 1990) of
-csrc/pyro_math.cuh against CUDA's double-precision exp/exp10/log/log10 on
-the device."""
+"""The table-driven exponential (Tang 1989) and logarithm (Tang 1990) and
+the Newton-Raphson reciprocal of csrc/pyro_math.cuh against CUDA's
+double-precision exp/exp10/log/log10 and division on the device."""
 
 import numpy as np
 import pytest
@@ -80,3 +80,21 @@ def test_log_against_cuda():
         # both within about 1 ulp of the logarithm: a few ulps apart
         assert rel.max() < 1e-15, (ten, rel.max())
         assert np.all(same[~finite])
+
+
+def test_rcp_against_cuda_division():
+    """Within an ulp of CUDA's correctly rounded 1.0 / x over the normal
+    range whose reciprocals are normal, and equal to it on most
+    arguments."""
+    rng = np.random.default_rng(3)
+    mag = 10.0 ** rng.uniform(-300.0, 300.0, 2_000_000)
+    x = np.concatenate([
+        mag * rng.choice([-1.0, 1.0], mag.size),
+        rng.uniform(0.5, 2.0, 1_000_000),
+        1.0 + np.arange(-300, 300) / 2 ** 40,
+        [1.0, -1.0, 2.0, 0.5, 3.0, 10.0, np.nextafter(1.0, 0.0),
+         np.nextafter(1.0, 2.0)]])
+    mine, ref = _run(x, 0, "pyro_rcp_check")
+    rel = np.abs(mine - ref) / np.abs(ref)
+    assert rel.max() <= 2.3e-16, rel.max()
+    assert np.mean(mine == ref) > 0.9
