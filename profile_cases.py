@@ -8,6 +8,7 @@
     python profile_cases.py transport [states]
     python profile_cases.py serving [cells] [launches]
     python profile_cases.py flamelet_solve [copies]
+    python profile_cases.py peaks [repeats]
 
 Each case builds its inputs on the current CUDA device (inputs larger than
 the 129 MB L2 at the default sizes, a few GB at most), runs the kernel three
@@ -217,6 +218,28 @@ def flamelet_solve(copies: int = 256):
           f"{'/'.join(str(int(c)) for c in stages[:4])}")
 
 
+def peaks(repeats: int = 5):
+    """The FP64 rates the rooflines use, measured live: DFMA FLOP/s, CUDA's
+    double exp and log per second, and the FP64 tensor-core rate of
+    mma.sync m8n8k4 and m16n8k16 (flops per second), printed as JSON."""
+    import json
+
+    import torch
+
+    from pyrometheus_gb300 import native
+    dev = _dev()
+    scratch = torch.empty(int(native.peaks_scratch_doubles()),
+                          dtype=torch.float64, device=dev)
+    dfma, exp_rate, log_rate = native.measure_fp64(scratch, repeats)
+    dmma_s, dmma_l = native.measure_dmma(scratch, repeats)
+    rcp = native.measure_fp64_rcp(scratch, repeats)
+    print(json.dumps({"dfma_flops": dfma, "exp_per_s": exp_rate,
+                      "log_per_s": log_rate, "rcp_per_s": rcp,
+                      "dmma_m8n8k4_flops": dmma_s,
+                      "dmma_m16n8k16_flops": dmma_l,
+                      "dmma_over_dfma": max(dmma_s, dmma_l) / dfma}))
+
+
 def main(argv=None):
     argv = list(sys.argv[1:] if argv is None else argv)
     if not argv:
@@ -238,6 +261,8 @@ def main(argv=None):
         serving(*rest)
     elif case == "flamelet_solve":
         flamelet_solve(*rest)
+    elif case == "peaks":
+        peaks(*rest)
     else:
         raise SystemExit(f"unknown case {case!r}")
     print("ok")
