@@ -4,6 +4,7 @@
     python profile_cases.py vjp [states]
     python profile_cases.py block_thomas [nv] [systems] [n_min] [n_max]
     python profile_cases.py block_thomas_seg [nv] [systems] [n_min] [n_max]
+    python profile_cases.py block_thomas_resolve [nv] [systems] [n_min] [n_max]
     python profile_cases.py batched_lu [nv] [cells]
     python profile_cases.py transport [states]
     python profile_cases.py serving [cells] [launches]
@@ -57,13 +58,14 @@ def jacobian(states: int = 1 << 15, vjp: bool = False):
     else:
         nc = sol.n_species + 1
         J = torch.empty((states, nc, nc), dtype=torch.float64, device=dev)
+        F = torch.empty((nc, states), dtype=torch.float64, device=dev)
         for _ in range(3):
-            th.get_reactor_jacobian(P, T, Y, out=J)
+            th.get_reactor_source_and_jacobian(P, T, Y, out=(F, J))
     torch.cuda.synchronize()
 
 
 def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
-                 n_max: int = 1024, kernel=None):
+                 n_max: int = 1024, kernel=None, resolve=False):
     import torch
 
     from pyrometheus_gb300.flamelet import BlockThomasSolver
@@ -81,6 +83,10 @@ def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
     solver = BlockThomasSolver(nv, lengths, device=dev, kernel=kernel)
     for _ in range(3):
         solver.solve(L, C, U, b)
+    if resolve:
+        B = torch.randn((2, rows, nv), generator=g, **f64)
+        for _ in range(3):
+            solver.resolve(L, U, B)
     torch.cuda.synchronize()
 
 
@@ -253,6 +259,8 @@ def main(argv=None):
         block_thomas(*rest)
     elif case == "block_thomas_seg":
         block_thomas(*rest, kernel="seg")
+    elif case == "block_thomas_resolve":
+        block_thomas(*rest, resolve=True)
     elif case == "batched_lu":
         batched_lu(*rest)
     elif case == "transport":
