@@ -605,7 +605,7 @@ PYRO_EXPORT int pyro_block_thomas_small(const double* L, const double* C,
 // pivoting.  Row interchanges are relabellings (a lane keeps its row and
 // tracks the position LAPACK's swaps would move it to); the pivot is the
 // largest |a| of the eligible rows, ties to the lowest position, as getrf
-// chooses it.  Below the pivot the pass is LU's elimination (its
+// chooses it (up to candidates equal to 2^-16 relative, see pivot_key).  Below the pivot the pass is LU's elimination (its
 // multipliers and the pivot rows are exactly getrf's factors, kept in the
 // workspace in the layout of the kernels above); above the pivot it also
 // eliminates (Gauss-Jordan), which in SIMT costs nothing extra: the lanes
@@ -632,10 +632,19 @@ struct SegCfg {
                                 : NV <= 8 ? 3 : 4;
 };
 
-__device__ __forceinline__ long long abs_key(double v) {
-  // |v|'s bit pattern orders like |v|; NaN ranks below every number
-  const long long b = __double_as_longlong(v) & 0x7fffffffffffffffLL;
-  return b > 0x7ff0000000000000LL ? -1LL : b;
+// Pivot key of an eligible row: the top 27 bits of |v|'s bit pattern
+// (exponent and 16 mantissa bits, which order like |v|), then 15 - position
+// in the low 4 bits, so one unsigned max picks the largest |v| and, among
+// candidates equal to 2^-16 relative, the lowest position -- getrf's
+// choice up to those near-ties.  NaN and zero rank lowest (key bits 0);
+// rows already pivoted are not candidates (key 0, below every candidate
+// through the position bits being at most 15 and eligibility ORed in).
+__device__ __forceinline__ unsigned pivot_key(double v, int pos) {
+  const unsigned long long b =
+      (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffULL;
+  const unsigned top =
+      b > 0x7ff0000000000000ULL ? 0u : (unsigned)(b >> 36);  // 27 bits
+  return (top << 5) | 16u | (unsigned)(15 - pos);
 }
 
 template <int NV>
@@ -657,6 +666,11 @@ __global__ void __launch_bounds__(kSegWarps * 32)
   // lanes past the last segment (32 mod NV of them) own no system and no
   // shared rows; they read segment 0's rows and never write them
   double* st = s_st[wid] + (seg < P ? seg : 0) * NV * RS;
+  // this lane's segment as a lane mask (the lanes past the last segment
+  // form one group of their own)
+  const unsigned segmask =
+      seg < P ? (((1u << NV) - 1u) << base)
+              : (P * NV >= 32 ? 0u : ~((1u << (P * NV)) - 1u));
   for (;;) {
     int q0 = 0;
     if (lane == 0) q0 = atomicAdd(counter, P);
@@ -724,23 +738,20 @@ __global__ void __launch_bounds__(kSegWarps * 32)
       double myinv = 0.0, lu[NV];
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
-        long long bk = elig ? abs_key(a[k]) : -2LL;
-        int bpl = (pos << 8) | lane;  // position, then lane, in one int
-        // segmented argmax: after the rounds with offsets 1, 2, 4, 8 each
-        // lane holds the best of positions [r, r + 2^rounds) mod NV
+        // segmented argmax of the 32-bit keys: after the rounds with
+        // offsets 1, 2, 4, 8 each lane holds the largest key of positions
+        // [r, r + 2^rounds) mod NV of its segment
+        unsigned best = elig ? pivot_key(a[k], pos) : 0u;
 #pragma unroll
         for (int o = 0, off = 1; o < Cfg::ROUNDS; ++o, off <<= 1) {
           const int rr = r + off;
           const int src = base + (rr >= NV ? rr - NV : rr);
-          const long long ok = __shfl_sync(0xffffffffu, bk, src);
-          const int opl = __shfl_sync(0xffffffffu, bpl, src);
-          // larger |a| first, then the lower position
-          const bool take = ok > bk || (ok == bk && opl < bpl);
-          bk = take ? ok : bk;
-          bpl = take ? opl : bpl;
+          best = max(best, __shfl_sync(0xffffffffu, best, src));
         }
-        const int bp = bpl >> 8, bl = bpl & 0xff;
-        if (bk == 0 && act) singular = true;
+        const int bp = 15 - (int)(best & 15u);
+        const unsigned won = __ballot_sync(0xffffffffu, elig && pos == bp);
+        const int bl = __ffs(won & segmask) - 1;
+        if ((best >> 5) == 0 && act) singular = true;
         if (r == k) mypiv = bp;
         const bool is_piv = lane == bl;
         const double pv = __shfl_sync(0xffffffffu, a[k], bl);
