@@ -209,7 +209,56 @@ def _sample_jobs(target_s: float, per_state_s: float, lanes: int,
     return [(chunk, 1000 + i) for i in range(total // chunk)]
 
 
+def _ref_cpp_sample(n, seed):
+    """(library, inputs) for timing the reference's generated C++ on *n*
+    seeded states of the workload, or None where its header was never
+    rendered (``oracle/ref_cpp.py``)."""
+    from oracle import ref_cpp
+    if not ref_cpp.available("synthetic53"):
+        return None
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    from pyrometheus_gb300 import synthetic
+    sol = synthetic.config2_mechanism()
+    t, p, y = synthetic.sample_states(sol, n, seed=seed)
+    e = Oracle(sol).get_mixture_internal_energy_mass(t, y)
+    return ref_cpp.load("synthetic53"), (p, t, y, e)
+
+
+def _ref_cpp_rate(lib, inputs, threads):
+    from oracle import ref_cpp
+    p, t, y, e = inputs
+    t0 = time.perf_counter()
+    ref_cpp.fused_step(lib, p, t, y, e, 1500.0, threads)
+    return t.shape[0] / (time.perf_counter() - t0)
+
+
+REF_CPP_SAMPLE = ("the reference's own generated C++ (its C++ target, "
+                  "pyrometheus/codegen/cpp.py, rendered for this mechanism "
+                  "and compiled with g++ -O3 by oracle/ref_cpp.py): "
+                  "get_density, get_net_production_rates, get_temperature "
+                  "per state")
+
+
 def cpu_baseline(target_s: float):
+    """States/s of the reference's generated C++ on one host core over a
+    bounded sample (about *target_s* seconds); the numpy oracle port where
+    that C++ was never rendered.  Only the evaluation is timed, not the
+    state generation."""
+    ref = _ref_cpp_sample(8192, 1000)
+    if ref is not None:
+        lib, inputs = ref
+        per_state = 1.0 / _ref_cpp_rate(lib, inputs, 1)
+        n = int(min(max(target_s / per_state, 8192), 2_000_000))
+        lib, inputs = _ref_cpp_sample(n, 1001)
+        v = _ref_cpp_rate(lib, inputs, 1)
+        return {"value": v, "unit": "states/s", "cores": 1,
+                "kind": "reference",
+                "sample": f"{n} states of the workload, {REF_CPP_SAMPLE}, "
+                          "1 thread"}
+    return _port_cpu_baseline(target_s)
+
+
+def _port_cpu_baseline(target_s: float):
     """States/s of the oracle port on one host core over a bounded sample
     (chunks of 16,384 states, about *target_s* seconds of work; only the
     evaluation is timed, not the state generation)."""
@@ -225,14 +274,36 @@ def cpu_baseline(target_s: float):
 
 
 def run_reference(args):
-    """The reference arm: the oracle port on all host cores (spawned worker
-    processes), each step a bounded sample of the workload."""
+    """The reference arm: the reference's own generated C++ on all host
+    cores (OpenMP threads), each step a bounded sample of the workload;
+    the oracle port in spawned worker processes where that C++ was never
+    rendered."""
     rank, world, _ = dist_info()
     if rank != 0:
         return
-    import multiprocessing as mp
     cores = len(os.sched_getaffinity(0))
     steps, warmup = max(1, args.steps), max(0, args.warmup)
+    ref = _ref_cpp_sample(16384, 1002)
+    if ref is not None:
+        lib, inputs = ref
+        per_state = 1.0 / _ref_cpp_rate(lib, inputs, cores)
+        # about min(cpu_seconds, 4) s per step
+        n = int(min(max(min(args.cpu_seconds, 4.0) / per_state, 16384),
+                    4_194_304))
+        lib, inputs = _ref_cpp_sample(n, 1003)
+        vals = []
+        for s_ in range(warmup + steps):
+            v = _ref_cpp_rate(lib, inputs, cores)
+            if s_ >= warmup:
+                vals.append(v)
+        v = statistics.median(vals)
+        base = {"value": v, "unit": "states/s", "cores": cores,
+                "kind": "reference",
+                "sample": f"{n} states of the workload per step, "
+                          f"{REF_CPP_SAMPLE}, {cores} OpenMP threads"}
+        _print_reference(args, world, v, base)
+        return
+    import multiprocessing as mp
     per_state = _oracle_chunk((2048, 7)) / 2048
     jobs = _sample_jobs(min(args.cpu_seconds, 4.0), per_state, cores)
     vals = []
@@ -251,6 +322,11 @@ def run_reference(args):
                       f"of {jobs[0][0]} over {cores} worker processes "
                       "(wall clock, oracle numpy restatement of the "
                       "reference's generated class)"}
+    _print_reference(args, world, v, base)
+
+
+def _print_reference(args, world, v, base):
+    steps, warmup = max(1, args.steps), max(0, args.warmup)
     out = {
         "metric": METRIC,
         "value": v, "unit": "states/s", "n_gpus": args.gpus, "steps": steps,

@@ -368,6 +368,26 @@ class StringifyMapper:
             self.rec(expr.condition, PREC_NONE, *args, **kwargs),
             self.rec(expr.else_, PREC_NONE, *args, **kwargs))
 
+class CCodeMapper(StringifyMapper):
+    """Renders expressions as C (``pymbolic.mapper.c_code.CCodeMapper``,
+    which the reference's C++ target subclasses, ``cpp.py:48-52``):
+    ``pow(a, b)`` for powers, ``(c ? a : b)`` for conditionals, ``&&`` /
+    ``||`` / ``!`` for logic; everything else as the Python mapper, whose
+    compound operands are always parenthesised (so the tree's evaluation
+    order is kept)."""
+
+    def map_power(self, expr, enclosing_prec, *args, **kwargs):
+        return "pow(%s, %s)" % (self.rec(expr.base, PREC_NONE, *args,
+                                         **kwargs),
+                                self.rec(expr.exponent, PREC_NONE, *args,
+                                         **kwargs))
+
+    def map_if(self, expr, enclosing_prec, *args, **kwargs):
+        return "(%s ? %s : %s)" % (
+            self.rec(expr.condition, PREC_NONE, *args, **kwargs),
+            self.rec(expr.then, PREC_NONE, *args, **kwargs),
+            self.rec(expr.else_, PREC_NONE, *args, **kwargs))
+
 # }}}
 
 
@@ -471,9 +491,12 @@ def _install_stubs():
     for name, val in globals().items():
         if name.startswith("PREC_"):
             setattr(stringifier, name, val)
+    c_code = types.ModuleType("pymbolic.mapper.c_code")
+    c_code.CCodeMapper = CCodeMapper
     pymbolic.primitives = prim
     pymbolic.mapper = mapper
     mapper.stringifier = stringifier
+    mapper.c_code = c_code
 
     mako = types.ModuleType("mako")
     mako_template = types.ModuleType("mako.template")
@@ -487,7 +510,8 @@ def _install_stubs():
 
     mods = {"cantera": ct, "pymbolic": pymbolic,
             "pymbolic.primitives": prim, "pymbolic.mapper": mapper,
-            "pymbolic.mapper.stringifier": stringifier, "mako": mako,
+            "pymbolic.mapper.stringifier": stringifier,
+            "pymbolic.mapper.c_code": c_code, "mako": mako,
             "mako.template": mako_template, "pyrometheus": pkg}
     return mods
 
@@ -543,6 +567,43 @@ class _TransportPlaceholder:
     @staticmethod
     def get_binary_diff_coeffs_polynomial(i, j):
         return np.array([1.0, 0.0, 0.0, 0.0, 0.0])
+
+
+_REF_CPP = None
+
+
+def reference_cpp_generator():
+    """The reference's ``CppCodeGenerator`` (``codegen/cpp.py``), imported
+    the same way."""
+    global _REF_CPP
+    if _REF_CPP is not None:
+        return _REF_CPP
+    if not reference_available():
+        raise RuntimeError("reference checkout not found (set "
+                           "PYRO_REFERENCE_ROOT to its root)")
+    mods = _install_stubs()
+    saved = {k: sys.modules.get(k) for k in mods}
+    saved.update({k: sys.modules.get(k) for k in
+                  ("pyrometheus.codegen", "pyrometheus.codegen.cpp",
+                   "pyrometheus.chem_expr")})
+    try:
+        sys.modules.update(mods)
+        cppcg = importlib.import_module("pyrometheus.codegen.cpp")
+        _REF_CPP = cppcg.CppCodeGenerator
+    finally:
+        for k, v in saved.items():
+            if v is None:
+                sys.modules.pop(k, None)
+            else:
+                sys.modules[k] = v
+    return _REF_CPP
+
+
+def reference_cpp_source(sol, name: str = "Thermochemistry") -> str:
+    """The C++20 header the reference's C++ target generates for *sol*."""
+    if getattr(sol, "transport", None) is None:
+        sol = _TransportPlaceholder(sol)
+    return reference_cpp_generator().generate(name, sol)
 
 
 def reference_source(sol, name: str = "Thermochemistry") -> str:
