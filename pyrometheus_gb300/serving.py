@@ -347,8 +347,17 @@ class ReactorPool:
                 if self._slots is None:
                     # the active cells of [0, n): rebuilt after admissions
                     # and harvests, so a fragmented pool launches only
-                    # threads that have a cell
-                    self._slots = torch.nonzero(self.active[:n]).flatten()
+                    # threads that have a cell; grouped by the octave of
+                    # the steps each has left ((t_end - t) / h), so the
+                    # cells of a warp use up their attempts together,
+                    # ascending slots within an octave so neighbouring
+                    # threads still read neighbouring cells (each cell's
+                    # arithmetic does not depend on the order)
+                    act = torch.nonzero(self.active[:n]).flatten()
+                    left = (self.t_end[act] - self.t[act]) / self.h[act]
+                    octave = torch.floor(torch.log2(torch.clamp(
+                        left, min=1.0, max=1e30)))
+                    self._slots = act[torch.argsort(octave, stable=True)]
                 self.done[:n].zero_()
                 if self._slots.numel():
                     be.fused_step(self, int(self._slots.numel()),
