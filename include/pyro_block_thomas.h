@@ -25,9 +25,12 @@ extern "C" {
 
 typedef struct CUstream_st* cudaStream_t;
 
-/* Doubles of workspace pyro_block_thomas needs for `rows` packed rows
- * (per row: the LU factors of the modified diagonal block C'_i, b'_i and
- * the pivots, kept for the backward solves). */
+/* Doubles of workspace the solvers need for `rows` packed rows
+ * (rows = row_off[nsys]): per row the LU factors of the modified diagonal
+ * block C'_i, b'_i and the pivots, kept for the backward solves and
+ * pyro_block_thomas_resolve; for nv <= 16 then, after all rows of those,
+ * S_i | t_i = C'_i^-1 (U_i | b'_i) of every row (nv x (nv + 1), written by
+ * pyro_block_thomas_seg for its backward sweep). */
 int64_t pyro_block_thomas_work_doubles(int nv, int64_t rows);
 
 /* Dynamic shared memory of one CTA for blocks of size nv. */
@@ -61,11 +64,14 @@ int pyro_block_thomas_small(const double* L, const double* C, const double* U,
 /* pyro_block_thomas for blocks of size nv <= 16 with 32 / nv systems per
  * warp (three at nv = 10), one lane per block row and the working rows in
  * registers: every lane of every FP64 instruction works, and nothing
- * synchronises beyond a warp.  Pivoting and the kept factors are getrf's,
- * in the workspace layout of pyro_block_thomas (so
- * pyro_block_thomas_resolve applies).  Same arguments as
- * pyro_block_thomas without the CTA size (one warp per CTA); ctas: grid
- * size (0 = all resident).  Replaces the same reference function,
+ * synchronises beyond a warp.  A persistent grid whose lane segments each
+ * take the next system of `order` when theirs is done; two launches (the
+ * forward sweep, then x_i = t_i - S_i x_{i+1} backward), the counter
+ * cleared before each.  Pivoting and the kept factors are getrf's, in the
+ * workspace layout of pyro_block_thomas (so pyro_block_thomas_resolve
+ * applies).  Same arguments as pyro_block_thomas without the CTA size
+ * (four warps per CTA); ctas: forward grid size (0 = one warp per SM
+ * partition).  Replaces the same reference function,
  * pyrometheus/flamelets/linear_solver.py:6-103. */
 int pyro_block_thomas_seg(const double* L, const double* C, const double* U,
                           const double* b, double* x, const int64_t* row_off,

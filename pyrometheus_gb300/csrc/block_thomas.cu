@@ -499,9 +499,12 @@ int launch_small(const double* L, const double* C, const double* U,
 
 }  // namespace
 
-// Doubles of workspace pyro_block_thomas needs for `rows` packed rows.
+// Doubles of workspace pyro_block_thomas needs for `rows` packed rows: per
+// row the factors, b' and the pivots; for nv <= 16 (the segmented kernel)
+// then S_i | t_i of every row after them.
 PYRO_EXPORT int64_t pyro_block_thomas_work_doubles(int nv, int64_t rows) {
-  return rows * ((int64_t)nv * nv + 2 * nv);
+  const int64_t st = nv <= 16 ? (int64_t)nv * (nv + 1) : 0;
+  return rows * ((int64_t)nv * nv + 2 * nv + st);
 }
 
 // Shared memory of one CTA for block size nv.
@@ -592,12 +595,24 @@ PYRO_EXPORT int pyro_block_thomas_small(const double* L, const double* C,
 // Small blocks, several systems per warp (nv <= 16).
 //
 // A warp-wide FP64 instruction costs GB300's narrow FP64 pipe the same
-// however many of its lanes are active, so small blocks need every lane
+// however many of its lanes are active (each SM partition retires one every
+// 64 cycles, and a dependent one no sooner), so small blocks need every lane
 // busy, and the CTA-per-system kernel above, whose 10 x 10 steps keep a few
 // lanes busy between barriers, cannot.  Here a system takes a segment of NV
-// consecutive lanes (P = 32 / NV systems per warp: three at nv = 10) and
+// consecutive lanes (P = 32 / NV segments per warp: three at nv = 10) and
 // lane r of a segment holds row r of the system's working blocks in
 // registers; nothing synchronises beyond the warp.
+//
+// Balance.  With the FP64 pipe of an SM partition the bound, the solve
+// takes as long as the busiest partition's FP64 instructions, so the work
+// is spread in units of one system per segment, not one warp's worth: the
+// grid is persistent (one warp per SM partition by default) and a segment
+// whose system is done takes the next one from the caller's order (longest
+// first), so every segment stays busy until the queue is empty.  Segments
+// of one warp are then at different rows of different systems, in lockstep
+// only as instruction streams; the forward and backward sweeps are two
+// kernels (two launches on the stream) so that every warp step runs one
+// sweep's instructions for all its segments.
 //
 // Forward sweep, per block row: C'_i | b'_i = (C_i | b_i) - L_{i-1}
 // (S_{i-1} | t_{i-1}) with S_{i-1} | t_{i-1} read from warp-private shared
@@ -605,23 +620,24 @@ PYRO_EXPORT int pyro_block_thomas_small(const double* L, const double* C,
 // pivoting.  Row interchanges are relabellings (a lane keeps its row and
 // tracks the position LAPACK's swaps would move it to); the pivot is the
 // largest |a| of the eligible rows, ties to the lowest position, as getrf
-// chooses it (up to candidates equal to 2^-16 relative, see pivot_key).  Below the pivot the pass is LU's elimination (its
-// multipliers and the pivot rows are exactly getrf's factors, kept in the
-// workspace in the layout of the kernels above); above the pivot it also
-// eliminates (Gauss-Jordan), which in SIMT costs nothing extra: the lanes
-// of rows above the pivot run the same instructions as the others.  Each
-// lane's right-hand-side row, scaled by its pivot's reciprocal, is then row
-// `pivot step` of S_i | t_i.  The backward sweep solves with the kept LU
-// factors, x_i = C'_i^-1 (b'_i - U_i x_{i+1}), as the reference does.
+// chooses it (up to candidates equal to 2^-16 relative, see pivot_key).
+// Below the pivot the pass is LU's elimination (its multipliers and the
+// pivot rows are exactly getrf's factors, kept in the workspace in the
+// layout of the kernels above); above the pivot it also eliminates
+// (Gauss-Jordan), which in SIMT costs nothing extra: the lanes of rows above
+// the pivot run the same instructions as the others.  Each lane's
+// right-hand-side row, scaled by its pivot's reciprocal, is then row
+// `pivot step` of S_i | t_i, kept in shared memory for the next row and in
+// the workspace for the backward sweep; t_{N-1} = x_{N-1} goes to x.  The
+// backward sweep is x_i = t_i - S_i x_{i+1}, the reference's x_i = C'_i^-1
+// (b'_i - U_i x_{i+1}) with C'_i^-1 applied in the forward sweep; the LU
+// factors are kept as well, for pyro_block_thomas_resolve.
 
 namespace {
 
-// one warp per CTA: the CTAs (one work item of 32 / nv systems each) are
-// all resident at once, and the hardware spreads them over the SMs round
-// robin, so every SM gets long and short systems alike (with four-warp
-// CTAs of consecutive longest-first items, SM loads differed 1.7-fold and
-// the FP64 pipe of the busiest SM was the only one kept busy)
-constexpr int kSegWarps = 1;
+// warps per CTA of the sweeps: four, so that a CTA's warps sit on the four
+// partitions of its SM
+constexpr int kSegWarps = 4;
 
 template <int NV>
 struct SegCfg {
@@ -647,6 +663,75 @@ __device__ __forceinline__ unsigned pivot_key(double v, int pos) {
   return (top << 5) | 16u | (unsigned)(15 - pos);
 }
 
+// Lane geometry of the segmented kernels: segment, row in it, first lane,
+// and the segment as a lane mask (the lanes past the last segment, 32 mod
+// NV of them, own no system and form one group of their own).
+template <int NV>
+struct SegLane {
+  int lane, seg, r, base;
+  bool in_seg;
+  unsigned mask;
+  __device__ SegLane() {
+    constexpr int P = SegCfg<NV>::P;
+    lane = threadIdx.x & 31;
+    seg = lane / NV;
+    r = lane - seg * NV;
+    base = seg * NV;
+    in_seg = seg < P;
+    mask = in_seg ? (((1u << NV) - 1u) << base)
+                  : (P * NV >= 32 ? 0u : ~((1u << (P * NV)) - 1u));
+  }
+};
+
+// Queue step of the segmented kernels: every segment that needs a system
+// takes the next position of the order (one atomic per segment, read by
+// its lanes); returns the position, or nsys and beyond when the queue is
+// empty.  All lanes of the warp call it.
+template <int NV>
+__device__ __forceinline__ int seg_fetch(const SegLane<NV>& g, bool need,
+                                         int* __restrict__ counter) {
+  int q = 0;
+  if (need && g.r == 0) q = atomicAdd(counter, 1);
+  return __shfl_sync(0xffffffffu, q, g.in_seg ? g.base : 0);
+}
+
+// Segmented maximum of a 32-bit key: every lane gets the largest key of its
+// segment.  Up to four segments per warp, one full-warp redux.sync per
+// segment (the others contributing 0), independent of one another; more
+// segments, shuffle rounds with offsets 1, 2, 4, 8 inside the segment
+// (after them each lane holds the largest key of positions [r, r +
+// 2^rounds) mod NV).
+template <int NV>
+__device__ __forceinline__ unsigned seg_max(const SegLane<NV>& g,
+                                            unsigned key) {
+  using Cfg = SegCfg<NV>;
+  unsigned best = 0u;
+  if constexpr (Cfg::P <= 4) {
+#pragma unroll
+    for (int s = 0; s < Cfg::P; ++s) {
+      const unsigned m = __reduce_max_sync(0xffffffffu, g.seg == s ? key : 0u);
+      if (g.seg == s) best = m;
+    }
+  } else {
+    best = key;
+#pragma unroll
+    for (int o = 0, off = 1; o < Cfg::ROUNDS; ++o, off <<= 1) {
+      const int rr = g.r + off;
+      const int src = g.base + (rr >= NV ? rr - NV : rr);
+      best = max(best, __shfl_sync(0xffffffffu, best, src));
+    }
+  }
+  return best;
+}
+
+// L2 prefetch of the 8 nv bytes at p (both ends, which may sit in two
+// lines).
+template <int NV>
+__device__ __forceinline__ void prefetch_row(const double* p) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p + NV - 1));
+}
+
 template <int NV>
 __global__ void __launch_bounds__(kSegWarps * 32)
     k_block_thomas_seg(const double* __restrict__ Lm,
@@ -658,205 +743,217 @@ __global__ void __launch_bounds__(kSegWarps * 32)
                        double* __restrict__ work, int* __restrict__ counter,
                        int* __restrict__ status) {
   using Cfg = SegCfg<NV>;
-  constexpr int P = Cfg::P, RS = Cfg::RS, NC = 2 * NV + 1;
-  constexpr int64_t NN = (int64_t)NV * NV, WROW = NN + 2 * NV;
+  constexpr int RS = Cfg::RS, NC = 2 * NV + 1;
+  constexpr int64_t NN = (int64_t)NV * NV, WROW = NN + 2 * NV,
+                    SROW = (int64_t)NV * RS;
+  constexpr unsigned full = 0xffffffffu;
   __shared__ double s_st[kSegWarps][Cfg::SMEM];
-  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  const int seg = lane / NV, r = lane - seg * NV, base = seg * NV;
-  // lanes past the last segment (32 mod NV of them) own no system and no
-  // shared rows; they read segment 0's rows and never write them
-  double* st = s_st[wid] + (seg < P ? seg : 0) * NV * RS;
-  // this lane's segment as a lane mask (the lanes past the last segment
-  // form one group of their own)
-  const unsigned segmask =
-      seg < P ? (((1u << NV) - 1u) << base)
-              : (P * NV >= 32 ? 0u : ~((1u << (P * NV)) - 1u));
+  const SegLane<NV> g;
+  const int r = g.r, lane = g.lane;
+  // lanes past the last segment read segment 0's rows, never write them
+  double* st = s_st[threadIdx.x >> 5] + (g.in_seg ? g.seg : 0) * NV * RS;
+  // S_i | t_i of every row, after the factors (for the backward kernel)
+  double* __restrict__ sg = work + row_off[nsys] * WROW;
+  bool live = g.in_seg;  // the segment may still take systems
+  int N = 0, i = 0;      // rows of the segment's system, its next row
+  int64_t r0 = 0;
+  bool singular = false;
   for (;;) {
-    int q0 = 0;
-    if (lane == 0) q0 = atomicAdd(counter, P);
-    q0 = __shfl_sync(0xffffffffu, q0, 0);
-    if (q0 >= nsys) break;
-    const int q = q0 + seg;
-    const bool has = seg < P && q < nsys;
-    int64_t r0 = 0;
-    int N = 0;
-    if (has) {
-      const int s = order[q];
-      r0 = row_off[s];
-      const int64_t n64 = row_off[s + 1] - r0;
-      // an empty (or inverted) row range is skipped and flagged
-      N = n64 > 0 ? (int)n64 : 0;
-      if (n64 <= 0 && r == 0 && status) atomicOr(status, 2);
+    const bool need = live && i >= N;
+    const int q = seg_fetch(g, need, counter);
+    if (need) {
+      if (q >= nsys) {
+        live = false;
+      } else {
+        const int s = order[q];
+        r0 = row_off[s];
+        const int64_t n64 = row_off[s + 1] - r0;
+        // an empty (or inverted) row range is skipped and flagged
+        N = n64 > 0 ? (int)n64 : 0;
+        i = 0;
+        if (n64 <= 0 && r == 0 && status) atomicOr(status, 2);
+      }
     }
-    const int nmax = __reduce_max_sync(0xffffffffu, N);
-    bool singular = false;
-    double xlast = 0.0;
-    // ---- forward sweep
-    for (int i = 0; i < nmax; ++i) {
-      const bool act = i < N;
-      const int64_t row = r0 + i;
-      double a[NC], l[NV];
-      if (act) {
-        const double* __restrict__ Ci = Cm + row * NN + r * NV;
+    if (!__any_sync(full, live)) break;
+    const bool act = live && i < N;
+    const int64_t row = r0 + i;
+    double a[NC];
+    if (act) {
+      if (i + 1 < N) {
+        // the next row's blocks to L2 while this one is worked on
+        prefetch_row<NV>(Cm + (row + 1) * NN + r * NV);
+        prefetch_row<NV>(Lm + row * NN + r * NV);
+        if (i + 2 < N) prefetch_row<NV>(Um + (row + 1) * NN + r * NV);
+      }
+      const double* __restrict__ Ci = Cm + row * NN + r * NV;
 #pragma unroll
-        for (int j = 0; j < NV; ++j) a[j] = __ldg(Ci + j);
-        a[2 * NV] = __ldg(B + row * NV + r);
-        if (i + 1 < N) {
-          const double* __restrict__ Ui = Um + row * NN + r * NV;
+      for (int j = 0; j < NV; ++j) a[j] = __ldg(Ci + j);
+      a[2 * NV] = __ldg(B + row * NV + r);
+      if (i + 1 < N) {
+        const double* __restrict__ Ui = Um + row * NN + r * NV;
 #pragma unroll
-          for (int j = 0; j < NV; ++j) a[NV + j] = __ldg(Ui + j);
-        } else {
-#pragma unroll
-          for (int j = 0; j < NV; ++j) a[NV + j] = 0.0;
-        }
-        if (i > 0) {
-          const double* __restrict__ Li = Lm + (row - 1) * NN + r * NV;
-#pragma unroll
-          for (int k = 0; k < NV; ++k) l[k] = __ldg(Li + k);
-        }
+        for (int j = 0; j < NV; ++j) a[NV + j] = __ldg(Ui + j);
       } else {
 #pragma unroll
-        for (int j = 0; j < NC; ++j) a[j] = 0.0;
+        for (int j = 0; j < NV; ++j) a[NV + j] = 0.0;
       }
-      if (i > 0) {
-        // C' = C - L S_prev, b' = b - L t_prev (S | t in shared memory)
+    } else {
 #pragma unroll
-        for (int k = 0; k < NV; ++k) {
-          const double lk = act ? l[k] : 0.0;
+      for (int j = 0; j < NC; ++j) a[j] = 0.0;
+    }
+    if (act && i > 0) {
+      // C' = C - L S_prev, b' = b - L t_prev (S | t in shared memory)
+      const double* __restrict__ Li = Lm + (row - 1) * NN + r * NV;
+      double l[NV];
 #pragma unroll
-          for (int j = 0; j < NV; ++j)
-            a[j] = fma(-lk, st[k * RS + j], a[j]);
-          a[2 * NV] = fma(-lk, st[k * RS + NV], a[2 * NV]);
-        }
-      }
-      double* __restrict__ w = work + row * WROW;
-      if (act) w[NN + r] = a[2 * NV];  // b'_i, original row order
-      __syncwarp();
-      // elimination with relabelled partial pivoting
-      int pos = r, myk = 0, mypiv = 0;
-      bool elig = true;
-      double myinv = 0.0, lu[NV];
+      for (int k = 0; k < NV; ++k) l[k] = __ldg(Li + k);
 #pragma unroll
       for (int k = 0; k < NV; ++k) {
-        // segmented argmax of the 32-bit keys: after the rounds with
-        // offsets 1, 2, 4, 8 each lane holds the largest key of positions
-        // [r, r + 2^rounds) mod NV of its segment
-        unsigned best = elig ? pivot_key(a[k], pos) : 0u;
 #pragma unroll
-        for (int o = 0, off = 1; o < Cfg::ROUNDS; ++o, off <<= 1) {
-          const int rr = r + off;
-          const int src = base + (rr >= NV ? rr - NV : rr);
-          best = max(best, __shfl_sync(0xffffffffu, best, src));
-        }
-        const int bp = 15 - (int)(best & 15u);
-        const unsigned won = __ballot_sync(0xffffffffu, elig && pos == bp);
-        const int bl = __ffs(won & segmask) - 1;
-        if ((best >> 5) == 0 && act) singular = true;
-        if (r == k) mypiv = bp;
-        const bool is_piv = lane == bl;
-        const double pv = __shfl_sync(0xffffffffu, a[k], bl);
-        const double inv = pyro_rcp(pv);
-        const double m = is_piv ? 0.0 : a[k] * inv;
-        if (elig && !is_piv) lu[k] = m;  // getrf's multiplier
-        if (is_piv) {
-#pragma unroll
-          for (int j = k; j < NV; ++j) lu[j] = a[j];  // getrf's U row
-          myinv = inv;
-          myk = k;
-        }
-#pragma unroll
-        for (int j = k + 1; j < NC; ++j) {
-          const double pj = __shfl_sync(0xffffffffu, a[j], bl);
-          a[j] = fma(-m, pj, a[j]);
-        }
-        if (pos == k) pos = bp;
-        if (is_piv) {
-          pos = k;
-          elig = false;
-        }
+        for (int j = 0; j < NV; ++j) a[j] = fma(-l[k], st[k * RS + j], a[j]);
+        a[2 * NV] = fma(-l[k], st[k * RS + NV], a[2 * NV]);
       }
-      if (act) {
-        // factors in getrf's row order (position myk), pivots as swaps
-        double* __restrict__ wf = w + myk * NV;
+    }
+    double* __restrict__ w = work + row * WROW;
+    if (act) w[NN + r] = a[2 * NV];  // b'_i, original row order
+    __syncwarp();
+    // elimination with relabelled partial pivoting; the next step's pivot
+    // key and reciprocal are formed as soon as its column is updated (every
+    // lane takes the reciprocal of its own candidate, the pivot lane's is
+    // shuffled out), so the argmax and the reciprocal overlap the rest of
+    // the step's updates instead of following them
+    int pos = r, myk = 0, mypiv = 0;
+    bool elig = true;
+    double myinv = 0.0, lu[NV];
+    unsigned key = pivot_key(a[0], r);
+    double rc = pyro_rcp3(a[0]);
 #pragma unroll
-        for (int j = 0; j < NV; ++j) wf[j] = lu[j];
-        w[NN + NV + r] = (double)mypiv;
+    for (int k = 0; k < NV; ++k) {
+      const unsigned best = seg_max(g, key);
+      const int bp = 15 - (int)(best & 15u);
+      const unsigned won = __ballot_sync(full, elig && pos == bp);
+      const int bl = __ffs(won & g.mask) - 1;
+      if ((best >> 5) == 0 && act) singular = true;
+      if (r == k) mypiv = bp;
+      const bool is_piv = lane == bl;
+      const double inv = __shfl_sync(full, rc, bl);
+      const double m = is_piv ? 0.0 : a[k] * inv;
+      if (elig && !is_piv) lu[k] = m;  // getrf's multiplier
+      if (is_piv) {
+#pragma unroll
+        for (int j = k; j < NV; ++j) lu[j] = a[j];  // getrf's U row
+        myinv = inv;
+        myk = k;
       }
-      // row myk of S_i | t_i, for the next row's update (and x_{N-1})
+      if (pos == k) pos = bp;
+      if (is_piv) {
+        pos = k;
+        elig = false;
+      }
+      if (k + 1 < NV) {
+        const double p1 = __shfl_sync(full, a[k + 1], bl);
+        a[k + 1] = fma(-m, p1, a[k + 1]);
+        key = elig ? pivot_key(a[k + 1], pos) : 0u;
+        rc = pyro_rcp3(a[k + 1]);
+      }
+#pragma unroll
+      for (int j = (k + 1 < NV ? k + 2 : k + 1); j < NC; ++j) {
+        const double pj = __shfl_sync(full, a[j], bl);
+        a[j] = fma(-m, pj, a[j]);
+      }
+    }
+    if (act) {
+      // factors in getrf's row order (position myk), pivots as swaps
+      double* __restrict__ wf = w + myk * NV;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) wf[j] = lu[j];
+      w[NN + NV + r] = (double)mypiv;
+      // row myk of S_i | t_i: for the next row's update (shared memory) and
+      // the backward sweep (workspace); t_{N-1} = x_{N-1}
+      double* __restrict__ sgr = sg + row * SROW + myk * RS;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) {
+        const double sj = a[NV + j] * myinv;
+        st[myk * RS + j] = sj;
+        sgr[j] = sj;
+      }
       const double tk = a[2 * NV] * myinv;
-      if (seg < P) {
-#pragma unroll
-        for (int j = 0; j < NV; ++j) st[myk * RS + j] = a[NV + j] * myinv;
-        st[myk * RS + NV] = tk;
+      st[myk * RS + NV] = tk;
+      sgr[NV] = tk;
+      if (i == N - 1) {
+        X[row * NV + myk] = tk;
+        if (singular && r == 0 && status) atomicOr(status, 1);
+        singular = false;
       }
-      if (act && i == N - 1) X[row * NV + myk] = tk;
-      __syncwarp();
-      if (i == N - 1) xlast = st[r * RS + NV];  // x_{N-1}, variable order
+      ++i;
     }
-    // ---- backward sweep: x_i = C'_i^-1 (b'_i - U_i x_{i+1})
-    double x = xlast;
-    for (int i = nmax - 2; i >= 0; --i) {
-      const bool act = i <= N - 2;
-      const int64_t row = r0 + i;
-      const double* __restrict__ w = work + row * WROW;
-      double f[NV], v = 0.0, d = 1.0;
-      int perm_src = r;
-      if (act) {
-        v = w[NN + r];
-#pragma unroll
-        for (int j = 0; j < NV; ++j) f[j] = w[r * NV + j];
-        d = f[0];
-#pragma unroll
-        for (int j = 1; j < NV; ++j)
-          if (j == r) d = f[j];
-        // original row held at position r after getrf's swaps
-        int j = r;
-#pragma unroll
-        for (int k = NV - 1; k >= 0; --k) {
-          const int pk = (int)w[NN + NV + k];
-          if (j == k)
-            j = pk;
-          else if (j == pk)
-            j = k;
-        }
-        perm_src = j;
+    __syncwarp();
+  }
+}
+
+// Backward sweep of the segmented solve: x_i = t_i - S_i x_{i+1} with
+// S_i = C'_i^-1 U_i and t_i = C'_i^-1 b'_i from the forward kernel (the
+// same recurrence as x_i = C'_i^-1 (b'_i - U_i x_{i+1}), one matrix-vector
+// product per row instead of two triangular solves) and x_{N-1} in x;
+// segments take systems from the queue as in the forward sweep.
+template <int NV>
+__global__ void __launch_bounds__(kSegWarps * 32)
+    k_block_thomas_seg_back(double* __restrict__ X,
+                            const int64_t* __restrict__ row_off,
+                            const int* __restrict__ order, int nsys,
+                            const double* __restrict__ work,
+                            int* __restrict__ counter) {
+  constexpr int RS = SegCfg<NV>::RS;
+  constexpr int64_t WROW = (int64_t)NV * NV + 2 * NV, SROW = (int64_t)NV * RS;
+  constexpr unsigned full = 0xffffffffu;
+  const SegLane<NV> g;
+  const int r = g.r, base = g.base;
+  const double* __restrict__ sg = work + row_off[nsys] * WROW;
+  bool live = g.in_seg;
+  int i = -1;  // next row to solve, counting down; < 0: none
+  int64_t r0 = 0;
+  double x = 0.0;  // this lane's entry of x_{i+1}
+  for (;;) {
+    const bool need = live && i < 0;
+    const int q = seg_fetch(g, need, counter);
+    if (need) {
+      if (q >= nsys) {
+        live = false;
       } else {
-#pragma unroll
-        for (int j = 0; j < NV; ++j) f[j] = 0.0;
-      }
-      // v_r = b'_r - (U_i x_{i+1})_r in original order; every lane takes
-      // part in the shuffles
-      {
-        const double* __restrict__ Ui = Um + (act ? row : 0) * NN + r * NV;
-#pragma unroll
-        for (int k = 0; k < NV; ++k) {
-          const double xk = __shfl_sync(0xffffffffu, x, base + k);
-          if (act) v = fma(-__ldg(Ui + k), xk, v);
+        const int s = order[q];
+        r0 = row_off[s];
+        const int64_t n64 = row_off[s + 1] - r0;
+        // one-row and empty systems have no backward rows
+        if (n64 >= 2) {
+          i = (int)n64 - 2;
+          x = X[(r0 + n64 - 1) * NV + r];
         }
       }
-      double y = __shfl_sync(0xffffffffu, v, base + perm_src);
-      // unit lower: y_r -= L[r][k] y_k, k < r
-#pragma unroll
-      for (int k = 0; k < NV - 1; ++k) {
-        const double yk = __shfl_sync(0xffffffffu, y, base + k);
-        if (r > k) y = fma(-f[k], yk, y);
-      }
-      // upper: x_r = (y_r - sum_{k > r} U[r][k] x_k) / U[r][r]
-      const double inv = pyro_rcp(d);
-#pragma unroll
-      for (int k = NV - 1; k >= 0; --k) {
-        if (r == k) y *= inv;
-        const double xk = __shfl_sync(0xffffffffu, y, base + k);
-        if (r < k) y = fma(-f[k], xk, y);
-      }
-      // a segment whose system is shorter than the warp's longest idles
-      // through the first rows of this loop and keeps x_{N-1} meanwhile
-      if (act) {
-        x = y;
-        X[row * NV + r] = x;
-      }
     }
-    if (singular && status) atomicOr(status, 1);
+    if (!__any_sync(full, live)) break;
+    const bool act = live && i >= 0;
+    const int64_t row = r0 + (act ? i : 0);
+    double v = 0.0, srow[NV];
+    if (act) {
+      const double* __restrict__ p = sg + row * SROW + r * RS;
+      if (i > 0) prefetch_row<RS>(p - SROW);
+#pragma unroll
+      for (int j = 0; j < NV; ++j) srow[j] = p[j];
+      v = p[NV];
+    } else {
+#pragma unroll
+      for (int j = 0; j < NV; ++j) srow[j] = 0.0;
+    }
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double xk = __shfl_sync(full, x, base + k);
+      v = fma(-srow[k], xk, v);
+    }
+    if (act) {
+      x = v;
+      X[row * NV + r] = v;
+      --i;
+    }
   }
 }
 
@@ -865,26 +962,36 @@ int launch_seg(const double* L, const double* C, const double* U,
                const double* b, double* x, const int64_t* row_off,
                const int* order, int nsys, double* work, int* counter,
                int* status, int ctas, cudaStream_t stream) {
-  if (ctas <= 0) {
-    int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-            &per_sm, k_block_thomas_seg<NV>, kSegWarps * 32, 0) !=
-            cudaSuccess ||
-        per_sm < 1) {
-      (void)cudaGetLastError();
-      per_sm = 1;
-    }
-    ctas = per_sm * pyro_sm_count();
-  }
   const int per_cta = kSegWarps * SegCfg<NV>::P;
   const int need = (nsys + per_cta - 1) / per_cta;
+  // default grid: one warp per SM partition
+  if (ctas <= 0) ctas = pyro_sm_count() * 4 / kSegWarps;
   if (ctas > need) ctas = need;
+  // the backward sweep has few FP64 instructions per row and waits on its
+  // loads and shuffles: as many warps as fit
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+          &per_sm, k_block_thomas_seg_back<NV>, kSegWarps * 32, 0) !=
+          cudaSuccess ||
+      per_sm < 1) {
+    (void)cudaGetLastError();
+    per_sm = 1;
+  }
+  int back = per_sm * pyro_sm_count();
+  if (back > need) back = need;
   if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
     (void)cudaGetLastError();
     return PYRO_ERR_LAUNCH;
   }
   k_block_thomas_seg<NV><<<ctas, kSegWarps * 32, 0, stream>>>(
       L, C, U, b, x, row_off, order, nsys, work, counter, status);
+  PYRO_CHECK_LAUNCH();
+  if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  k_block_thomas_seg_back<NV><<<back, kSegWarps * 32, 0, stream>>>(
+      x, row_off, order, nsys, work, counter);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }
@@ -893,8 +1000,9 @@ int launch_seg(const double* L, const double* C, const double* U,
 
 // pyro_block_thomas for blocks of size nv <= 16 with 32 / nv systems per
 // warp, one lane per block row (see above).  Same arguments and workspace
-// layout as pyro_block_thomas; the CTA size is fixed (one warp); ctas:
-// grid size (0 = all resident).
+// layout as pyro_block_thomas; two launches (forward, backward); the CTA
+// size is fixed (four warps); ctas: forward grid size (0 = one warp per SM
+// partition).
 PYRO_EXPORT int pyro_block_thomas_seg(const double* L, const double* C,
                                       const double* U, const double* b,
                                       double* x, const int64_t* row_off,

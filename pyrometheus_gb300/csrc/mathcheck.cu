@@ -63,26 +63,25 @@ PYRO_EXPORT int pyro_log_check(const double* x, double* mine, double* ref,
 namespace {
 
 __global__ void k_rcpcheck(const double* __restrict__ x, double* mine,
-                           double* ref, int64_t n) {
+                           double* ref, int third, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * blockDim.x) {
     const double v = x[i];
-    mine[i] = pyro_rcp(v);
+    mine[i] = third ? pyro_rcp3(v) : pyro_rcp(v);
     ref[i] = 1.0 / v;
   }
 }
 
 }  // namespace
 
-// mine[i] = pyro_rcp(x[i]), ref[i] = CUDA's 1.0 / x[i].  Device pointers;
-// asynchronous on stream.
+// mine[i] = pyro_rcp(x[i]) (third = 0) or pyro_rcp3(x[i]) (third = 1),
+// ref[i] = CUDA's 1.0 / x[i].  Device pointers; asynchronous on stream.
 PYRO_EXPORT int pyro_rcp_check(const double* x, double* mine, double* ref,
-                               int unused, int64_t n, cudaStream_t stream) {
-  (void)unused;
+                               int third, int64_t n, cudaStream_t stream) {
   if (n < 0 || (n > 0 && (!x || !mine || !ref))) return PYRO_ERR_ARGUMENT;
   if (n == 0) return PYRO_OK;
   k_rcpcheck<<<pyro_grid(n, 256, pyro_sm_count() * 4), 256, 0, stream>>>(
-      x, mine, ref, n);
+      x, mine, ref, third, n);
   PYRO_CHECK_LAUNCH();
   return PYRO_OK;
 }

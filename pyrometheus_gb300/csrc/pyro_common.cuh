@@ -74,3 +74,16 @@ __device__ __forceinline__ double pyro_rcp(double x) {
   e = fma(-x, r, 1.0);
   return fma(r, e, r);
 }
+
+// 1/x with one third-order step instead of two Newton-Raphson steps: with
+// the seed r = (1 - e) / x, 1/x = r (1 + e + e^2 + ...), so
+// r (1 + (e + e^2)) leaves a relative error of order e^3 -- below double
+// rounding for seeds good to 2^-18 -- in three FMAs instead of four (the
+// same series Markstein's paper truncates after e).  Same special cases as
+// pyro_rcp; checked against the IEEE division like it.
+__device__ __forceinline__ double pyro_rcp3(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  const double e = fma(-x, r, 1.0);
+  return fma(r, fma(e, e, e), r);
+}

@@ -47,7 +47,9 @@ def test_block_thomas_library_exports_header_symbols():
     for name in declared("pyro_block_thomas.h"):
         assert hasattr(so, name), name
     so.pyro_block_thomas_work_doubles.restype = ctypes.c_int64
-    assert so.pyro_block_thomas_work_doubles(10, 7) == 7 * (100 + 20)
+    # factors, b' and pivots per row; for nv <= 16 also S | t per row
+    assert so.pyro_block_thomas_work_doubles(10, 7) == 7 * (100 + 20 + 110)
+    assert so.pyro_block_thomas_work_doubles(54, 7) == 7 * (54 * 54 + 108)
 
 
 @pytest.mark.parametrize("header,builder", [

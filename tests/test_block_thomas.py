@@ -26,8 +26,12 @@ def _rel(x, ref):
 
 @pytest.mark.parametrize("tag", TAGS)
 def test_oracle_matches_reference_block_thomas(tag):
+    """The oracle's solve against the reference's on its golden systems, to
+    cond(A)·eps (cond up to 3e4): the two solve the diagonal blocks through
+    the platform's LAPACK, whose rounding differs between machines (1e-13
+    at nv = 54 on an Arm build, below 1e-14 on x86)."""
     lengths, L, C, U, b, x = _golden(tag)
-    assert _rel(solve_packed(lengths, L, C, U, b), x) < 1e-14
+    assert _rel(solve_packed(lengths, L, C, U, b), x) < 1e-12
 
 
 def test_oracle_against_dense_solve():
@@ -118,6 +122,34 @@ def test_cuda_block_thomas_uneven_batch(nv, kernel):
         be_ref = _residual(L[sl], C[sl], U[sl], b[sl], ref[sl])
         assert be_got <= 16.0 * max(be_ref, nv * 1.1e-16)
         r0 += n
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nv", [3, 10, 16])
+@pytest.mark.parametrize("ctas", [1, 3])
+def test_seg_segments_take_systems_in_turn(nv, ctas):
+    """The segmented kernel with a grid far smaller than the batch: one or
+    three CTAs of four warps, so every lane segment solves tens of systems
+    of uneven lengths one after another (forward sweeps, then backward
+    sweeps, each segment taking the next system of the order when its own
+    is done), lengths 1 to 90 (one-row systems included); in a CUDA graph,
+    replayed with new right-hand sides."""
+    _cuda()
+    from pyrometheus_gb300.flamelet import BlockThomasSolver
+    lengths, L, C, U, b = make_systems(300, nv, 1, 90, seed=40 + nv)
+    assert (lengths == 1).any()
+    ref = solve_packed(lengths, L, C, U, b)
+    dev = torch.device("cuda")
+    t = [torch.as_tensor(a, device=dev).contiguous() for a in (L, C, U, b)]
+    solver = BlockThomasSolver(nv, lengths, kernel="seg", ctas=ctas,
+                               use_graph=True)
+    got = solver.solve(*t).cpu().numpy()
+    solver.check_status()
+    assert _rel(got, ref) < 1e-10
+    b2 = np.random.default_rng(nv).standard_normal(b.shape)
+    t[3].copy_(torch.as_tensor(b2))
+    got2 = solver.solve(*t).cpu().numpy()
+    assert _rel(got2, solve_packed(lengths, L, C, U, b2)) < 1e-10
 
 
 @pytest.mark.gpu

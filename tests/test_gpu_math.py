@@ -82,10 +82,12 @@ def test_log_against_cuda():
         assert np.all(same[~finite])
 
 
-def test_rcp_against_cuda_division():
+@pytest.mark.parametrize("third", [0, 1], ids=["newton2", "cubic"])
+def test_rcp_against_cuda_division(third):
     """Within an ulp of CUDA's correctly rounded 1.0 / x over the normal
     range whose reciprocals are normal, and equal to it on most
-    arguments."""
+    arguments: two Newton-Raphson steps (pyro_rcp) and one third-order
+    step (pyro_rcp3)."""
     rng = np.random.default_rng(3)
     mag = 10.0 ** rng.uniform(-300.0, 300.0, 2_000_000)
     x = np.concatenate([
@@ -94,7 +96,7 @@ def test_rcp_against_cuda_division():
         1.0 + np.arange(-300, 300) / 2 ** 40,
         [1.0, -1.0, 2.0, 0.5, 3.0, 10.0, np.nextafter(1.0, 0.0),
          np.nextafter(1.0, 2.0)]])
-    mine, ref = _run(x, 0, "pyro_rcp_check")
+    mine, ref = _run(x, third, "pyro_rcp_check")
     rel = np.abs(mine - ref) / np.abs(ref)
     assert rel.max() <= 2.3e-16, rel.max()
     assert np.mean(mine == ref) > 0.9
