@@ -64,24 +64,28 @@ int pyro_block_thomas_small(const double* L, const double* C, const double* U,
 /* pyro_block_thomas for blocks of size nv <= 16 with 32 / nv systems per
  * warp (three at nv = 10), one lane per block row and the working rows in
  * registers: every lane of every FP64 instruction works, and nothing
- * synchronises beyond a warp.  A persistent grid whose lane segments each
- * take the next system of `order` when theirs is done; two launches (the
- * forward sweep, then x_i = t_i - S_i x_{i+1} backward), the counter
- * cleared before each.  Pivoting and the kept factors are getrf's, in the
- * workspace layout of pyro_block_thomas (so pyro_block_thomas_resolve
- * applies).  Same arguments as pyro_block_thomas without the CTA size
- * (four warps per CTA); ctas: forward grid size (0 = one warp per SM
- * partition).  Replaces the same reference function,
- * pyrometheus/flamelets/linear_solver.py:6-103. */
+ * synchronises beyond a warp.  Two-ended: each system is eliminated from
+ * its first row down and from its last row up to its middle row m = N / 2
+ * (two independent sweeps), the middle row is solved, and x follows
+ * outwards, x_i = t_i - S_i x_{i+-1}.  A persistent grid whose lane
+ * segments each take the next sweep of `order` when theirs is done; three
+ * launches (sweeps, middle rows, sweeps back), the counter cleared before
+ * each.  Pivoting is getrf's; the factors (of C'_i above the middle row,
+ * of the upward sweep's modified blocks below it, of the middle row's
+ * matrix at m) stay in the workspace for pyro_block_thomas_seg_resolve.
+ * Same arguments as pyro_block_thomas without the CTA size (four warps
+ * per CTA); ctas: forward grid size (0 = one or two warps per SM
+ * partition by the batch size).  Replaces the same reference function,
+ * pyrometheus/flamelets/linear_solver.py:6-103 (the same solution; the
+ * reference sweeps top-down only). */
 int pyro_block_thomas_seg(const double* L, const double* C, const double* U,
                           const double* b, double* x, const int64_t* row_off,
                           const int* order, int nsys, int nv, double* work,
                           int* counter, int* status, int ctas,
                           cudaStream_t stream);
 
-/* More right-hand sides for systems already solved: after pyro_block_thomas,
- * pyro_block_thomas_small or pyro_block_thomas_seg, `work` holds every row's
- * LU factors and
+/* More right-hand sides for systems already solved: after pyro_block_thomas
+ * or pyro_block_thomas_small, `work` holds every row's LU factors and
  * pivots of C'_i; for the same L, C, U this solves nrhs (1..4) further
  * systems, B[c][rows][nv] -> X[c][rows][nv] (the c-th at offset
  * c * rhs_stride), with the vector recurrences only (4 nv^2 FMAs per row
@@ -97,6 +101,16 @@ int pyro_block_thomas_resolve(const double* L, const double* U,
                               const int* order, int nsys, int nv,
                               const double* work, int* counter, int* status,
                               cudaStream_t stream);
+
+/* pyro_block_thomas_resolve after pyro_block_thomas_seg: the same
+ * arguments (nv <= 16), the vector recurrences of the two-ended sweeps
+ * with its kept factors and S | t blocks. */
+int pyro_block_thomas_seg_resolve(const double* L, const double* U,
+                                  const double* B, double* X, int nrhs,
+                                  int64_t rhs_stride, const int64_t* row_off,
+                                  const int* order, int nsys, int nv,
+                                  const double* work, int* counter,
+                                  int* status, cudaStream_t stream);
 
 /* No counterpart in the reference (its block_thomas allocates through JAX
  * on every call).  For callers that cannot allocate device memory when they

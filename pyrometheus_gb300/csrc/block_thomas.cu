@@ -644,8 +644,6 @@ struct SegCfg {
   static constexpr int P = 32 / NV;         // systems per warp
   static constexpr int RS = NV + 1;         // shared row stride (S | t)
   static constexpr int SMEM = P * NV * RS;  // doubles per warp
-  static constexpr int ROUNDS = NV <= 1 ? 0 : NV <= 2 ? 1 : NV <= 4 ? 2
-                                : NV <= 8 ? 3 : 4;
 };
 
 // Pivot key of an eligible row: the top 27 bits of |v|'s bit pattern
@@ -713,9 +711,10 @@ __device__ __forceinline__ unsigned seg_max(const SegLane<NV>& g,
       if (g.seg == s) best = m;
     }
   } else {
+    constexpr int rounds = NV <= 1 ? 0 : NV <= 2 ? 1 : NV <= 4 ? 2 : 3;
     best = key;
 #pragma unroll
-    for (int o = 0, off = 1; o < Cfg::ROUNDS; ++o, off <<= 1) {
+    for (int o = 0, off = 1; o < rounds; ++o, off <<= 1) {
       const int rr = g.r + off;
       const int src = g.base + (rr >= NV ? rr - NV : rr);
       best = max(best, __shfl_sync(0xffffffffu, best, src));
@@ -724,20 +723,101 @@ __device__ __forceinline__ unsigned seg_max(const SegLane<NV>& g,
   return best;
 }
 
-// L2 prefetch of the 8 nv bytes at p (both ends, which may sit in two
+// L2 prefetch of the 8 n bytes at p (both ends, which may sit in two
 // lines).
-template <int NV>
+template <int N>
 __device__ __forceinline__ void prefetch_row(const double* p) {
   asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
-  asm volatile("prefetch.global.L2 [%0];" ::"l"(p + NV - 1));
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(p + N - 1));
 }
 
+// Elimination of one block row held by a segment, lane r holding row r of
+// [A | R] in a[0..NV) | a[NV..NC): Gauss-Jordan with relabelled partial
+// pivoting, software-pipelined -- as soon as step k has updated column
+// k + 1, the pivot of step k + 1 is searched (key maximum over the segment,
+// ballot) and every lane takes the reciprocal of its own candidate (the
+// pivot lane's is shuffled out), all under step k's remaining updates.  On
+// entry `best` is the segment maximum of column 0's keys and `rc` this
+// lane's pyro_rcp3(a[0]).  On return lu holds this lane's row of getrf's
+// factors (its position in getrf's row order is myk), mypiv getrf's pivot
+// of step r, and a[NV..NC) * myinv is row myk of A^-1 R; singular is set on
+// a zero pivot of an active segment.
+template <int NV, int NC>
+__device__ __forceinline__ void seg_eliminate(const SegLane<NV>& g, bool act,
+                                              double (&a)[NC], unsigned best,
+                                              double rc, double (&lu)[NV],
+                                              int& myk, int& mypiv,
+                                              double& myinv, bool& singular) {
+  constexpr unsigned full = 0xffffffffu;
+  const int r = g.r, lane = g.lane;
+  int pos = r;
+  bool elig = true;
+  myk = 0;
+  mypiv = 0;
+  myinv = 0.0;
+  int bp = 15 - (int)(best & 15u);
+  int bl = __ffs(__ballot_sync(full, pos == bp) & g.mask) - 1;
+#pragma unroll
+  for (int k = 0; k < NV; ++k) {
+    if ((best >> 5) == 0 && act) singular = true;
+    if (r == k) mypiv = bp;
+    const bool is_piv = lane == bl;
+    const double inv = __shfl_sync(full, rc, bl);
+    const double m = is_piv ? 0.0 : a[k] * inv;
+    if (elig && !is_piv) lu[k] = m;  // getrf's multiplier
+    if (is_piv) {
+#pragma unroll
+      for (int j = k; j < NV; ++j) lu[j] = a[j];  // getrf's U row
+      myinv = inv;
+      myk = k;
+    }
+    if (pos == k) pos = bp;
+    if (is_piv) {
+      pos = k;
+      elig = false;
+    }
+    int nbl = bl;
+    if (k + 1 < NV) {
+      const double p1 = __shfl_sync(full, a[k + 1], bl);
+      a[k + 1] = fma(-m, p1, a[k + 1]);
+      best = seg_max(g, elig ? pivot_key(a[k + 1], pos) : 0u);
+      rc = pyro_rcp3(a[k + 1]);
+      bp = 15 - (int)(best & 15u);
+      nbl = __ffs(__ballot_sync(full, elig && pos == bp) & g.mask) - 1;
+    }
+#pragma unroll
+    for (int j = (k + 1 < NV ? k + 2 : k + 1); j < NC; ++j) {
+      const double pj = __shfl_sync(full, a[j], bl);
+      a[j] = fma(-m, pj, a[j]);
+    }
+    bl = nbl;
+  }
+}
+
+// Rows and split of a system of the two-ended sweeps: N rows, the middle
+// row m = N / 2; unit 0 eliminates rows 0 .. m-1 downwards, unit 1 rows
+// N-1 .. m+1 upwards.
+__device__ __forceinline__ int seg_unit_rows(int N, int dir) {
+  const int m = N >> 1;
+  const int c = dir == 0 ? m : N - 1 - m;
+  return c > 0 ? c : 0;
+}
+
+// Forward sweeps: every segment takes units (system, direction) from the
+// queue -- position q is direction q & 1 of system order[q >> 1] -- and
+// eliminates the unit's rows in order.  Step t of a downward unit is row
+// i = t: C'_i | b'_i = (C_i | b_i) - L_{i-1} (S_{i-1} | t_{i-1}), then the
+// elimination over [C'_i | U_i | b'_i]; of an upward unit row i = N-1-t:
+// C^_i | b^_i = (C_i | b_i) - U_i (S^_{i+1} | t^_{i+1}), then the
+// elimination over [C^_i | L_{i-1} | b^_i].  The factors go to row i of the
+// workspace, S_i | t_i (or S^_i | t^_i) to the S | t region and, for the
+// unit's next row, to the warp's shared memory.
 template <int NV>
 __global__ void __launch_bounds__(kSegWarps * 32)
     k_block_thomas_seg(const double* __restrict__ Lm,
                        const double* __restrict__ Cm,
                        const double* __restrict__ Um,
-                       const double* __restrict__ B, double* __restrict__ X,
+                       const double* __restrict__ B,
                        const int64_t* __restrict__ row_off,
                        const int* __restrict__ order, int nsys,
                        double* __restrict__ work, int* __restrict__ counter,
@@ -749,153 +829,221 @@ __global__ void __launch_bounds__(kSegWarps * 32)
   constexpr unsigned full = 0xffffffffu;
   __shared__ double s_st[kSegWarps][Cfg::SMEM];
   const SegLane<NV> g;
-  const int r = g.r, lane = g.lane;
+  const int r = g.r;
   // lanes past the last segment read segment 0's rows, never write them
   double* st = s_st[threadIdx.x >> 5] + (g.in_seg ? g.seg : 0) * NV * RS;
-  // S_i | t_i of every row, after the factors (for the backward kernel)
+  // the previous row's S | t is kept finite between units (zero before the
+  // first and after every last row), so the update runs branch-free with
+  // zero couplings on a unit's first row
+  for (int e = g.lane; e < Cfg::SMEM; e += 32)
+    s_st[threadIdx.x >> 5][e] = 0.0;
+  __syncwarp();
   double* __restrict__ sg = work + row_off[nsys] * WROW;
-  bool live = g.in_seg;  // the segment may still take systems
-  int N = 0, i = 0;      // rows of the segment's system, its next row
+  bool live = g.in_seg;  // the segment may still take units
+  int N = 0, dir = 0, cnt = 0, t = 0;
   int64_t r0 = 0;
   bool singular = false;
   for (;;) {
-    const bool need = live && i >= N;
+    const bool need = live && t >= cnt;
     const int q = seg_fetch(g, need, counter);
     if (need) {
-      if (q >= nsys) {
+      if (q >= 2 * nsys) {
         live = false;
       } else {
-        const int s = order[q];
+        const int s = order[q >> 1];
+        dir = q & 1;
         r0 = row_off[s];
         const int64_t n64 = row_off[s + 1] - r0;
         // an empty (or inverted) row range is skipped and flagged
         N = n64 > 0 ? (int)n64 : 0;
-        i = 0;
-        if (n64 <= 0 && r == 0 && status) atomicOr(status, 2);
+        cnt = seg_unit_rows(N, dir);
+        t = 0;
+        if (n64 <= 0 && dir == 0 && r == 0 && status) atomicOr(status, 2);
       }
     }
     if (!__any_sync(full, live)) break;
-    const bool act = live && i < N;
+    const bool act = live && t < cnt;
+    const bool down = dir == 0;
+    const int i = down ? t : N - 1 - t;
     const int64_t row = r0 + i;
-    double a[NC];
+    // coupling to the row eliminated before (L_{i-1} down, U_i up) and the
+    // right-hand-side block (U_i down, L_{i-1} up)
+    const double* __restrict__ Pm = down ? Lm : Um;
+    const double* __restrict__ Qm = down ? Um : Lm;
+    const int64_t prow = down ? row - 1 : row, qrow = down ? row : row - 1;
+    double a[NC], l[NV];
     if (act) {
-      if (i + 1 < N) {
+      if (t + 1 < cnt) {
         // the next row's blocks to L2 while this one is worked on
-        prefetch_row<NV>(Cm + (row + 1) * NN + r * NV);
-        prefetch_row<NV>(Lm + row * NN + r * NV);
-        if (i + 2 < N) prefetch_row<NV>(Um + (row + 1) * NN + r * NV);
+        const int64_t step = down ? 1 : -1;
+        prefetch_row<NV>(Cm + (row + step) * NN + r * NV);
+        prefetch_row<NV>(Pm + (prow + step) * NN + r * NV);
+        prefetch_row<NV>(Qm + (qrow + step) * NN + r * NV);
       }
       const double* __restrict__ Ci = Cm + row * NN + r * NV;
+      const double* __restrict__ Qi = Qm + qrow * NN + r * NV;
 #pragma unroll
-      for (int j = 0; j < NV; ++j) a[j] = __ldg(Ci + j);
-      a[2 * NV] = __ldg(B + row * NV + r);
-      if (i + 1 < N) {
-        const double* __restrict__ Ui = Um + row * NN + r * NV;
-#pragma unroll
-        for (int j = 0; j < NV; ++j) a[NV + j] = __ldg(Ui + j);
-      } else {
-#pragma unroll
-        for (int j = 0; j < NV; ++j) a[NV + j] = 0.0;
+      for (int j = 0; j < NV; ++j) {
+        a[j] = __ldg(Ci + j);
+        a[NV + j] = __ldg(Qi + j);
       }
+      a[2 * NV] = __ldg(B + row * NV + r);
+      // (a unit's first row has no coupling; its address stays in bounds)
+      const double* __restrict__ Pi = Pm + (t > 0 ? prow : row) * NN + r * NV;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) l[k] = t > 0 ? __ldg(Pi + k) : 0.0;
     } else {
 #pragma unroll
       for (int j = 0; j < NC; ++j) a[j] = 0.0;
+#pragma unroll
+      for (int k = 0; k < NV; ++k) l[k] = 0.0;
     }
-    if (act && i > 0) {
-      // C' = C - L S_prev, b' = b - L t_prev (S | t in shared memory)
-      const double* __restrict__ Li = Lm + (row - 1) * NN + r * NV;
-      double l[NV];
+    // C' = C - P S_prev, b' = b - P t_prev (S | t in shared memory), column
+    // 0 first so that its pivot search starts under the other columns'
+    // updates
 #pragma unroll
-      for (int k = 0; k < NV; ++k) l[k] = __ldg(Li + k);
+    for (int k = 0; k < NV; ++k) a[0] = fma(-l[k], st[k * RS], a[0]);
+    const unsigned best = seg_max(g, pivot_key(a[0], r));
+    const double rc = pyro_rcp3(a[0]);
 #pragma unroll
-      for (int k = 0; k < NV; ++k) {
+    for (int j = 1; j < NV; ++j) {
 #pragma unroll
-        for (int j = 0; j < NV; ++j) a[j] = fma(-l[k], st[k * RS + j], a[j]);
-        a[2 * NV] = fma(-l[k], st[k * RS + NV], a[2 * NV]);
-      }
+      for (int k = 0; k < NV; ++k) a[j] = fma(-l[k], st[k * RS + j], a[j]);
     }
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+      a[2 * NV] = fma(-l[k], st[k * RS + NV], a[2 * NV]);
     double* __restrict__ w = work + row * WROW;
     if (act) w[NN + r] = a[2 * NV];  // b'_i, original row order
     __syncwarp();
-    // elimination with relabelled partial pivoting; the next step's pivot
-    // key and reciprocal are formed as soon as its column is updated (every
-    // lane takes the reciprocal of its own candidate, the pivot lane's is
-    // shuffled out), so the argmax and the reciprocal overlap the rest of
-    // the step's updates instead of following them
-    int pos = r, myk = 0, mypiv = 0;
-    bool elig = true;
-    double myinv = 0.0, lu[NV];
-    unsigned key = pivot_key(a[0], r);
-    double rc = pyro_rcp3(a[0]);
-#pragma unroll
-    for (int k = 0; k < NV; ++k) {
-      const unsigned best = seg_max(g, key);
-      const int bp = 15 - (int)(best & 15u);
-      const unsigned won = __ballot_sync(full, elig && pos == bp);
-      const int bl = __ffs(won & g.mask) - 1;
-      if ((best >> 5) == 0 && act) singular = true;
-      if (r == k) mypiv = bp;
-      const bool is_piv = lane == bl;
-      const double inv = __shfl_sync(full, rc, bl);
-      const double m = is_piv ? 0.0 : a[k] * inv;
-      if (elig && !is_piv) lu[k] = m;  // getrf's multiplier
-      if (is_piv) {
-#pragma unroll
-        for (int j = k; j < NV; ++j) lu[j] = a[j];  // getrf's U row
-        myinv = inv;
-        myk = k;
-      }
-      if (pos == k) pos = bp;
-      if (is_piv) {
-        pos = k;
-        elig = false;
-      }
-      if (k + 1 < NV) {
-        const double p1 = __shfl_sync(full, a[k + 1], bl);
-        a[k + 1] = fma(-m, p1, a[k + 1]);
-        key = elig ? pivot_key(a[k + 1], pos) : 0u;
-        rc = pyro_rcp3(a[k + 1]);
-      }
-#pragma unroll
-      for (int j = (k + 1 < NV ? k + 2 : k + 1); j < NC; ++j) {
-        const double pj = __shfl_sync(full, a[j], bl);
-        a[j] = fma(-m, pj, a[j]);
-      }
-    }
+    int myk, mypiv;
+    double myinv, lu[NV];
+    seg_eliminate<NV, NC>(g, act, a, best, rc, lu, myk, mypiv, myinv,
+                          singular);
     if (act) {
       // factors in getrf's row order (position myk), pivots as swaps
       double* __restrict__ wf = w + myk * NV;
 #pragma unroll
       for (int j = 0; j < NV; ++j) wf[j] = lu[j];
       w[NN + NV + r] = (double)mypiv;
-      // row myk of S_i | t_i: for the next row's update (shared memory) and
-      // the backward sweep (workspace); t_{N-1} = x_{N-1}
+      // row myk of S_i | t_i: for the unit's next row (shared memory, zeros
+      // after its last row) and the backward sweeps (workspace)
+      const bool last = t == cnt - 1;
       double* __restrict__ sgr = sg + row * SROW + myk * RS;
 #pragma unroll
       for (int j = 0; j < NV; ++j) {
         const double sj = a[NV + j] * myinv;
-        st[myk * RS + j] = sj;
+        st[myk * RS + j] = last ? 0.0 : sj;
         sgr[j] = sj;
       }
       const double tk = a[2 * NV] * myinv;
-      st[myk * RS + NV] = tk;
+      st[myk * RS + NV] = last ? 0.0 : tk;
       sgr[NV] = tk;
-      if (i == N - 1) {
-        X[row * NV + myk] = tk;
+      if (last) {
         if (singular && r == 0 && status) atomicOr(status, 1);
         singular = false;
       }
-      ++i;
+      ++t;
     }
     __syncwarp();
   }
 }
 
-// Backward sweep of the segmented solve: x_i = t_i - S_i x_{i+1} with
-// S_i = C'_i^-1 U_i and t_i = C'_i^-1 b'_i from the forward kernel (the
-// same recurrence as x_i = C'_i^-1 (b'_i - U_i x_{i+1}), one matrix-vector
-// product per row instead of two triangular solves) and x_{N-1} in x;
-// segments take systems from the queue as in the forward sweep.
+// Middle rows: for every system, row m = N / 2 couples to both sweeps,
+// (C_m - L_{m-1} S_{m-1} - U_m S^_{m+1}) x_m = b_m - L_{m-1} t_{m-1} -
+// U_m t^_{m+1} (a missing side drops out); one elimination per system,
+// factors kept at row m, x_m to x.
+template <int NV>
+__global__ void __launch_bounds__(kSegWarps * 32)
+    k_block_thomas_seg_mid(const double* __restrict__ Lm,
+                           const double* __restrict__ Cm,
+                           const double* __restrict__ Um,
+                           const double* __restrict__ B,
+                           double* __restrict__ X,
+                           const int64_t* __restrict__ row_off,
+                           const int* __restrict__ order, int nsys,
+                           double* __restrict__ work,
+                           int* __restrict__ counter,
+                           int* __restrict__ status) {
+  constexpr int RS = SegCfg<NV>::RS, NC = NV + 1;
+  constexpr int64_t NN = (int64_t)NV * NV, WROW = NN + 2 * NV,
+                    SROW = (int64_t)NV * RS;
+  constexpr unsigned full = 0xffffffffu;
+  const SegLane<NV> g;
+  const int r = g.r;
+  const double* __restrict__ sg = work + row_off[nsys] * WROW;
+  bool live = g.in_seg;
+  for (;;) {
+    const int q = seg_fetch(g, live, counter);
+    int N = 0;
+    int64_t r0 = 0;
+    if (live) {
+      if (q >= nsys) {
+        live = false;
+      } else {
+        const int s = order[q];
+        r0 = row_off[s];
+        const int64_t n64 = row_off[s + 1] - r0;
+        N = n64 > 0 ? (int)n64 : 0;
+      }
+    }
+    if (!__any_sync(full, live)) break;
+    const bool act = live && N > 0;
+    const int m = N >> 1;
+    const int64_t row = r0 + m;
+    double a[NC];
+    if (act) {
+      const double* __restrict__ Ci = Cm + row * NN + r * NV;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) a[j] = __ldg(Ci + j);
+      a[NV] = __ldg(B + row * NV + r);
+      if (m >= 1) {
+        const double* __restrict__ Li = Lm + (row - 1) * NN + r * NV;
+        const double* __restrict__ S = sg + (row - 1) * SROW;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          const double lk = __ldg(Li + k);
+#pragma unroll
+          for (int j = 0; j < NC; ++j) a[j] = fma(-lk, S[k * RS + j], a[j]);
+        }
+      }
+      if (m + 1 <= N - 1) {
+        const double* __restrict__ Ui = Um + row * NN + r * NV;
+        const double* __restrict__ S = sg + (row + 1) * SROW;
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+          const double uk = __ldg(Ui + k);
+#pragma unroll
+          for (int j = 0; j < NC; ++j) a[j] = fma(-uk, S[k * RS + j], a[j]);
+        }
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < NC; ++j) a[j] = 0.0;
+    }
+    double* __restrict__ w = work + row * WROW;
+    if (act) w[NN + r] = a[NV];
+    const unsigned best = seg_max(g, pivot_key(a[0], r));
+    const double rc = pyro_rcp3(a[0]);
+    int myk, mypiv;
+    double myinv, lu[NV];
+    bool singular = false;
+    seg_eliminate<NV, NC>(g, act, a, best, rc, lu, myk, mypiv, myinv,
+                          singular);
+    if (act) {
+      double* __restrict__ wf = w + myk * NV;
+#pragma unroll
+      for (int j = 0; j < NV; ++j) wf[j] = lu[j];
+      w[NN + NV + r] = (double)mypiv;
+      X[row * NV + myk] = a[NV] * myinv;
+      if (singular && r == 0 && status) atomicOr(status, 1);
+    }
+  }
+}
+
+// Backward sweeps from the middle row: unit (system, direction) as in the
+// forward kernel; downwards x_i = t_i - S_i x_{i+1} for i = m-1 .. 0,
+// upwards x_i = t^_i - S^_i x_{i-1} for i = m+1 .. N-1, starting from x_m.
 template <int NV>
 __global__ void __launch_bounds__(kSegWarps * 32)
     k_block_thomas_seg_back(double* __restrict__ X,
@@ -910,33 +1058,34 @@ __global__ void __launch_bounds__(kSegWarps * 32)
   const int r = g.r, base = g.base;
   const double* __restrict__ sg = work + row_off[nsys] * WROW;
   bool live = g.in_seg;
-  int i = -1;  // next row to solve, counting down; < 0: none
+  int cnt = 0, t = 0, dir = 0, m = 0;
   int64_t r0 = 0;
-  double x = 0.0;  // this lane's entry of x_{i+1}
+  double x = 0.0;  // this lane's entry of the previous row's x
   for (;;) {
-    const bool need = live && i < 0;
+    const bool need = live && t >= cnt;
     const int q = seg_fetch(g, need, counter);
     if (need) {
-      if (q >= nsys) {
+      if (q >= 2 * nsys) {
         live = false;
       } else {
-        const int s = order[q];
+        const int s = order[q >> 1];
+        dir = q & 1;
         r0 = row_off[s];
         const int64_t n64 = row_off[s + 1] - r0;
-        // one-row and empty systems have no backward rows
-        if (n64 >= 2) {
-          i = (int)n64 - 2;
-          x = X[(r0 + n64 - 1) * NV + r];
-        }
+        const int N = n64 > 0 ? (int)n64 : 0;
+        m = N >> 1;
+        cnt = seg_unit_rows(N, dir);
+        t = 0;
+        if (cnt > 0) x = X[(r0 + m) * NV + r];
       }
     }
     if (!__any_sync(full, live)) break;
-    const bool act = live && i >= 0;
-    const int64_t row = r0 + (act ? i : 0);
+    const bool act = live && t < cnt;
+    const int64_t row = r0 + (act ? (dir == 0 ? m - 1 - t : m + 1 + t) : 0);
     double v = 0.0, srow[NV];
     if (act) {
       const double* __restrict__ p = sg + row * SROW + r * RS;
-      if (i > 0) prefetch_row<RS>(p - SROW);
+      if (t + 1 < cnt) prefetch_row<RS>(dir == 0 ? p - SROW : p + SROW);
 #pragma unroll
       for (int j = 0; j < NV; ++j) srow[j] = p[j];
       v = p[NV];
@@ -952,9 +1101,222 @@ __global__ void __launch_bounds__(kSegWarps * 32)
     if (act) {
       x = v;
       X[row * NV + r] = v;
-      --i;
+      ++t;
     }
   }
+}
+
+// y = F^-1 v inside a segment: F's getrf factors (lane r holding factor
+// row r, f, and its diagonal d) and pivots, v in original row order on the
+// lanes; returns this lane's entry of y (variable order).
+template <int NV>
+__device__ __forceinline__ double seg_lu_solve(const SegLane<NV>& g,
+                                               const double (&f)[NV],
+                                               double d, int perm_src,
+                                               double v) {
+  constexpr unsigned full = 0xffffffffu;
+  const int r = g.r, base = g.base;
+  double y = __shfl_sync(full, v, base + perm_src);
+  // unit lower: y_r -= L[r][k] y_k, k < r
+#pragma unroll
+  for (int k = 0; k < NV - 1; ++k) {
+    const double yk = __shfl_sync(full, y, base + k);
+    if (r > k) y = fma(-f[k], yk, y);
+  }
+  // upper: y_r = (y_r - sum_{k > r} U[r][k] y_k) / U[r][r]
+  const double inv = pyro_rcp3(d);
+#pragma unroll
+  for (int k = NV - 1; k >= 0; --k) {
+    if (r == k) y *= inv;
+    const double yk = __shfl_sync(full, y, base + k);
+    if (r < k) y = fma(-f[k], yk, y);
+  }
+  return y;
+}
+
+// Re-solve after pyro_block_thomas_seg, with its kept factors (two-ended,
+// like the solve): per system and right-hand side, in steps
+// v = base - M y [then y = F^-1 v], y the previous step's result:
+//   1  rows i = 0 .. m-1:        base b_i, M = L_{i-1} (none at i = 0), F_i
+//   2  row m:                    base b_m, M = L_{m-1} (none at m = 0)
+//   3  rows i = N-1 .. m+1:      base b_i, M = U_i (none at i = N-1), F_i
+//   4  row m:                    base step 2's v, M = U_m (none without
+//                                rows below m), F_m: x_m
+//   5  rows i = m-1 .. 0:        base t_i, M = S_i (y = x_m first)
+//   6  rows i = m+1 .. N-1:      base t^_i, M = S^_i (y = x_m first)
+// with the intermediate vectors in x.  Every segment runs one step per
+// warp step, at its own system, right-hand side and phase.
+template <int NV>
+__global__ void __launch_bounds__(kSegWarps * 32)
+    k_block_thomas_seg_resolve(const double* __restrict__ Lm,
+                               const double* __restrict__ Um,
+                               const double* __restrict__ B,
+                               double* __restrict__ X, int nrhs,
+                               int64_t rhs_stride,
+                               const int64_t* __restrict__ row_off,
+                               const int* __restrict__ order, int nsys,
+                               const double* __restrict__ work,
+                               int* __restrict__ counter,
+                               int* __restrict__ status) {
+  constexpr int RS = SegCfg<NV>::RS;
+  constexpr int64_t NN = (int64_t)NV * NV, WROW = NN + 2 * NV,
+                    SROW = (int64_t)NV * RS;
+  constexpr unsigned full = 0xffffffffu;
+  const SegLane<NV> g;
+  const int r = g.r, base = g.base;
+  const double* __restrict__ sg = work + row_off[nsys] * WROW;
+  bool live = g.in_seg, busy = false;
+  int N = 0, m = 0, c = 0, ph = 0, i = 0;
+  int64_t r0 = 0;
+  double y = 0.0, xm = 0.0;
+  for (;;) {
+    const bool need = live && !busy;
+    const int q = seg_fetch(g, need, counter);
+    if (need) {
+      if (q >= nsys) {
+        live = false;
+      } else {
+        const int s = order[q];
+        r0 = row_off[s];
+        const int64_t n64 = row_off[s + 1] - r0;
+        N = n64 > 0 ? (int)n64 : 0;
+        if (n64 <= 0 && r == 0 && status) atomicOr(status, 2);
+        m = N >> 1;
+        c = 0;
+        ph = 1;
+        i = 0;
+        busy = N > 0;
+      }
+    }
+    if (!__any_sync(full, live)) break;
+    // skip the empty phases (1: no rows above m; 3: none below; 5, 6
+    // likewise) and move to the next right-hand side after phase 6
+    if (busy && ph == 1 && i >= m) { ph = 2; i = m; }
+    if (busy && ph == 3 && i < m + 1) { ph = 4; i = m; }
+    if (busy && ph == 5 && i < 0) { ph = 6; i = m + 1; y = xm; }
+    if (busy && ph == 6 && i > N - 1) {
+      if (++c < nrhs) {
+        ph = m >= 1 ? 1 : 2;
+        i = 0;
+      } else {
+        busy = false;
+      }
+    }
+    const bool act = live && busy;
+    const int64_t row = r0 + i;
+    const double* __restrict__ Bc = B + (int64_t)c * rhs_stride;
+    double* __restrict__ Xc = X + (int64_t)c * rhs_stride;
+    // the step's base, coupling rows and whether it solves with F_row
+    double v = 0.0, mrow[NV];
+    bool solve = false, coupled = false;
+    if (act) {
+      const double* __restrict__ M = nullptr;
+      int64_t mstride = NV;
+      if (ph == 1) {
+        v = __ldg(Bc + row * NV + r);
+        if (i > 0) M = Lm + (row - 1) * NN;
+        solve = true;
+      } else if (ph == 2) {
+        v = __ldg(Bc + row * NV + r);
+        if (m >= 1) M = Lm + (row - 1) * NN;
+      } else if (ph == 3) {
+        v = __ldg(Bc + row * NV + r);
+        if (i < N - 1) M = Um + row * NN;
+        solve = true;
+      } else if (ph == 4) {
+        v = Xc[row * NV + r];
+        if (m + 1 <= N - 1) M = Um + row * NN;
+        solve = true;
+      } else {
+        v = Xc[row * NV + r];
+        M = sg + row * SROW;
+        mstride = RS;
+      }
+      coupled = M != nullptr;
+      const double* __restrict__ Mr = (coupled ? M : Bc + row * NV) +
+                                      (coupled ? r * mstride : 0);
+#pragma unroll
+      for (int k = 0; k < NV; ++k) mrow[k] = coupled ? Mr[k] : 0.0;
+    } else {
+#pragma unroll
+      for (int k = 0; k < NV; ++k) mrow[k] = 0.0;
+    }
+    // an uncoupled step takes nothing from y (which may hold a previous
+    // system's non-finite result)
+    const double ys = coupled ? y : 0.0;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+      const double yk = __shfl_sync(full, ys, base + k);
+      v = fma(-mrow[k], yk, v);
+    }
+    // y = F^-1 v where the step solves (the other segments' lanes pass v)
+    if (__any_sync(full, solve)) {
+      const double* __restrict__ w = work + row * WROW;
+      double f[NV], d = 1.0;
+      int perm_src = r;
+      if (solve) {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) f[j] = w[r * NV + j];
+        d = f[0];
+#pragma unroll
+        for (int j = 1; j < NV; ++j)
+          if (j == r) d = f[j];
+        // original row held at position r after getrf's swaps
+        int j = r;
+#pragma unroll
+        for (int k = NV - 1; k >= 0; --k) {
+          const int pk = (int)w[NN + NV + k];
+          if (j == k)
+            j = pk;
+          else if (j == pk)
+            j = k;
+        }
+        perm_src = j;
+      } else {
+#pragma unroll
+        for (int j = 0; j < NV; ++j) f[j] = 0.0;
+      }
+      const double yl = seg_lu_solve<NV>(g, f, d, perm_src, v);
+      if (solve) v = yl;
+    }
+    if (act) {
+      Xc[row * NV + r] = v;
+      y = v;
+      if (ph == 1) {
+        ++i;
+      } else if (ph == 2) {
+        ph = 3;
+        i = N - 1;
+      } else if (ph == 3) {
+        --i;
+      } else if (ph == 4) {
+        xm = v;
+        ph = 5;
+        i = m - 1;
+      } else if (ph == 5) {
+        --i;
+      } else {
+        ++i;
+      }
+    }
+  }
+}
+
+template <int NV>
+int seg_grid(const void* kernel, int nunits, int ctas) {
+  const int per_cta = kSegWarps * SegCfg<NV>::P;
+  const int need = (nunits + per_cta - 1) / per_cta;
+  if (ctas <= 0) {
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+            &per_sm, kernel, kSegWarps * 32, 0) != cudaSuccess ||
+        per_sm < 1) {
+      (void)cudaGetLastError();
+      per_sm = 1;
+    }
+    ctas = per_sm * pyro_sm_count();
+  }
+  return ctas < need ? ctas : need;
 }
 
 template <int NV>
@@ -962,28 +1324,35 @@ int launch_seg(const double* L, const double* C, const double* U,
                const double* b, double* x, const int64_t* row_off,
                const int* order, int nsys, double* work, int* counter,
                int* status, int ctas, cudaStream_t stream) {
-  const int per_cta = kSegWarps * SegCfg<NV>::P;
-  const int need = (nsys + per_cta - 1) / per_cta;
-  // default grid: one warp per SM partition
-  if (ctas <= 0) ctas = pyro_sm_count() * 4 / kSegWarps;
-  if (ctas > need) ctas = need;
-  // the backward sweep has few FP64 instructions per row and waits on its
-  // loads and shuffles: as many warps as fit
-  int per_sm = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-          &per_sm, k_block_thomas_seg_back<NV>, kSegWarps * 32, 0) !=
-          cudaSuccess ||
-      per_sm < 1) {
-    (void)cudaGetLastError();
-    per_sm = 1;
+  // forward grid: by default two warps per SM partition (one's shuffle,
+  // redux and reciprocal latencies under the other's FP64 work) when every
+  // segment gets two sweeps or more (8,192 sweeps of 32..512 rows at nv =
+  // 10: 15.3 ms against 19.2 ms with one warp, 17.0 ms with three), else
+  // one
+  const int units = 2 * nsys;
+  if (ctas <= 0) {
+    const int segs_per_warp_slot = pyro_sm_count() * 4 * SegCfg<NV>::P;
+    const int w = units >= 2 * 2 * segs_per_warp_slot ? 2 : 1;
+    ctas = pyro_sm_count() * w * 4 / kSegWarps;
   }
-  int back = per_sm * pyro_sm_count();
-  if (back > need) back = need;
+  const int fwd = seg_grid<NV>((const void*)k_block_thomas_seg<NV>, units,
+                               ctas);
+  const int mid = seg_grid<NV>((const void*)k_block_thomas_seg_mid<NV>, nsys,
+                               0);
+  const int back = seg_grid<NV>((const void*)k_block_thomas_seg_back<NV>,
+                                units, 0);
   if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
     (void)cudaGetLastError();
     return PYRO_ERR_LAUNCH;
   }
-  k_block_thomas_seg<NV><<<ctas, kSegWarps * 32, 0, stream>>>(
+  k_block_thomas_seg<NV><<<fwd, kSegWarps * 32, 0, stream>>>(
+      L, C, U, b, row_off, order, nsys, work, counter, status);
+  PYRO_CHECK_LAUNCH();
+  if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  k_block_thomas_seg_mid<NV><<<mid, kSegWarps * 32, 0, stream>>>(
       L, C, U, b, x, row_off, order, nsys, work, counter, status);
   PYRO_CHECK_LAUNCH();
   if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
@@ -996,13 +1365,34 @@ int launch_seg(const double* L, const double* C, const double* U,
   return PYRO_OK;
 }
 
+template <int NV>
+int launch_seg_resolve(const double* L, const double* U, const double* B,
+                       double* X, int nrhs, int64_t rhs_stride,
+                       const int64_t* row_off, const int* order, int nsys,
+                       const double* work, int* counter, int* status,
+                       cudaStream_t stream) {
+  const int grid = seg_grid<NV>(
+      (const void*)k_block_thomas_seg_resolve<NV>, nsys, 0);
+  if (cudaMemsetAsync(counter, 0, sizeof(int), stream) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return PYRO_ERR_LAUNCH;
+  }
+  k_block_thomas_seg_resolve<NV><<<grid, kSegWarps * 32, 0, stream>>>(
+      L, U, B, X, nrhs, rhs_stride, row_off, order, nsys, work, counter,
+      status);
+  PYRO_CHECK_LAUNCH();
+  return PYRO_OK;
+}
+
 }  // namespace
 
 // pyro_block_thomas for blocks of size nv <= 16 with 32 / nv systems per
 // warp, one lane per block row (see above).  Same arguments and workspace
-// layout as pyro_block_thomas; two launches (forward, backward); the CTA
-// size is fixed (four warps); ctas: forward grid size (0 = one warp per SM
-// partition).
+// size as pyro_block_thomas (the factors two-ended: re-solve with
+// pyro_block_thomas_seg_resolve); three launches (sweeps to the middle
+// rows, middle rows, sweeps back); the CTA size is fixed (four warps);
+// ctas: forward grid size (0 = one or two warps per SM partition by the
+// batch size).
 PYRO_EXPORT int pyro_block_thomas_seg(const double* L, const double* C,
                                       const double* U, const double* b,
                                       double* x, const int64_t* row_off,
@@ -1028,11 +1418,42 @@ PYRO_EXPORT int pyro_block_thomas_seg(const double* L, const double* C,
   }
 }
 
+// More right-hand sides after pyro_block_thomas_seg (whose two-ended
+// factors the re-solve below cannot use): arguments as for
+// pyro_block_thomas_resolve, nv <= 16.
+PYRO_EXPORT int pyro_block_thomas_seg_resolve(
+    const double* L, const double* U, const double* B, double* X,
+    int nrhs, int64_t rhs_stride, const int64_t* row_off, const int* order,
+    int nsys, int nv, const double* work, int* counter, int* status,
+    cudaStream_t stream) {
+  if (nsys < 0 || nv < 1 || nv > 16 || nrhs < 1 || nrhs > 4)
+    return PYRO_ERR_ARGUMENT;
+  if (nsys == 0) return PYRO_OK;
+  if (!L || !U || !B || !X || !row_off || !order || !work || !counter)
+    return PYRO_ERR_ARGUMENT;
+  if (nrhs > 1 && rhs_stride < 1) return PYRO_ERR_ARGUMENT;
+  switch (nv) {
+#define PYRO_BT_SEGR(NV)                                                     \
+  case NV:                                                                   \
+    return launch_seg_resolve<NV>(L, U, B, X, nrhs, rhs_stride, row_off,     \
+                                  order, nsys, work, counter, status,        \
+                                  stream);
+    PYRO_BT_SEGR(1) PYRO_BT_SEGR(2) PYRO_BT_SEGR(3) PYRO_BT_SEGR(4)
+    PYRO_BT_SEGR(5) PYRO_BT_SEGR(6) PYRO_BT_SEGR(7) PYRO_BT_SEGR(8)
+    PYRO_BT_SEGR(9) PYRO_BT_SEGR(10) PYRO_BT_SEGR(11) PYRO_BT_SEGR(12)
+    PYRO_BT_SEGR(13) PYRO_BT_SEGR(14) PYRO_BT_SEGR(15) PYRO_BT_SEGR(16)
+#undef PYRO_BT_SEGR
+    default:
+      return PYRO_ERR_ARGUMENT;
+  }
+}
+
 // ------------------------------------------------------------------------
 // Re-solve with kept factors.
 //
 // After pyro_block_thomas or pyro_block_thomas_small, `work` holds for
-// every row the LU factors and pivots of C'_i.  More right-hand sides for
+// every row the LU factors and pivots of C'_i (pyro_block_thomas_seg's
+// two-ended factors have their own re-solve above).  More right-hand sides for
 // the same L, C, U (the EOS-consistency adjoint solves share one operator,
 // thermodynamic_consistency.py:105-307; a chord Newton iteration reuses its
 // Jacobian) need only the vector recurrences:
@@ -1233,7 +1654,7 @@ int launch_resolve(const double* L, const double* U, const double* B,
 
 // nrhs (1..4) right-hand sides B[c][rows][nv] (c-th at B + c * rhs_stride)
 // -> X[c][rows][nv] for the systems whose factors a previous
-// pyro_block_thomas / _small / _seg call with the same L, C, U left in
+// pyro_block_thomas / _small call with the same L, C, U left in
 // `work`.  order, counter as for pyro_block_thomas (counter zeroed here);
 // status (may be NULL): bit 1 for an empty row range; nv <= 64.  B and X
 // must not overlap.  Asynchronous on `stream`.

@@ -176,15 +176,17 @@ class BlockThomasSolver:
             raise ValueError("out must be contiguous and shaped like B")
         stream = torch.cuda.current_stream(self.device)
         n = Bv.shape[0]
+        fn = (self.lib.pyro_block_thomas_seg_resolve if self.kernel == "seg"
+              else self.lib.pyro_block_thomas_resolve)
         for c0 in range(0, n, 4):
             k = min(4, n - c0)
-            _check(self.lib.pyro_block_thomas_resolve(
+            _check(fn(
                 L.data_ptr(), U.data_ptr(), Bv[c0].data_ptr(),
                 Xv[c0].data_ptr(), k, rows * nv, self.offsets.data_ptr(),
                 self.order.data_ptr(), self.nsys, nv, self.work.data_ptr(),
                 self.counter.data_ptr(), self.status.data_ptr(),
                 ctypes.c_void_p(stream.cuda_stream)),
-                "pyro_block_thomas_resolve")
+                "block-Thomas re-solve")
         return X
 
     def check_status(self):

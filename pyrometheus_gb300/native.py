@@ -170,6 +170,9 @@ def block_thomas_lib() -> ctypes.CDLL:
     lib.pyro_block_thomas_resolve.restype = I
     lib.pyro_block_thomas_resolve.argtypes = [P, P, P, P, I, I64, P, P, I, I,
                                               P, P, P, P]
+    lib.pyro_block_thomas_seg_resolve.restype = I
+    lib.pyro_block_thomas_seg_resolve.argtypes = [P, P, P, P, I, I64, P, P,
+                                                  I, I, P, P, P, P]
     return lib
 
 

@@ -129,11 +129,11 @@ def test_cuda_block_thomas_uneven_batch(nv, kernel):
 @pytest.mark.parametrize("ctas", [1, 3])
 def test_seg_segments_take_systems_in_turn(nv, ctas):
     """The segmented kernel with a grid far smaller than the batch: one or
-    three CTAs of four warps, so every lane segment solves tens of systems
-    of uneven lengths one after another (forward sweeps, then backward
-    sweeps, each segment taking the next system of the order when its own
-    is done), lengths 1 to 90 (one-row systems included); in a CUDA graph,
-    replayed with new right-hand sides."""
+    three CTAs of four warps, so every lane segment runs tens of sweeps of
+    uneven lengths one after another (each segment taking the next sweep of
+    the order when its own is done), lengths 1 to 90 (one- and two-row
+    systems, whose sweeps are empty, included); in a CUDA graph, replayed
+    with new right-hand sides, then two more through the re-solve."""
     _cuda()
     from pyrometheus_gb300.flamelet import BlockThomasSolver
     lengths, L, C, U, b = make_systems(300, nv, 1, 90, seed=40 + nv)
@@ -150,6 +150,12 @@ def test_seg_segments_take_systems_in_turn(nv, ctas):
     t[3].copy_(torch.as_tensor(b2))
     got2 = solver.solve(*t).cpu().numpy()
     assert _rel(got2, solve_packed(lengths, L, C, U, b2)) < 1e-10
+    # two more right-hand sides from the kept factors
+    B = np.random.default_rng(nv + 1).standard_normal((2,) + b.shape)
+    X = solver.resolve(t[0], t[2], torch.as_tensor(B, device=dev))
+    X = X.cpu().numpy()
+    for c in range(2):
+        assert _rel(X[c], solve_packed(lengths, L, C, U, B[c])) < 1e-10
 
 
 @pytest.mark.gpu
@@ -226,7 +232,9 @@ def test_empty_systems_are_skipped_and_flagged(kernel):
     b2 = torch.as_tensor(rng.standard_normal((rows, nv)), device=dev)
     x2 = torch.full_like(b2, float("nan"))
     status.zero_()
-    assert lib.pyro_block_thomas_resolve(
+    resolve = (lib.pyro_block_thomas_seg_resolve if kernel == "seg"
+               else lib.pyro_block_thomas_resolve)
+    assert resolve(
         t[0].data_ptr(), t[2].data_ptr(), b2.data_ptr(), x2.data_ptr(), 1,
         0, offs.data_ptr(), order.data_ptr(), 5, nv, work.data_ptr(),
         counter.data_ptr(), status.data_ptr(), sp) == 0
@@ -238,9 +246,10 @@ def test_empty_systems_are_skipped_and_flagged(kernel):
 
 @pytest.mark.gpu
 def test_seg_kernel_workspace_serves_resolve_and_matches_cta():
-    """The several-systems-per-warp kernel keeps getrf's factors and pivots
-    in the shared workspace layout: re-solves from its workspace equal
-    fresh solves, and its solution equals the CTA kernel's to rounding."""
+    """The several-systems-per-warp kernel keeps its two-ended factors, S |
+    t blocks and pivots in the workspace: re-solves from it (its own
+    re-solve, three right-hand sides in one call) equal fresh solves, and
+    its solution equals the CTA kernel's to rounding."""
     _cuda()
     from pyrometheus_gb300.flamelet import BlockThomasSolver
     lengths, L, C, U, b = make_systems(97, 10, 1, 90, seed=23)
