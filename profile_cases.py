@@ -3,8 +3,9 @@
     python profile_cases.py jacobian [states]
     python profile_cases.py vjp [states]
     python profile_cases.py block_thomas [nv] [systems] [n_min] [n_max]
-    python profile_cases.py block_thomas_seg [nv] [systems] [n_min] [n_max]
+    python profile_cases.py block_thomas_seg [nv] [systems] [n_min] [n_max] [ctas]
     python profile_cases.py block_thomas_resolve [nv] [systems] [n_min] [n_max]
+    python profile_cases.py block_thomas_seg_resolve [nv] [systems] [n_min] [n_max]
     python profile_cases.py batched_lu [nv] [cells]
     python profile_cases.py transport [states]
     python profile_cases.py serving [cells] [launches]
@@ -65,7 +66,8 @@ def jacobian(states: int = 1 << 15, vjp: bool = False):
 
 
 def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
-                 n_max: int = 1024, kernel=None, resolve=False):
+                 n_max: int = 1024, ctas: int = 0, kernel=None,
+                 resolve=False):
     import torch
 
     from pyrometheus_gb300.flamelet import BlockThomasSolver
@@ -80,7 +82,8 @@ def block_thomas(nv: int = 10, systems: int = 304, n_min: int = 64,
     L = torch.randn((rows, nv, nv), generator=g, **f64)
     U = torch.randn((rows, nv, nv), generator=g, **f64)
     b = torch.randn((rows, nv), generator=g, **f64)
-    solver = BlockThomasSolver(nv, lengths, device=dev, kernel=kernel)
+    solver = BlockThomasSolver(nv, lengths, device=dev, kernel=kernel,
+                               ctas=ctas)
     for _ in range(3):
         solver.solve(L, C, U, b)
     if resolve:
@@ -260,7 +263,9 @@ def main(argv=None):
     elif case == "block_thomas_seg":
         block_thomas(*rest, kernel="seg")
     elif case == "block_thomas_resolve":
-        block_thomas(*rest, resolve=True)
+        block_thomas(*rest, kernel="cta", resolve=True)
+    elif case == "block_thomas_seg_resolve":
+        block_thomas(*rest, kernel="seg", resolve=True)
     elif case == "batched_lu":
         batched_lu(*rest)
     elif case == "transport":
