@@ -381,6 +381,38 @@ class _Emitter:
         z_off = [zero_offs[it * jgroup + ln]
                  if it * jgroup + ln < len(zero_offs) else 0xFFFF
                  for it in range(ziters) for ln in range(jgroup)]
+        # reaction blocks: the 32 lanes of one warp in one round run
+        # reactions of one kind (a falloff round, a three-body round, the
+        # elementary rounds), never a mix whose branches the warp would run
+        # one after another; blocks go to the warps of a state's group by
+        # estimated cost (longest first to the least loaded warp), and
+        # jq_lane_rx[round][lane] is the reaction of each lane (-1: none)
+        # (with all reactions in one round anyway, a warp that mixes kinds
+        # runs each branch once either way, and one round shares the rest)
+        cat_cost = {"falloff": 3.0, "three-body": 1.25, "elementary": 1.0}
+        blocks: List[List] = []
+        for qq, j in enumerate(perm):
+            kind = m.rx[j].kind
+            if not blocks or blocks[-1][0] != kind or len(blocks[-1][1]) == 32:
+                blocks.append([kind, []])
+            blocks[-1][1].append(qq)
+        nwarp = jgroup // 32
+        warp_blocks: List[List[List[int]]] = [[] for _ in range(nwarp)]
+        load = [0.0] * nwarp
+        for kind, qs in sorted(blocks, key=lambda b: -cat_cost[b[0]]):
+            wi = min(range(nwarp), key=lambda i: (load[i], i))
+            warp_blocks[wi].append(qs)
+            load[wi] += cat_cost[kind]
+        q_rounds = max(len(x) for x in warp_blocks)
+        lane_rx = []
+        if R <= jgroup:
+            q_rounds = 1
+            lane_rx = list(range(R)) + [-1] * (jgroup - R)
+        for rd in range(q_rounds if R > jgroup else 0):
+            for wi in range(nwarp):
+                qs = warp_blocks[wi][rd] if rd < len(warp_blocks[wi]) else []
+                lane_rx.extend(qs[ln] if ln < len(qs) else -1
+                               for ln in range(32))
         # species -> third-body entries (permuted reaction, e - default)
         stinc: List[List[Tuple[int, float]]] = [[] for _ in range(S)]
         for qq, j in enumerate(perm):
@@ -407,6 +439,65 @@ class _Emitter:
         for k in range(S):
             si_slot.extend(inc[k])
             si0.append(len(si_slot))
+        # per-species sums over a species' slots (five FMAs each) and its
+        # third-body entries (one or two), split into parts of nearly equal
+        # weight so the group's threads (one part each per round) run
+        # balanced loops; a species' first part is its owner, which adds
+        # the others' partial sums in order
+        wt = [5 * (si0[k + 1] - si0[k]) + 2 * (st0[k + 1] - st0[k])
+              for k in range(S)]
+        target = max(1, -(-sum(wt) // jgroup))
+        while True:
+            parts = []
+            for k in range(S):
+                n_sl = si0[k + 1] - si0[k]
+                n_p = max(1, -(-wt[k] // target))
+                n_p = min(n_p, max(1, n_sl))
+                for pp in range(n_p):
+                    a0 = si0[k] + (n_sl * pp) // n_p
+                    a1 = si0[k] + (n_sl * (pp + 1)) // n_p
+                    last = pp == n_p - 1
+                    parts.append((k, pp, a0, a1,
+                                  st0[k] if last else 0,
+                                  st0[k + 1] if last else 0))
+            # one part per thread and round at most, and the others' partial
+            # sums must fit the q vector they reuse (5 doubles a part)
+            if (len(parts) <= jgroup and 5 * (len(parts) - S) <= R) or \
+                    target >= max(wt):
+                break
+            target += 1
+        p_rounds = -(-len(parts) // jgroup)
+        # non-owner parts keep their partial sums in scratch slots; the
+        # owner lists them
+        extra_of: List[List[int]] = [[] for _ in range(S)]
+        p_sp, p_s0, p_s1, p_t0, p_t1, p_slot = [], [], [], [], [], []
+        nextra = 0
+        for (k, pp, a0, a1, t0, t1) in parts:
+            p_sp.append(k)
+            p_s0.append(a0)
+            p_s1.append(a1)
+            p_t0.append(t0)
+            p_t1.append(t1)
+            if pp == 0:
+                p_slot.append(-1)
+            else:
+                p_slot.append(nextra)
+                extra_of[k].append(nextra)
+                nextra += 1
+        pad = p_rounds * jgroup - len(parts)
+        p_sp += [-1] * pad
+        p_s0 += [0] * pad
+        p_s1 += [0] * pad
+        p_t0 += [0] * pad
+        p_t1 += [0] * pad
+        p_slot += [-1] * pad
+        px0, px_slot = [0], []
+        for k in range(S):
+            px_slot.extend(extra_of[k])
+            px0.append(len(px_slot))
+        if 5 * nextra > R:
+            raise NotImplementedError("per-species parts exceed the "
+                                      "scratch of the Jacobian kernel")
         nf = max(1, len(fo_low))
         nasa = [[m.tmid[k]] + list(m.hi[k]) + list(m.lo[k]) + [0.0]
                 for k in range(S)]
@@ -428,6 +519,21 @@ class _Emitter:
         w(f"#define JW_DOUBLES {jw_doubles}")
         w(f"#define JGROUP {jgroup}")
         w(f"#define JGROUPS {jgroups}")
+        w(f"#define JQ_ROUNDS {q_rounds}")
+        w(f"#define JP_ROUNDS {p_rounds}")
+        w(arr("short", "jq_lane_rx", [q_rounds * jgroup],
+              [_cint(v) for v in lane_rx]))
+        w(arr("short", "jp_sp", [p_rounds * jgroup],
+              [_cint(v) for v in p_sp]))
+        w(arr("int", "jp_s0", [p_rounds * jgroup], [_cint(v) for v in p_s0]))
+        w(arr("int", "jp_s1", [p_rounds * jgroup], [_cint(v) for v in p_s1]))
+        w(arr("int", "jp_t0", [p_rounds * jgroup], [_cint(v) for v in p_t0]))
+        w(arr("int", "jp_t1", [p_rounds * jgroup], [_cint(v) for v in p_t1]))
+        w(arr("short", "jp_slot", [p_rounds * jgroup],
+              [_cint(v) for v in p_slot]))
+        w(arr("int", "jp_x0", [S + 1], [_cint(v) for v in px0]))
+        w(arr("short", "jp_xslot", [max(1, len(px_slot))],
+              [_cint(v) for v in (px_slot or [0])]))
         w(arr("int", "jq_flags", [R], [_cint(flags[j]) for j in perm]))
         w(arr("int", "jq_slot0", [R + 1], [_cint(v) for v in slot0]))
         w(arr("int", "jq_nr", [R], [_cint(v) for v in q_nr]))
@@ -695,14 +801,15 @@ class _Emitter:
                  [_cint(v) for v in (st_rx or [0])]))
         w(_table(qual, "double", "k_st_de", [max(1, len(st_de))],
                  [_hexd(v) for v in (st_de or [0.0])]))
-        # reactions ordered by kind for the warp-per-state Jacobian: lanes
-        # of a warp take consecutive entries, so same-kind reactions run
-        # side by side (no serialised falloff/third-body branches)
+        # reactions ordered for the Jacobian kernel's lane blocks: by kind,
+        # then reversibility, side sizes and rate form, so the reactions a
+        # warp runs side by side take the same branches and trip counts
         def kind_key(j):
             r = m.rx[j]
             rank = {"elementary": 0, "three-body": 1, "falloff": 2}[r.kind]
             troe = 1 if r.kind == "falloff" and r.ftype == "Troe" else 0
-            return (rank, troe, flags[j] >> 3 & 3, j)
+            return (rank, troe, int(r.reversible), len(r.fwd), len(r.rev),
+                    flags[j] >> 3 & 3, j)
         perm = sorted(range(R), key=kind_key)
         w(_table(qual, "short", "k_rx_perm", [R], [_cint(v) for v in perm]))
         L.extend(self._jacobian_tables(perm, flags, rates, dnu, defeff,

@@ -19,8 +19,10 @@
 //   mass-action dq/dc_m;
 //   chain rule through c(T, Y) and rho(T, Y), then the dT/dt row.
 //
-// k_reactor_jacobian: one warp per state.  Lanes take reactions in an
-// order sorted by kind, so a warp's lanes run the same code path; the
+// k_reactor_jacobian: a group of one warp per state (two warps for large
+// mechanisms).  Lanes take reactions in generated blocks of one kind per
+// warp and round (sorted by reversibility and side sizes within), so a
+// warp's lanes run the same code path and trip counts; the
 // tables they index with different reactions or species are global-memory
 // copies read through L1 (the constant cache would serialise the 32
 // different addresses).  Each lane writes, per slot of its reaction, the
@@ -547,34 +549,82 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
     s.c0 = LOG_P0_OVER_R - lnT;
     s.ctot = pyro::group_sum(ct, gid, t, red);
     pyro::group_sync(gid);
-    // per reaction (threads over the kind-sorted numbering)
-    for (int qq = t; qq < NR; qq += JGROUP)
-      pyro::jac_reaction(qq, s, c, g, h, D, Dq, DdT, Hq, Qc);
+    // per reaction: lane blocks of one kind per warp and round (the
+    // generated map jq_lane_rx; -1 for an idle lane)
+#pragma unroll 1
+    for (int rd = 0; rd < JQ_ROUNDS; ++rd) {
+      const int qq = __ldg(jq_lane_rx + rd * JGROUP + t);
+      if (qq >= 0) pyro::jac_reaction(qq, s, c, g, h, D, Dq, DdT, Hq, Qc);
+    }
     pyro::group_sync(gid);
-    // per species k: w_k, dw_k/dT|c, the rank-1 third-body vector a_k,
-    // u_k = sum_m dw_k/dc_m c_m and the column sum
-    // shj_k = RT sum_j h_j dw_j/dc_k, from per-reaction sums; then the
-    // row constants of the assembly
     const double RT = GAS_CONSTANT * T;
     const double inv_sig = 1.0 / sigma;
-    double pQ = 0.0, pHA = 0.0, pHU = 0.0, pdQ = 0.0;
-    for (int k = t; k < NS; k += JGROUP) {
+    // the sums run over parts of each species' slot list of nearly equal
+    // length (generated: jp_*), one per thread and round; a species' other
+    // parts leave their partial sums in the dead q vector for its owner
+    double pw[JP_ROUNDS], pjt[JP_ROUNDS], pa[JP_ROUNDS], pu[JP_ROUNDS],
+        phj[JP_ROUNDS];
+#pragma unroll
+    for (int rd = 0; rd < JP_ROUNDS; ++rd) {
+      const int e = rd * JGROUP + t;
       double w = 0.0, jt = 0.0, a = 0.0, u = 0.0, hj = 0.0;
-      const int t1 = __ldg(jg_si0 + k + 1);
-      for (int t = __ldg(jg_si0 + k); t < t1; ++t) {
-        const int sl = __ldg(jg_si_slot + t);
-        const int qq = __ldg(jq_slot_rx + sl);
-        const double nu = __ldg(jq_nu + sl);
-        w = fma(nu, Dq[qq], w);
-        jt = fma(nu, DdT[qq], jt);
-        a = fma(__ldg(jq_slot_anu + sl), D[NSLOT + qq], a);
-        u = fma(nu, Qc[qq], u);
-        hj = fma(Hq[qq], D[sl], hj);
+      if (__ldg(jp_sp + e) >= 0) {
+        const int t1 = __ldg(jp_s1 + e);
+        for (int t = __ldg(jp_s0 + e); t < t1; ++t) {
+          const int sl = __ldg(jg_si_slot + t);
+          const int qq = __ldg(jq_slot_rx + sl);
+          const double nu = __ldg(jq_nu + sl);
+          w = fma(nu, Dq[qq], w);
+          jt = fma(nu, DdT[qq], jt);
+          a = fma(__ldg(jq_slot_anu + sl), D[NSLOT + qq], a);
+          u = fma(nu, Qc[qq], u);
+          hj = fma(Hq[qq], D[sl], hj);
+        }
+        const int e1 = __ldg(jp_t1 + e);
+        for (int t = __ldg(jp_t0 + e); t < e1; ++t) {
+          const int qq = __ldg(jg_st_q + t);
+          hj = fma(Hq[qq] * __ldg(jg_st_de + t), D[NSLOT + qq], hj);
+        }
       }
-      const int e1 = __ldg(jg_st0 + k + 1);
-      for (int t = __ldg(jg_st0 + k); t < e1; ++t) {
-        const int qq = __ldg(jg_st_q + t);
-        hj = fma(Hq[qq] * __ldg(jg_st_de + t), D[NSLOT + qq], hj);
+      pw[rd] = w;
+      pjt[rd] = jt;
+      pa[rd] = a;
+      pu[rd] = u;
+      phj[rd] = hj;
+    }
+    pyro::group_sync(gid);  // every thread is done with Dq
+    double* px = Dq;
+#pragma unroll
+    for (int rd = 0; rd < JP_ROUNDS; ++rd) {
+      const int sl = __ldg(jp_slot + rd * JGROUP + t);
+      if (sl >= 0) {
+        px[5 * sl] = pw[rd];
+        px[5 * sl + 1] = pjt[rd];
+        px[5 * sl + 2] = pa[rd];
+        px[5 * sl + 3] = pu[rd];
+        px[5 * sl + 4] = phj[rd];
+      }
+    }
+    pyro::group_sync(gid);
+    // per species k (its owner thread): w_k, dw_k/dT|c, the rank-1
+    // third-body vector a_k, u_k = sum_m dw_k/dc_m c_m and the column sum
+    // shj_k = RT sum_j h_j dw_j/dc_k; then the row constants of the
+    // assembly
+    double pQ = 0.0, pHA = 0.0, pHU = 0.0, pdQ = 0.0;
+#pragma unroll
+    for (int rd = 0; rd < JP_ROUNDS; ++rd) {
+      const int e = rd * JGROUP + t;
+      const int k = __ldg(jp_sp + e);
+      if (k < 0 || __ldg(jp_slot + e) >= 0) continue;
+      double w = pw[rd], jt = pjt[rd], a = pa[rd], u = pu[rd], hj = phj[rd];
+      const int x1 = __ldg(jp_x0 + k + 1);
+      for (int x = __ldg(jp_x0 + k); x < x1; ++x) {
+        const double* q = px + 5 * __ldg(jp_xslot + x);
+        w += q[0];
+        jt += q[1];
+        a += q[2];
+        u += q[3];
+        hj += q[4];
       }
       u = fma(a, s.ctot, u);
       sw[k] = w;
