@@ -101,6 +101,61 @@ __device__ __forceinline__ double dprod(int j, int side, int a, int cnt,
   return d * others;
 }
 
+// Falloff rate coefficient and its derivatives (Lindemann, or Troe when
+// `troe`): kf = k_hi F Pr / (1 + Pr), Pr = m k_lo / k_hi, log10 F =
+// log10 Fcent / (1 + f^2), f = x / (n - 0.14 x), x = log10 Pr - 0.4 -
+// 0.67 log10 Fcent, n = 0.75 - 1.27 log10 Fcent (python.py's falloff
+// blending); returns kf, d ln kf / dT at fixed m (dxh, dxl: the exponent
+// derivatives of k_hi, k_lo) and d kf / dm.  Five divisions (reciprocals
+// reused) and the table logarithm read through L1.
+struct FalloffDeriv {
+  double kf, dlnkf, dkfdM;
+};
+
+__device__ __forceinline__ FalloffDeriv falloff_deriv(
+    bool troe, bool troe_t2, double a0, double a1, double a2, double a3,
+    double a4, double T, double invT, double m, double k_hi, double k_lo,
+    double dxh, double dxl) {
+  const double pr = m * k_lo / k_hi;
+  double blend = 1.0, dlnF_dT = 0.0, phi_x = 0.0;
+  if (troe) {
+    const double ln10 = 2.302585092994045684;
+    const double e3 = PEXP(T * a1);
+    const double e1 = PEXP(T * a3);
+    double fsum = a0 * e3 + a2 * e1;
+    double dfsum = a0 * a1 * e3 + a2 * a3 * e1;
+    if (troe_t2) {
+      const double e2 = PEXP(a4 * invT);
+      fsum += e2;
+      dfsum -= a4 * invT * invT * e2;
+    }
+    const double L = pyro_log10_g(fsum);
+    const double dL = dfsum / (fsum * ln10);
+    double fac = -1.0 / 0.14, dfac = 0.0, fx = 0.0;
+    if (pr > 0.0) {
+      const double xx = pyro_log10_g(pr) + (-0.4 - 0.67 * L);
+      const double nn = 0.75 - 1.27 * L;
+      const double iden = 1.0 / (nn - 0.14 * xx);
+      fac = xx * iden;
+      fx = nn * iden * iden;
+      const double fn = -fac * iden;
+      const double dxx = (dxl - dxh) * (1.0 / ln10) - 0.67 * dL;
+      dfac = fx * dxx + fn * (-1.27 * dL);
+    }
+    const double iopf = 1.0 / (1.0 + fac * fac);
+    blend = PEXP10(L * iopf);
+    const double g2 = 2.0 * L * fac * iopf * iopf;
+    dlnF_dT = ln10 * (dL * iopf - g2 * dfac);
+    phi_x = -g2 * fx;
+  }
+  const double i1pr = 1.0 / (1.0 + pr);
+  FalloffDeriv o;
+  o.kf = k_hi * (blend * pr * i1pr);
+  o.dlnkf = dxh + dlnF_dT + (dxl - dxh) * i1pr;
+  o.dkfdM = blend * k_lo * i1pr * (phi_x + i1pr);
+  return o;
+}
+
 // Net rate, its temperature and third-body derivatives, and the rate
 // coefficients of reaction j.  h: column of h/RT.
 template <class CT>
@@ -131,42 +186,13 @@ __device__ __forceinline__ RxnDeriv reaction_deriv(int j,
                                   k_fo_low[sl][2], T, lnT, invT, xl);
     const double dxh = darr_dT(form, k_rx_rate[j][1], k_rx_rate[j][2], invT);
     const double dxl = darr_dT(lform, k_fo_low[sl][1], k_fo_low[sl][2], invT);
-    const double pr = m * k_lo / k_hi;
-    double blend = 1.0, dlnF_dT = 0.0, phi_x = 0.0;
-    if (f & RX_TROE) {
-      const double ln10 = 2.302585092994045684;
-      const double e3 = PEXP(T * k_fo_troe[sl][1]);
-      const double e1 = PEXP(T * k_fo_troe[sl][3]);
-      double fsum = k_fo_troe[sl][0] * e3 + k_fo_troe[sl][2] * e1;
-      double dfsum = k_fo_troe[sl][0] * k_fo_troe[sl][1] * e3 +
-                     k_fo_troe[sl][2] * k_fo_troe[sl][3] * e1;
-      if (f & RX_TROE_T2) {
-        const double e2 = PEXP(k_fo_troe[sl][4] * invT);
-        fsum += e2;
-        dfsum -= k_fo_troe[sl][4] * invT * invT * e2;
-      }
-      const double L = log10(fsum);
-      const double dL = dfsum / (fsum * ln10);
-      double fac = -1.0 / 0.14, dfac = 0.0, fx = 0.0;
-      if (pr > 0.0) {
-        const double xx = log10(pr) + (-0.4 - 0.67 * L);
-        const double nn = 0.75 - 1.27 * L;
-        const double den = nn - 0.14 * xx;
-        fac = xx / den;
-        fx = nn / (den * den);
-        const double fn = -xx / (den * den);
-        const double dxx = (dxl - dxh) / ln10 - 0.67 * dL;
-        dfac = fx * dxx + fn * (-1.27 * dL);
-      }
-      const double opf = 1.0 + fac * fac;
-      blend = PEXP10(L / opf);
-      const double dphi = dL / opf - 2.0 * L * fac / (opf * opf) * dfac;
-      dlnF_dT = ln10 * dphi;
-      phi_x = -2.0 * L * fac * fx / (opf * opf);
-    }
-    out.kf = k_hi * (blend * pr / (1.0 + pr));
-    dlnkf = dxh + dlnF_dT + (dxl - dxh) / (1.0 + pr);
-    dkfdM = blend * k_lo / (1.0 + pr) * (phi_x + 1.0 / (1.0 + pr));
+    const FalloffDeriv fd = falloff_deriv(
+        (f & RX_TROE) != 0, (f & RX_TROE_T2) != 0, k_fo_troe[sl][0],
+        k_fo_troe[sl][1], k_fo_troe[sl][2], k_fo_troe[sl][3],
+        k_fo_troe[sl][4], T, invT, m, k_hi, k_lo, dxh, dxl);
+    out.kf = fd.kf;
+    dlnkf = fd.dlnkf;
+    dkfdM = fd.dkfdM;
   } else {
     ek = arrhenius(form, k_rx_rate[j][0], k_rx_rate[j][1], k_rx_rate[j][2], T,
                    lnT, invT, x);
@@ -305,44 +331,14 @@ __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
     const double k_lo = arrhenius(lform, l0, l1, l2, T, lnT, invT, xl);
     const double dxh = darr_dT(form, p1, p2, invT);
     const double dxl = darr_dT(lform, l1, l2, invT);
-    const double pr = m * k_lo / k_hi;
-    double blend = 1.0, dlnF_dT = 0.0, phi_x = 0.0;
-    if (f & RX_TROE) {
-      const double ln10 = 2.302585092994045684;
-      const double t0 = __ldg(&jf_troe[0][sl]), t1 = __ldg(&jf_troe[1][sl]);
-      const double t2 = __ldg(&jf_troe[2][sl]), t3 = __ldg(&jf_troe[3][sl]);
-      const double e3 = PEXP(T * t1);
-      const double e1 = PEXP(T * t3);
-      double fsum = t0 * e3 + t2 * e1;
-      double dfsum = t0 * t1 * e3 + t2 * t3 * e1;
-      if (f & RX_TROE_T2) {
-        const double t4 = __ldg(&jf_troe[4][sl]);
-        const double e2 = PEXP(t4 * invT);
-        fsum += e2;
-        dfsum -= t4 * invT * invT * e2;
-      }
-      const double L = log10(fsum);
-      const double dL = dfsum / (fsum * ln10);
-      double fac = -1.0 / 0.14, dfac = 0.0, fx = 0.0;
-      if (pr > 0.0) {
-        const double xx = log10(pr) + (-0.4 - 0.67 * L);
-        const double nn = 0.75 - 1.27 * L;
-        const double den = nn - 0.14 * xx;
-        fac = xx / den;
-        fx = nn / (den * den);
-        const double fn = -xx / (den * den);
-        const double dxx = (dxl - dxh) / ln10 - 0.67 * dL;
-        dfac = fx * dxx + fn * (-1.27 * dL);
-      }
-      const double opf = 1.0 + fac * fac;
-      blend = PEXP10(L / opf);
-      const double dphi = dL / opf - 2.0 * L * fac / (opf * opf) * dfac;
-      dlnF_dT = ln10 * dphi;
-      phi_x = -2.0 * L * fac * fx / (opf * opf);
-    }
-    kf = k_hi * (blend * pr / (1.0 + pr));
-    dlnkf = dxh + dlnF_dT + (dxl - dxh) / (1.0 + pr);
-    dkfdM = blend * k_lo / (1.0 + pr) * (phi_x + 1.0 / (1.0 + pr));
+    const bool troe = (f & RX_TROE) != 0, troe_t2 = (f & RX_TROE_T2) != 0;
+    const FalloffDeriv fd = falloff_deriv(
+        troe, troe_t2, __ldg(&jf_troe[0][sl]), __ldg(&jf_troe[1][sl]),
+        __ldg(&jf_troe[2][sl]), __ldg(&jf_troe[3][sl]),
+        __ldg(&jf_troe[4][sl]), T, invT, m, k_hi, k_lo, dxh, dxl);
+    kf = fd.kf;
+    dlnkf = fd.dlnkf;
+    dkfdM = fd.dkfdM;
   } else {
     const double ek = arrhenius(form, p0, p1, p2, T, lnT, invT, x);
     exp_form = form == FORM_EXP;

@@ -88,7 +88,10 @@ __shared__ double pyro_log_smem[3 * (PYRO_LOG_N + 1)];
 #define PYRO_TABLES_SMEM \
   ((PYRO_EXP_N + 3 * (PYRO_LOG_N + 1)) * sizeof(double))
 
-__device__ __forceinline__ double pyro_log(double x) {
+// kGlobal: read the table from global memory through L1 (kernels whose
+// shared memory is spoken for) instead of the staged copy
+template <bool kGlobal>
+__device__ __forceinline__ double pyro_log_t(double x) {
   const int hx = __double2hiint(x);
   if (hx < 0x00100000 || hx >= 0x7ff00000) return log(x);
   const int mant = hx & 0x000fffff;
@@ -97,8 +100,19 @@ __device__ __forceinline__ double pyro_log(double x) {
   const int j = (mant + (1 << 12)) >> 13;  // nearest j/128, 0..128
   const double F = (double)(PYRO_LOG_N + j) * (1.0 / PYRO_LOG_N);
   const double f = y - F;
-  const double* t = pyro_log_smem + 3 * j;
-  const double u = f * t[0];
+  double t0, t1, t2;
+  if (kGlobal) {
+    const double* t = pyro_log_table + 3 * j;
+    t0 = __ldg(t);
+    t1 = __ldg(t + 1);
+    t2 = __ldg(t + 2);
+  } else {
+    const double* t = pyro_log_smem + 3 * j;
+    t0 = t[0];
+    t1 = t[1];
+    t2 = t[2];
+  }
+  const double u = f * t0;
   // ln(1 + u) = u + u^2 (-1/2 + u (1/3 + u (-1/4 + u (1/5 + u (-1/6 +
   // u / 7)))))
   const double lp = fma(u * u, fma(u, fma(u, fma(u, fma(u, fma(u, 1.0 / 7.0,
@@ -109,9 +123,18 @@ __device__ __forceinline__ double pyro_log(double x) {
                                    -0.5),
                         u);
   const double md = (double)m;
-  const double hi = fma(md, PYRO_LOG_LN2_HI, t[1]);
-  const double lo = fma(md, PYRO_LOG_LN2_LO, t[2]) + lp;
+  const double hi = fma(md, PYRO_LOG_LN2_HI, t1);
+  const double lo = fma(md, PYRO_LOG_LN2_LO, t2) + lp;
   return hi + lo;
+}
+
+__device__ __forceinline__ double pyro_log(double x) {
+  return pyro_log_t<false>(x);
+}
+
+// log10 with the table read from global memory (no staging)
+__device__ __forceinline__ double pyro_log10_g(double x) {
+  return pyro_log_t<true>(x) * PYRO_LOG_INV_LN10;
 }
 
 __device__ __forceinline__ double pyro_log10(double x) {
