@@ -350,11 +350,18 @@ class _Emitter:
                 groups[-1].append(e)
             else:
                 groups.append([e])
-        # threads per state: two warps where the per-state shared memory
-        # would hold an SM to fewer than 24 warps (so twice the warps fit
-        # beside the same shared memory), else one
+        # threads per state: 8 or 16 lanes for small mechanisms (its species
+        # and reactions keep few lanes busy, so a warp serves 4 or 2
+        # states), two warps where the per-state shared memory would hold
+        # an SM to fewer than 24 warps (so twice the warps fit beside the
+        # same shared memory), else one
         jw_doubles = 9 * S + 4 * R + nslot + R + 1
-        jgroup = 64 if 8 * jw_doubles > 8192 else 32
+        if S <= 12 and R <= 64:
+            jgroup = 8
+        elif S <= 24 and R <= 128:
+            jgroup = 16
+        else:
+            jgroup = 64 if 8 * jw_doubles > 8192 else 32
         # contiguous split of the groups into jgroup runs of nearly equal
         # length, one per thread of the state's group
         lanes: List[List[Tuple[int, int, float]]] = [[] for _ in
@@ -399,16 +406,18 @@ class _Emitter:
         nwarp = jgroup // 32
         warp_blocks: List[List[List[int]]] = [[] for _ in range(nwarp)]
         load = [0.0] * nwarp
-        for kind, qs in sorted(blocks, key=lambda b: -cat_cost[b[0]]):
+        for kind, qs in (sorted(blocks, key=lambda b: -cat_cost[b[0]])
+                         if nwarp else []):
             wi = min(range(nwarp), key=lambda i: (load[i], i))
             warp_blocks[wi].append(qs)
             load[wi] += cat_cost[kind]
-        q_rounds = max(len(x) for x in warp_blocks)
+        q_rounds = max(len(x) for x in warp_blocks) if nwarp else 0
         lane_rx = []
-        if R <= jgroup:
-            q_rounds = 1
-            lane_rx = list(range(R)) + [-1] * (jgroup - R)
-        for rd in range(q_rounds if R > jgroup else 0):
+        if R <= jgroup or nwarp == 0:
+            # one round, or sub-warp groups: consecutive reactions
+            q_rounds = -(-R // jgroup)
+            lane_rx = list(range(R)) + [-1] * (q_rounds * jgroup - R)
+        for rd in range(q_rounds if (R > jgroup and nwarp) else 0):
             for wi in range(nwarp):
                 qs = warp_blocks[wi][rd] if rd < len(warp_blocks[wi]) else []
                 lane_rx.extend(qs[ln] if ln < len(qs) else -1

@@ -417,15 +417,18 @@ __device__ __forceinline__ void jac_reaction(int qq, const StateScalars& s,
 
 }  // namespace pyro
 
-// A state is handled by a group of JGROUP threads (one warp, or two for
-// large mechanisms: the per-state shared memory then holds an SM to half
-// the states but still 16 warps, which the FP64 pipe needs to stay busy).
-// Group-wide sums reduce within each warp, then across the group's warps
+// A state is handled by a group of JGROUP threads: 8 or 16 lanes of a warp
+// for small mechanisms (a warp then serves 4 or 2 states, so its species
+// and reaction rounds keep most lanes busy), one warp, or two for large
+// mechanisms (the per-state shared memory then holds an SM to half the
+// states but still 16 warps, which the FP64 pipe needs to stay busy).
+// Group-wide sums reduce within the group's lanes (xor shuffles inside the
+// aligned group) or, for two warps, within each warp and then across them
 // through shared memory in a fixed order, behind a named barrier.
 namespace pyro {
 
 __device__ __forceinline__ void group_sync(int gid) {
-#if JGROUP == 32
+#if JGROUP <= 32
   (void)gid;
   __syncwarp();
 #else
@@ -435,13 +438,23 @@ __device__ __forceinline__ void group_sync(int gid) {
 
 __device__ __forceinline__ double group_sum(double v, int gid, int t,
                                             double* red) {
+#if JGROUP < 32
+  (void)gid;
+  (void)t;
+  (void)red;
+#pragma unroll
+  for (int o = JGROUP / 2; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+#else
   v = warp_sum(v);
+#endif
 #if JGROUP == 32
   (void)gid;
   (void)t;
   (void)red;
   return v;
-#else
+#elif JGROUP > 32
   if ((t & 31) == 0) red[t >> 5] = v;
   group_sync(gid);
   double r = red[0];
@@ -469,7 +482,7 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
   extern __shared__ double smem[];
   PEXP_PRELOAD();
   const int t = threadIdx.x % JGROUP, gid = threadIdx.x / JGROUP;
-  __shared__ double s_red[JGROUPS][JGROUP / 32];
+  __shared__ double s_red[JGROUPS][JGROUP >= 32 ? JGROUP / 32 : 1];
   double* red = s_red[gid];
   double* sc = smem + (size_t)gid * JW_DOUBLES;
   double* sh = sc + NS;
@@ -489,8 +502,14 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
   const LC c{sc}, g{sg}, h{sh};
   constexpr int NC = NS + 1;
   if (t == 0) D[JD_ZERO] = 0.0;
-  for (int64_t i = (int64_t)blockIdx.x * JGROUPS + gid; i < n;
-       i += (int64_t)gridDim.x * JGROUPS) {
+  // the groups of one warp (sub-warp groups) step through states together,
+  // so every lane reaches the warp-wide shuffles; a group past the last
+  // state works on a copy of it and stores nothing
+  constexpr int GPW = JGROUP < 32 ? 32 / JGROUP : 1;
+  for (int64_t i0 = (int64_t)blockIdx.x * JGROUPS + gid - gid % GPW; i0 < n;
+       i0 += (int64_t)gridDim.x * JGROUPS) {
+    const bool live = i0 + gid % GPW < n;
+    const int64_t i = live ? i0 + gid % GPW : n - 1;
     double* Ji = J + i * ldj;
     const double T = pyro_ld(Tp, t_inc, i);
     const double P = pyro_ld(Pp, p_inc, i);
@@ -647,8 +666,8 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
     if (F != nullptr) {
       // dT/dt = -Q / (rho cp), dY_k/dt = W_k w_k / rho (the thread that
       // formed w_k stores it)
-      if (t == 0) F[i] = -Q * inv_rcp;
-      for (int k = t; k < NS; k += JGROUP)
+      if (live && t == 0) F[i] = -Q * inv_rcp;
+      for (int k = t; live && k < NS; k += JGROUP)
         F[(int64_t)(k + 1) * ldf + i] = __ldg(jg_mw + k) * sw[k] / rho;
     }
     pyro::group_sync(gid);
@@ -659,7 +678,7 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
     // update list) and stored once, transformed, with no read-back.
     for (int it = 0; it < JZ_ITERS; ++it) {
       const int off = __ldg(jz_off + it * JGROUP + t);
-      if (off != 0xFFFF) {
+      if (live && off != 0xFFFF) {
         const int k = off / NC - 1, m = off - (k + 1) * NC - 1;
         Ji[off] = __ldg(jg_invmw + m) * sg[k];
       }
@@ -673,7 +692,7 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
         const double cf = __ldg(ju_coef + e);
         const double dv = D[__ldg(ju_src + e)];
         if (off != cur) {
-          if (cur >= 0 && cur != 0xFFFF) {
+          if (live && cur >= 0 && cur != 0xFFFF) {
             const int k = cur / NC - 1, m = cur - (k + 1) * NC - 1;
             Ji[cur] = __ldg(jg_invmw + m) * fma(__ldg(jg_mw + k), acc, sg[k]);
           }
@@ -682,7 +701,7 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
         }
         acc = fma(cf, dv, acc);
       }
-      if (cur >= 0 && cur != 0xFFFF) {
+      if (live && cur >= 0 && cur != 0xFFFF) {
         const int k = cur / NC - 1, m = cur - (k + 1) * NC - 1;
         Ji[cur] = __ldg(jg_invmw + m) * fma(__ldg(jg_mw + k), acc, sg[k]);
       }
@@ -700,10 +719,11 @@ __global__ void __launch_bounds__(JGROUPS * JGROUP)
             -rcp * inv_sig * iw + rho * GAS_CONSTANT * scp[jj] * iw;
         v = -dQdY * inv_rcp + qr2 * drcp;
       }
-      Ji[col] = v;
+      if (live) Ji[col] = v;
     }
     // column 0 of rows 1..S
-    for (int k = t; k < NS; k += JGROUP) Ji[(int64_t)(k + 1) * NC] = sjt[k];
+    for (int k = t; live && k < NS; k += JGROUP)
+      Ji[(int64_t)(k + 1) * NC] = sjt[k];
     pyro::group_sync(gid);
   }
 }
