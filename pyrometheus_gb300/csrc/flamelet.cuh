@@ -55,7 +55,9 @@ __global__ void __launch_bounds__(128)
   const int lane = threadIdx.x & 31;
   constexpr int NB = FNV * FNV;
   __shared__ double s_hm[4][NS];  // species enthalpies per unit mass
+  __shared__ double s_c0[4][NS];  // J[1+k][0] / cp of the row
   double* hm_w = s_hm[threadIdx.x >> 5];
+  double* c0_w = s_c0[threadIdx.x >> 5];
   for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
        r < rows; r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
     const int s = sys_of_row[r];
@@ -90,15 +92,16 @@ __global__ void __launch_bounds__(128)
     const double inv_cp = 1.0 / cp;
     __syncwarp();
     if (interior) {
-      // species rows: column 0 <- J[1+k][0] / cp, columns m <- J - J[.][0] h_m / cp
-      for (int k = 0; k < NS; ++k) {
-        double* row = Cr + (int64_t)(k + 1) * FNV;
-        const double jt = row[0];
-        __syncwarp();
-        for (int m = lane; m < NS; m += 32)
-          row[m + 1] = fma(-jt * inv_cp, hm_w[m], row[m + 1]);
-        if (lane == 0) row[0] = jt * inv_cp;
-        __syncwarp();
+      // species rows: column 0 <- J[1+k][0] / cp, columns m <- J - J[.][0]
+      // h_m / cp; the lanes over the block's elements (coalesced), each
+      // row's column 0 staged first
+      for (int k = lane; k < NS; k += 32)
+        c0_w[k] = Cr[(int64_t)(k + 1) * FNV] * inv_cp;
+      __syncwarp();
+      for (int e = FNV + lane; e < NB; e += 32) {
+        const int a = e / FNV, b = e - a * FNV;
+        const double c0 = c0_w[a - 1];
+        Cr[e] = b == 0 ? c0 : fma(-c0, hm_w[b - 1], Cr[e]);
       }
       // enthalpy row
       for (int m = lane; m < FNV; m += 32) {
