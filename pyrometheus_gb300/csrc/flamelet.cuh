@@ -35,13 +35,22 @@
 
 #define FNV (NS + 1)
 
-// one warp per row: transform the reactor Jacobian held in C in place and
-// write L and U.  ADJ: the adjoint operator of the EOS-consistency solves
-// instead (FlameletEquations.adjoint_operator, equations.py:451-516):
-// interior C_i = Lap_c I + (2 / chi_i) (dS/dphi_i)^T, boundary C_i =
-// chi_i / 2 dx^-2 I, and L, U the Laplacian's own (unscaled) couplings.
+// Transform the reactor Jacobian held in C in place and write L and U.
+// ADJ: the adjoint operator of the EOS-consistency solves instead
+// (FlameletEquations.adjoint_operator, equations.py:451-516): interior
+// C_i = Lap_c I + (2 / chi_i) (dS/dphi_i)^T, boundary C_i = chi_i / 2
+// dx^-2 I, and L, U the Laplacian's own (unscaled) couplings.
+//
+// A CTA takes tiles of kFbRows rows.  The per-row scalars (T, sigma, cp,
+// rho, the species enthalpies per unit mass, the Laplacian couplings) are
+// formed one thread per row, so every lane of those FP64 instructions
+// works (GB300's FP64 pipe retires a warp instruction per 64 cycles per
+// partition whatever its active lanes); then each warp takes rows of the
+// tile with its lanes over the block's elements (coalesced).
+constexpr int kFbRows = 128;
+
 template <bool ADJ>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(kFbRows)
     k_flamelet_blocks(const double* __restrict__ Pp, int64_t p_inc,
                       const double* __restrict__ Tt,
                       const double* __restrict__ Y, int64_t ldy,
@@ -52,103 +61,115 @@ __global__ void __launch_bounds__(128)
                       const double* __restrict__ inv_dx2,
                       double* __restrict__ L, double* __restrict__ C,
                       double* __restrict__ U, int64_t rows) {
-  const int lane = threadIdx.x & 31;
   constexpr int NB = FNV * FNV;
-  __shared__ double s_hm[4][NS];  // species enthalpies per unit mass
-  __shared__ double s_c0[4][NS];  // J[1+k][0] / cp of the row
-  double* hm_w = s_hm[threadIdx.x >> 5];
-  double* c0_w = s_c0[threadIdx.x >> 5];
-  for (int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-       r < rows; r += ((int64_t)gridDim.x * blockDim.x) >> 5) {
-    const int s = sys_of_row[r];
-    const int64_t r0 = row_off[s], r1 = row_off[s + 1];
-    const bool first = r == r0, last = r == r1 - 1;
-    const bool interior = !first && !last;
-    const double idx2 = inv_dx2[s];
-    const double T = Tt[r];
-    const double invT = 1.0 / T;
-    double* Cr = C + r * NB;
-    // cp (mass), sigma and the species enthalpies per unit mass
-    double sig = 0.0, cpp = 0.0;
-    for (int k = lane; k < NS; k += 32) {
-      const double wk = __ldg(Y + (int64_t)k * ldy + r) * k_inv_mw[k];
-      const pyro::Nasa a(k, T > k_tmid[k]);
-      const double cpk =
-          fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
-      const double hrt =
-          fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
-                            a[2] * (1.0 / 3.0)),
-                    a[1] * 0.5),
-              a[0]) +
-          a[5] * invT;
-      hm_w[k] = GAS_CONSTANT * T * hrt * k_inv_mw[k];
-      sig += wk;
-      cpp = fma(wk, cpk, cpp);
+  // per row of the tile: species enthalpies per unit mass, and the scalars
+  // 1/cp, v/rho, 1/T, 1/sigma, the C diagonal term, the L and U diagonals,
+  // 2/chi; the interior flag
+  __shared__ double s_hm[NS][kFbRows];
+  __shared__ double s_sc[8][kFbRows];
+  __shared__ int s_in[kFbRows];
+  __shared__ double s_c0[kFbRows / 32][NS];  // J[1+k][0] / cp of a row
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  double* c0_w = s_c0[wid];
+  for (int64_t base = (int64_t)blockIdx.x * kFbRows; base < rows;
+       base += (int64_t)gridDim.x * kFbRows) {
+    const int q = threadIdx.x;
+    const int64_t r = base + q;
+    if (r < rows) {
+      const int s = sys_of_row[r];
+      const int64_t r0 = row_off[s], r1 = row_off[s + 1];
+      const bool first = r == r0, last = r == r1 - 1;
+      const bool interior = !first && !last;
+      const double idx2 = inv_dx2[s];
+      const double T = Tt[r];
+      const double invT = 1.0 / T;
+      double sig = 0.0, cpp = 0.0;
+      for (int k = 0; k < NS; ++k) {
+        const double wk = __ldg(Y + (int64_t)k * ldy + r) * k_inv_mw[k];
+        const pyro::Nasa a(k, T > k_tmid[k]);
+        const double cpk =
+            fma(T, fma(T, fma(T, fma(T, a[4], a[3]), a[2]), a[1]), a[0]);
+        const double hrt =
+            fma(T, fma(T, fma(T, fma(T, a[4] * 0.2, a[3] * 0.25),
+                              a[2] * (1.0 / 3.0)),
+                      a[1] * 0.5),
+                a[0]) +
+            a[5] * invT;
+        s_hm[k][q] = GAS_CONSTANT * T * hrt * k_inv_mw[k];
+        sig += wk;
+        cpp = fma(wk, cpk, cpp);
+      }
+      const double cp = GAS_CONSTANT * cpp;
+      const double rho = pyro_ld(Pp, p_inc, r) / (GAS_CONSTANT * T * sig);
+      const double lap_c = interior ? -2.0 * idx2 : idx2;
+      const bool next_interior = !last && (r + 1 < r1 - 1);
+      s_sc[0][q] = 1.0 / cp;
+      s_sc[1][q] = visc[r] / rho;
+      s_sc[2][q] = invT;
+      s_sc[3][q] = 1.0 / sig;
+      s_sc[4][q] = (ADJ && interior) ? lap_c : 0.5 * chi[r] * lap_c;
+      s_sc[5][q] =
+          next_interior ? (ADJ ? idx2 : 0.5 * chi[r + 1] * idx2) : 0.0;
+      s_sc[6][q] = interior ? (ADJ ? idx2 : 0.5 * chi[r] * idx2) : 0.0;
+      s_sc[7][q] = ADJ ? 2.0 / chi[r] : 0.0;
+      s_in[q] = interior ? 1 : 0;
     }
-    const double sigma = pyro::warp_sum(sig);
-    const double cp = GAS_CONSTANT * pyro::warp_sum(cpp);
-    const double rho = pyro_ld(Pp, p_inc, r) / (GAS_CONSTANT * T * sigma);
-    const double vr = visc[r] / rho;
-    const double inv_cp = 1.0 / cp;
-    __syncwarp();
-    if (interior) {
-      // species rows: column 0 <- J[1+k][0] / cp, columns m <- J - J[.][0]
-      // h_m / cp; the lanes over the block's elements (coalesced), each
-      // row's column 0 staged first
-      for (int k = lane; k < NS; k += 32)
-        c0_w[k] = Cr[(int64_t)(k + 1) * FNV] * inv_cp;
-      __syncwarp();
-      for (int e = FNV + lane; e < NB; e += 32) {
-        const int a = e / FNV, b = e - a * FNV;
-        const double c0 = c0_w[a - 1];
-        Cr[e] = b == 0 ? c0 : fma(-c0, hm_w[b - 1], Cr[e]);
-      }
-      // enthalpy row
-      for (int m = lane; m < FNV; m += 32) {
-        double v;
-        if (m == 0) {
-          v = vr * invT * inv_cp;
-        } else {
-          v = vr * (k_inv_mw[m - 1] / sigma - hm_w[m - 1] * inv_cp * invT);
-        }
-        Cr[m] = v;
-      }
-      if (ADJ) {
-        // (2 / chi) dS/dphi, transposed in place (each off-diagonal pair
-        // swapped by one lane)
+    __syncthreads();
+    for (int q = wid; q < kFbRows && base + q < rows; q += kFbRows / 32) {
+      const int64_t rr = base + q;
+      double* Cr = C + rr * NB;
+      const double inv_cp = s_sc[0][q];
+      if (s_in[q]) {
+        // species rows: column 0 <- J[1+k][0] / cp, columns m <- J -
+        // J[.][0] h_m / cp (each row's column 0 staged first)
+        for (int k = lane; k < NS; k += 32)
+          c0_w[k] = Cr[(int64_t)(k + 1) * FNV] * inv_cp;
         __syncwarp();
-        const double sc = 2.0 / chi[r];
-        for (int e = lane; e < NB; e += 32) {
+        for (int e = FNV + lane; e < NB; e += 32) {
           const int a = e / FNV, b = e - a * FNV;
-          if (a < b) {
-            const double x = Cr[e], y = Cr[b * FNV + a];
-            Cr[e] = sc * y;
-            Cr[b * FNV + a] = sc * x;
-          } else if (a == b) {
-            Cr[e] *= sc;
+          const double c0 = c0_w[a - 1];
+          Cr[e] = b == 0 ? c0 : fma(-c0, s_hm[b - 1][q], Cr[e]);
+        }
+        // enthalpy row
+        const double vr = s_sc[1][q], invT = s_sc[2][q];
+        for (int m = lane; m < FNV; m += 32) {
+          Cr[m] = m == 0 ? vr * invT * inv_cp
+                         : vr * (k_inv_mw[m - 1] * s_sc[3][q] -
+                                 s_hm[m - 1][q] * inv_cp * invT);
+        }
+        if (ADJ) {
+          // (2 / chi) dS/dphi, transposed in place (each off-diagonal pair
+          // swapped by one lane)
+          __syncwarp();
+          const double sc = s_sc[7][q];
+          for (int e = lane; e < NB; e += 32) {
+            const int a = e / FNV, b = e - a * FNV;
+            if (a < b) {
+              const double x = Cr[e], y = Cr[b * FNV + a];
+              Cr[e] = sc * y;
+              Cr[b * FNV + a] = sc * x;
+            } else if (a == b) {
+              Cr[e] *= sc;
+            }
           }
         }
+      } else {
+        for (int e = lane; e < NB; e += 32) Cr[e] = 0.0;
       }
-    } else {
-      for (int e = lane; e < NB; e += 32) Cr[e] = 0.0;
+      __syncwarp();
+      // Laplacian diagonal, and the couplings
+      const double dgl = s_sc[4][q], lo = s_sc[5][q], up = s_sc[6][q];
+      for (int d = lane; d < FNV; d += 32) Cr[(int64_t)d * FNV + d] += dgl;
+      double* Lr = L + rr * NB;
+      double* Ur = U + rr * NB;
+      for (int e = lane; e < NB; e += 32) {
+        const bool diag = (e % (FNV + 1)) == 0;
+        Lr[e] = diag ? lo : 0.0;
+        Ur[e] = diag ? up : 0.0;
+      }
+      __syncwarp();
     }
-    __syncwarp();
-    // Laplacian diagonal, and the couplings
-    const double lap_c = interior ? -2.0 * idx2 : idx2;
-    const double dgl = (ADJ && interior) ? lap_c : 0.5 * chi[r] * lap_c;
-    for (int d = lane; d < FNV; d += 32) Cr[(int64_t)d * FNV + d] += dgl;
-    const bool next_interior = !last && (r + 1 < r1 - 1);
-    const double lo =
-        next_interior ? (ADJ ? idx2 : 0.5 * chi[r + 1] * idx2) : 0.0;
-    const double up = interior ? (ADJ ? idx2 : 0.5 * chi[r] * idx2) : 0.0;
-    double* Lr = L + r * NB;
-    double* Ur = U + r * NB;
-    for (int e = lane; e < NB; e += 32) {
-      const bool diag = (e % (FNV + 1)) == 0;
-      Lr[e] = diag ? lo : 0.0;
-      Ur[e] = diag ? up : 0.0;
-    }
-    __syncwarp();
+    __syncthreads();  // before the next tile's scalars
   }
 }
 
@@ -263,10 +284,10 @@ PYRO_EXPORT int pyro_flamelet_blocks(const double* p, int64_t p_inc,
   if (!p || !T || !Y || !chi || !visc || !row_off || !sys_of_row ||
       !inv_dx2 || !L || !C || !U)
     return PYRO_ERR_ARGUMENT;
-  int64_t blocks = (rows * 32 + 127) / 128;
-  const int64_t cap = (int64_t)pyro_sm_count() * 32;
+  int64_t blocks = (rows + kFbRows - 1) / kFbRows;
+  const int64_t cap = (int64_t)pyro_sm_count() * 16;
   if (blocks > cap) blocks = cap;
-  k_flamelet_blocks<false><<<(int)blocks, 128, 0, stream>>>(
+  k_flamelet_blocks<false><<<(int)blocks, kFbRows, 0, stream>>>(
       p, p_inc, T, Y, ldy, chi, visc, row_off, sys_of_row, inv_dx2, L, C, U,
       rows);
   PYRO_CHECK_LAUNCH();
@@ -283,10 +304,10 @@ PYRO_EXPORT int pyro_flamelet_adjoint_blocks(
   if (!p || !T || !Y || !chi || !visc || !row_off || !sys_of_row ||
       !inv_dx2 || !L || !C || !U)
     return PYRO_ERR_ARGUMENT;
-  int64_t blocks = (rows * 32 + 127) / 128;
-  const int64_t cap = (int64_t)pyro_sm_count() * 32;
+  int64_t blocks = (rows + kFbRows - 1) / kFbRows;
+  const int64_t cap = (int64_t)pyro_sm_count() * 16;
   if (blocks > cap) blocks = cap;
-  k_flamelet_blocks<true><<<(int)blocks, 128, 0, stream>>>(
+  k_flamelet_blocks<true><<<(int)blocks, kFbRows, 0, stream>>>(
       p, p_inc, T, Y, ldy, chi, visc, row_off, sys_of_row, inv_dx2, L, C, U,
       rows);
   PYRO_CHECK_LAUNCH();
