@@ -1179,11 +1179,15 @@ def run_gb300(args):
     torch.cuda.synchronize()
     barrier(dist)
     t0 = time.perf_counter()
+    e2e_marks = []
     for _ in range(e2e_steps):
-        e2e_step()
+        e2e_step()      # ends with the host read of the convergence flag
+        e2e_marks.append(time.perf_counter())
     torch.cuda.synchronize()
     barrier(dist)
     e2e_s = max_over_ranks(dist, time.perf_counter() - t0, dev)
+    e2e_step_ms = [round((b - a) * 1e3, 2) for a, b in
+                   zip([t0] + e2e_marks[:-1], e2e_marks)]
     e2e_value = n * world * e2e_steps / e2e_s
     h2d = (P_h.numel() + T_h.numel() + Y_h.numel() + E_h.numel()) * 8
     d2h = (W_h.numel() + To_h.numel()) * 8
@@ -1233,7 +1237,7 @@ def run_gb300(args):
         "gpu_launches": args.steps,
         "e2e": {"value": e2e_value, "unit": "states/s",
                 "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "steps": e2e_steps},
+                "steps": e2e_steps, "step_ms": e2e_step_ms},
         "roofline": {
             "bound": "fp64", "achieved": achieved / 1e12,
             "peak": dfma / 1e12, "unit": "TFLOP/s",

@@ -543,22 +543,30 @@ class CudaThermochemistryBase:
                 get_device_properties(dev).multi_processor_count
             chunk = max(1, round((1 << 18) / wave)) * wave
         m0 = int(min(chunk, n))
-        f64 = dict(dtype=torch.float64, device=dev)
-        bufs = []
-        for _ in range(2):
-            b = {"p": torch.empty(m0, **f64), "t": torch.empty(m0, **f64),
-                 "e": torch.empty(m0, **f64), "y": torch.empty((S, m0), **f64),
-                 "w": torch.empty((S, m0), **f64),
-                 "to": torch.empty(m0, **f64)}
-            for v in list(b.values()):
-                v.record_stream(h2d)
-                v.record_stream(d2h)
-            b["ready"] = torch.cuda.Event()
-            b["done"] = torch.cuda.Event()
-            b["free"] = torch.cuda.Event()
-            bufs.append(b)
+        # the two device chunks stay allocated between calls (keyed by the
+        # chunk size): a fresh allocation per call, held back by the copy
+        # streams until they drain, sent some calls through device
+        # allocations that stalled the pipeline; successive calls are
+        # ordered on the streams (each starts after the last one's copies)
+        bufs = self._stream_bufs.get(m0) if getattr(
+            self, "_stream_bufs", None) is not None else None
+        if bufs is None:
+            f64 = dict(dtype=torch.float64, device=dev)
+            bufs = []
+            for _ in range(2):
+                b = {"p": torch.empty(m0, **f64), "t": torch.empty(m0, **f64),
+                     "e": torch.empty(m0, **f64),
+                     "y": torch.empty((S, m0), **f64),
+                     "w": torch.empty((S, m0), **f64),
+                     "to": torch.empty(m0, **f64)}
+                b["ready"] = torch.cuda.Event()
+                b["done"] = torch.cuda.Event()
+                b["free"] = torch.cuda.Event()
+                bufs.append(b)
+            self._stream_bufs = {m0: bufs}
         self._fail.zero_()
         h2d.wait_stream(comp)
+        h2d.wait_stream(d2h)  # the previous call's reads of the chunks
         for c, s0 in enumerate(range(0, n, m0)):
             m = min(m0, n - s0)
             b = bufs[c % 2]

@@ -88,6 +88,35 @@ def test_fused_source_and_jacobian(name):
                           equal_nan=True)
 
 
+@pytest.mark.parametrize("name", ["synthetic9", "ref_sandiego", "ref_uiuc",
+                                  "ref_hong", "synthetic53"])
+def test_batch_tails_and_independence(name):
+    """Each state's Jacobian is its own group's work: batches of 1, 2, 3,
+    5, 7 and 13 states (a warp's last groups past the batch, at four
+    states per warp for the small mechanisms) give bit for bit the rows a
+    larger batch gives for the same states, and the source of the same
+    pass likewise."""
+    sol, g = load_golden(name)
+    th = _cls(sol)()
+    n = g["jac"].shape[0]
+    p, t, y = g["P"][:n], g["T"][:n], g["Y"][:, :n]
+    full = th.get_reactor_jacobian(p, t, y).cpu().numpy()
+    ffull, _ = th.get_reactor_source_and_jacobian(p, t, y)
+    ffull = ffull.cpu().numpy()
+    for m in (1, 2, 3, 5, 7, 13):
+        if m > n:
+            continue
+        for start in (0, n - m):
+            sl = slice(start, start + m)
+            jm = th.get_reactor_jacobian(p[sl], t[sl], y[:, sl])
+            jm = jm.cpu().numpy().reshape(m, *full.shape[1:])
+            assert np.array_equal(jm, full[sl], equal_nan=True), (m, start)
+            fm, _ = th.get_reactor_source_and_jacobian(p[sl], t[sl],
+                                                       y[:, sl])
+            fm = fm.cpu().numpy().reshape(ffull.shape[0], m)
+            assert np.array_equal(fm, ffull[:, sl], equal_nan=True)
+
+
 def test_jacobian_order_of_convergence_like_reference():
     """Central differences of the oracle source converge to the CUDA
     Jacobian at second order (test/test.py:360-374)."""
