@@ -10,6 +10,8 @@
     python profile_cases.py transport [states]
     python profile_cases.py serving [cells] [launches]
     python profile_cases.py flamelet_solve [copies]
+    python profile_cases.py flamelet_blocks [flamelets]
+    python profile_cases.py source_dp [states]
     python profile_cases.py peaks [repeats]
 
 Each case builds its inputs on the current CUDA device (inputs larger than
@@ -227,6 +229,48 @@ def flamelet_solve(copies: int = 256):
           f"{'/'.join(str(int(c)) for c in stages[:4])}")
 
 
+def flamelet_blocks(flamelets: int = 2048):
+    """``FlameletEquations.jac`` (the per-point reactor Jacobians, then
+    ``k_flamelet_blocks``) on *flamelets* seeded flamelets of 64..1024
+    points of the 9-species mechanism, three times."""
+    import torch
+
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
+    from pyrometheus_gb300.flamelet import FlameletEquations
+    dev = _dev()
+    sol = synthetic.config1_mechanism()
+    th = get_thermochem_class(sol)(device=dev)
+    lengths = np.random.default_rng(11).integers(64, 1025, size=flamelets)
+    prof = synthetic.flamelet_profiles(sol, lengths, seed=3)
+    eq = FlameletEquations(th, lengths, prof["dx"], prof["y_ox"],
+                           prof["y_fu"], device=dev)
+    T = torch.as_tensor(prof["T"], device=dev)
+    Y = torch.as_tensor(prof["Y"], device=dev)
+    chi = torch.as_tensor(prof["chi"], device=dev)
+    h = th.get_mixture_enthalpy_mass(T, Y)
+    for _ in range(3):
+        eq.jac(h, Y, chi, torch.zeros_like(chi), T, 101325.0, temperature=T)
+    torch.cuda.synchronize()
+
+
+def source_dp(states: int = 1 << 18):
+    """``get_reactor_source_dp`` on seeded states of the 53-species
+    mechanism, three times."""
+    import torch
+
+    from pyrometheus_gb300 import get_thermochem_class, synthetic
+    dev = _dev()
+    sol = synthetic.config2_mechanism()
+    th = get_thermochem_class(sol)(device=dev)
+    t, p, y = synthetic.sample_states(sol, states, seed=2)
+    T = torch.as_tensor(t, device=dev)
+    P = torch.as_tensor(p, device=dev)
+    Y = torch.as_tensor(y, device=dev)
+    for _ in range(3):
+        th.get_reactor_source_dp(P, T, Y)
+    torch.cuda.synchronize()
+
+
 def peaks(repeats: int = 5):
     """The FP64 rates the rooflines use, measured live: DFMA FLOP/s, CUDA's
     double exp and log per second, and the FP64 tensor-core rate of
@@ -274,6 +318,10 @@ def main(argv=None):
         serving(*rest)
     elif case == "flamelet_solve":
         flamelet_solve(*rest)
+    elif case == "flamelet_blocks":
+        flamelet_blocks(*rest)
+    elif case == "source_dp":
+        source_dp(*rest)
     elif case == "peaks":
         peaks(*rest)
     else:
