@@ -514,6 +514,13 @@ class _Emitter:
         # exp table, at most 512 threads
         jgroups = max(1, min(512 // jgroup,
                              (227 * 1024 - 16384) // (8 * jw_doubles)))
+        # sub-warp groups fill whole warps (their group sums shuffle across
+        # the full warp)
+        gpw = max(1, 32 // jgroup)
+        if jgroups < gpw:
+            raise NotImplementedError("mechanism too large for the "
+                                      "Jacobian kernel's sub-warp groups")
+        jgroups -= jgroups % gpw
 
         def arr(ctype, name, dims, vals):
             return _table(qual, ctype, name, dims, vals)

@@ -479,7 +479,7 @@ class CudaThermochemistryBase:
         chunks of *chunk* states (default: the whole waves of the hot kernel
         nearest 2^18 states): host-to-device copies, the kernel and
         device-to-host copies of successive chunks run on three streams
-        with double-buffered device chunks, so the transfers overlap the
+        with three device chunk buffers, so the transfers overlap the
         FP64 work.  Results land in *out*.
 
         :returns: ``(wdot[S, N], T_new[N])`` (the *out* tensors when given).
@@ -543,17 +543,19 @@ class CudaThermochemistryBase:
                 get_device_properties(dev).multi_processor_count
             chunk = max(1, round((1 << 18) / wave)) * wave
         m0 = int(min(chunk, n))
-        # the two device chunks stay allocated between calls (keyed by the
-        # chunk size): a fresh allocation per call, held back by the copy
-        # streams until they drain, sent some calls through device
-        # allocations that stalled the pipeline; successive calls are
-        # ordered on the streams (each starts after the last one's copies)
+        # three device chunks (the copies of one run ahead of the kernel on
+        # another, so a slow transfer does not stall the pipeline), kept
+        # allocated between calls (keyed by the chunk size): a fresh
+        # allocation per call, held back by the copy streams until they
+        # drain, sent some calls through device allocations that stalled
+        # the pipeline; successive calls are ordered on the streams (each
+        # starts after the last one's copies)
         bufs = self._stream_bufs.get(m0) if getattr(
             self, "_stream_bufs", None) is not None else None
         if bufs is None:
             f64 = dict(dtype=torch.float64, device=dev)
             bufs = []
-            for _ in range(2):
+            for _ in range(3):
                 b = {"p": torch.empty(m0, **f64), "t": torch.empty(m0, **f64),
                      "e": torch.empty(m0, **f64),
                      "y": torch.empty((S, m0), **f64),
@@ -569,8 +571,8 @@ class CudaThermochemistryBase:
         h2d.wait_stream(d2h)  # the previous call's reads of the chunks
         for c, s0 in enumerate(range(0, n, m0)):
             m = min(m0, n - s0)
-            b = bufs[c % 2]
-            if c >= 2:
+            b = bufs[c % len(bufs)]
+            if c >= len(bufs):
                 h2d.wait_event(b["free"])
             for key, src in (("p", p), ("t", t), ("e", e), ("y", y)):
                 native.copy_columns_async(b[key], src, 0, s0, m, h2d)

@@ -156,6 +156,26 @@ def test_scheduling_fences_are_opt_in():
                                    CudaGenerationOptions(fence_every=0))
 
 
+@pytest.mark.parametrize("n_reactions", [24, 56, 60, 64])
+def test_jacobian_groups_fill_whole_warps(n_reactions):
+    """The Jacobian kernel's state groups (8 lanes per state for small
+    mechanisms) fill whole warps of the CTA, whatever the shared memory per
+    state allows: 60 reactions on 9 species leave room for 45 states per
+    CTA, which the generator rounds down to 44 (a half-filled warp would
+    break the groups' warp-wide sums)."""
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.codegen.cuda import CudaCodeGenerator
+    sol = synthetic.make_mechanism(synthetic.SPECIES_9, n_reactions, 6, 4, 2,
+                                   seed=5, name="wide9",
+                                   orient_temperature=1500.0)
+    src = CudaCodeGenerator.generate("m", sol)
+    g = {k: int(re.search(rf"#define {k} (\d+)", src).group(1))
+         for k in ("JGROUP", "JGROUPS")}
+    assert g["JGROUP"] == 8
+    assert (g["JGROUP"] * g["JGROUPS"]) % 32 == 0
+    assert g["JGROUP"] * g["JGROUPS"] <= 512
+
+
 def test_cli_writes_source(tmp_path):
     from pyrometheus_gb300 import synthetic
     from pyrometheus_gb300.cli import main

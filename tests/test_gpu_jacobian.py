@@ -117,6 +117,33 @@ def test_batch_tails_and_independence(name):
             assert np.array_equal(fm, ffull[:, sl], equal_nan=True)
 
 
+def test_wide_small_mechanism():
+    """9 species with 60 reactions (8-lane state groups, 44 states per CTA
+    after rounding to whole warps): central differences of the oracle
+    source converge to the CUDA Jacobian at second order, and sub-batches
+    give the same rows bit for bit."""
+    from oracle.thermo_oracle import Thermochemistry as Oracle
+    from pyrometheus_gb300 import synthetic
+    sol = synthetic.make_mechanism(synthetic.SPECIES_9, 60, 6, 4, 2, seed=5,
+                                   name="wide9", orient_temperature=1500.0)
+    th = _cls(sol)()
+    orc = Oracle(sol)
+    t, p, y = synthetic.sample_states(sol, 45, seed=9)
+    full = th.get_reactor_jacobian(p, t, y).cpu().numpy()
+    for m in (1, 3, 13):
+        jm = th.get_reactor_jacobian(p[-m:], t[-m:], y[:, -m:])
+        jm = jm.cpu().numpy().reshape(m, *full.shape[1:])
+        assert np.array_equal(jm, full[-m:], equal_nan=True)
+    errs = []
+    deltas = [1e-3, 1e-4, 1e-5]
+    for rel in deltas:
+        jfd = orc.reactor_jacobian_fd(p[:2], t[:2], y[:, :2], rel=rel,
+                                      absolute_y=True)
+        errs.append(np.linalg.norm(full[:2] - jfd) / np.linalg.norm(full[:2]))
+    order = np.polyfit(np.log(deltas), np.log(errs), 1)[0]
+    assert order > 1.95, (errs, order)
+
+
 def test_jacobian_order_of_convergence_like_reference():
     """Central differences of the oracle source converge to the CUDA
     Jacobian at second order (test/test.py:360-374)."""
