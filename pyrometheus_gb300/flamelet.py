@@ -37,12 +37,16 @@ class BlockThomasSolver:
 
     ``kernel``: ``"cta"`` (one CTA per system, threads over matrix
     elements; any nv <= 64), ``"seg"`` (32 // nv systems per warp, one lane
-    per block row; nv <= 16) or ``"small"`` (one thread per system, nv <=
-    16); ``threads``: CTA size (``"cta"``: a multiple of 32; ``"small"``:
-    32 or 64 systems per CTA; ``"seg"``: fixed at 32); both ``None`` pick
-    from the autotuner cache or a size rule.  ``ctas``: persistent grid of the ``"cta"`` kernel (0:
-    all resident CTAs); ``use_graph``: capture the launch in a CUDA graph on
-    the first :meth:`solve` with given buffers and replay it afterwards.
+    per block row, each system eliminated from both ends to its middle
+    row; nv <= 16; re-solves through its own two-ended recurrence) or
+    ``"small"`` (one thread per system, nv <= 16); ``threads``: CTA size
+    (``"cta"``: a multiple of 32; ``"small"``: 32 or 64 systems per CTA;
+    ``"seg"``: recorded as 32, the kernel's CTAs are four warps); both
+    ``None`` pick from the autotuner cache or a size rule (``"seg"`` for
+    nv <= 16).  ``ctas``: persistent grid (0: the kernel's default; for
+    ``"seg"`` one or two warps per SM partition by the batch size);
+    ``use_graph``: capture the launch in a CUDA graph on the first
+    :meth:`solve` with given buffers and replay it afterwards.
     """
 
     def __init__(self, nv: int, lengths: Sequence[int], device=None,
