@@ -477,7 +477,7 @@ class CudaThermochemistryBase:
         ``temperature``, ``energy`` ([N]) and ``mass_fractions`` ([S, N]) and
         ``out = (wdot_host[S, N], T_host[N])``, the batch is streamed in
         chunks of *chunk* states (default: the whole waves of the hot kernel
-        nearest 2^18 states): host-to-device copies, the kernel and
+        nearest 2^17 states): host-to-device copies, the kernel and
         device-to-host copies of successive chunks run on three streams
         with three device chunk buffers, so the transfers overlap the
         FP64 work.  Results land in *out*.
@@ -541,7 +541,7 @@ class CudaThermochemistryBase:
         if chunk is None:
             wave = self._lib.pyro_hot_block_size() * torch.cuda.\
                 get_device_properties(dev).multi_processor_count
-            chunk = max(1, round((1 << 18) / wave)) * wave
+            chunk = max(1, round((1 << 17) / wave)) * wave
         m0 = int(min(chunk, n))
         # three device chunks (the copies of one run ahead of the kernel on
         # another, so a slow transfer does not stall the pipeline), kept
