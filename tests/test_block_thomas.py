@@ -159,6 +159,53 @@ def test_seg_segments_take_systems_in_turn(nv, ctas):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("nv", [5, 10])
+def test_seg_resolve_through_the_abi_with_a_padded_stride(nv):
+    """pyro_block_thomas_seg then pyro_block_thomas_seg_resolve through
+    the C ABI: four right-hand sides 7 doubles apart beyond their packed
+    size (the padding untouched), each against the oracle's solve."""
+    _cuda()
+    import ctypes
+
+    from pyrometheus_gb300 import native
+    lib = native.block_thomas_lib()
+    lengths, L, C, U, b = make_systems(70, nv, 1, 60, seed=60 + nv)
+    rows = int(lengths.sum())
+    dev = torch.device("cuda")
+    t = [torch.as_tensor(a, device=dev).contiguous() for a in (L, C, U, b)]
+    offs = torch.as_tensor(np.concatenate([[0], np.cumsum(lengths)]),
+                           dtype=torch.int64, device=dev)
+    order = torch.as_tensor(np.argsort(-lengths, kind="stable"),
+                            dtype=torch.int32, device=dev)
+    work = torch.empty(int(lib.pyro_block_thomas_work_doubles(nv, rows)),
+                       dtype=torch.float64, device=dev)
+    counter = torch.zeros(1, dtype=torch.int32, device=dev)
+    status = torch.zeros(1, dtype=torch.int32, device=dev)
+    x = torch.empty_like(t[3])
+    sp = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert lib.pyro_block_thomas_seg(
+        *[a.data_ptr() for a in t], x.data_ptr(), offs.data_ptr(),
+        order.data_ptr(), len(lengths), nv, work.data_ptr(),
+        counter.data_ptr(), status.data_ptr(), 0, sp) == 0
+    stride = rows * nv + 7
+    rng = np.random.default_rng(nv)
+    B = torch.as_tensor(rng.standard_normal(4 * stride), device=dev)
+    X = torch.full((4 * stride,), 7.5, dtype=torch.float64, device=dev)
+    assert lib.pyro_block_thomas_seg_resolve(
+        t[0].data_ptr(), t[2].data_ptr(), B.data_ptr(), X.data_ptr(), 4,
+        stride, offs.data_ptr(), order.data_ptr(), len(lengths), nv,
+        work.data_ptr(), counter.data_ptr(), status.data_ptr(), sp) == 0
+    torch.cuda.synchronize()
+    assert int(status.item()) == 0
+    Bh, Xh = B.cpu().numpy(), X.cpu().numpy()
+    for c in range(4):
+        bc = Bh[c * stride:c * stride + rows * nv].reshape(rows, nv)
+        xc = Xh[c * stride:c * stride + rows * nv].reshape(rows, nv)
+        assert _rel(xc, solve_packed(lengths, L, C, U, bc)) < 1e-10
+        assert np.all(Xh[c * stride + rows * nv:(c + 1) * stride] == 7.5)
+
+
+@pytest.mark.gpu
 def test_cuda_graph_replay_and_single_system_api():
     _cuda()
     from pyrometheus_gb300.flamelet import block_thomas as bt_gpu
