@@ -176,6 +176,55 @@ def test_jacobian_groups_fill_whole_warps(n_reactions):
     assert g["JGROUP"] * g["JGROUPS"] <= 512
 
 
+def _table(src, name):
+    m = re.search(rf"{name}\[[^\]]*\](?:\[[^\]]*\])? = \{{([^}}]*)\}}", src)
+    return [int(v, 0) for v in m.group(1).replace("\n", " ").split(",")
+            if v.strip()]
+
+
+@pytest.mark.parametrize("which", ["config1", "config2", "wide9"])
+def test_jacobian_lane_tables(which):
+    """The generated tables of the Jacobian kernel: every reaction runs on
+    exactly one (round, lane); with whole-warp groups each warp's block of
+    a round holds one kind of reaction; the per-species parts cover each
+    species' slot list exactly once, in order, the first part the owner,
+    the owners' lists naming the other parts' scratch slots."""
+    from pyrometheus_gb300 import synthetic
+    from pyrometheus_gb300.codegen.cuda import CudaCodeGenerator, _Model
+    sol = {"config1": synthetic.config1_mechanism,
+           "config2": synthetic.config2_mechanism,
+           "wide9": lambda: synthetic.make_mechanism(
+               synthetic.SPECIES_9, 60, 6, 4, 2, seed=5, name="wide9",
+               orient_temperature=1500.0)}[which]()
+    src = CudaCodeGenerator.generate("m", sol)
+    jg = int(re.search(r"#define JGROUP (\d+)", src).group(1))
+    nr = sol.n_reactions
+    lane_rx = _table(src, "jq_lane_rx")
+    assert sorted(q for q in lane_rx if q >= 0) == list(range(nr))
+    flags = _table(src, "jq_flags")
+    if jg >= 32:
+        for b0 in range(0, len(lane_rx), 32):
+            kinds = {flags[q] & 3 for q in lane_rx[b0:b0 + 32] if q >= 0}
+            assert len(kinds) <= 1
+    m = _Model(sol)
+    sp = _table(src, "jq_sp")
+    si0 = _table(src, "jg_si0")
+    si_slot = _table(src, "jg_si_slot")
+    p_sp, p_s0, p_s1 = (_table(src, n) for n in ("jp_sp", "jp_s0", "jp_s1"))
+    p_slot = _table(src, "jp_slot")
+    x0, xslot = _table(src, "jp_x0"), _table(src, "jp_xslot")
+    for k in range(m.S):
+        parts = [e for e, s_ in enumerate(p_sp) if s_ == k]
+        assert parts, k
+        cover = [a for e in parts for a in range(p_s0[e], p_s1[e])]
+        assert cover == list(range(si0[k], si0[k + 1]))
+        assert all(sp[si_slot[a]] == k for a in cover)
+        owners = [e for e in parts if p_slot[e] < 0]
+        assert len(owners) == 1 and owners[0] == parts[0]
+        assert sorted(xslot[x0[k]:x0[k + 1]]) == sorted(
+            p_slot[e] for e in parts[1:])
+
+
 def test_cli_writes_source(tmp_path):
     from pyrometheus_gb300 import synthetic
     from pyrometheus_gb300.cli import main
