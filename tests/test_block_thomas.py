@@ -34,6 +34,60 @@ def test_oracle_matches_reference_block_thomas(tag):
     assert _rel(solve_packed(lengths, L, C, U, b), x) < 1e-12
 
 
+def _two_ended(lengths, L, C, U, b):
+    """The segmented kernels' recurrences in numpy: per system, rows 0 ..
+    m-1 eliminated downwards (S_i = C'_i^-1 U_i), rows N-1 .. m+1 upwards
+    (S^_i = C^_i^-1 L_{i-1}), the middle row m = N // 2 solved with both
+    couplings, then x outwards from it."""
+    x = np.empty_like(b)
+    r0 = 0
+    for n in lengths:
+        n = int(n)
+        m = n >> 1
+        S, t = {}, {}
+        for i in range(m):
+            cp, bp = C[r0 + i].copy(), b[r0 + i].copy()
+            if i:
+                cp -= L[r0 + i - 1] @ S[i - 1]
+                bp -= L[r0 + i - 1] @ t[i - 1]
+            S[i], t[i] = (np.linalg.solve(cp, U[r0 + i]),
+                          np.linalg.solve(cp, bp))
+        for k in range(n - 1 - m):
+            i = n - 1 - k
+            cp, bp = C[r0 + i].copy(), b[r0 + i].copy()
+            if k:
+                cp -= U[r0 + i] @ S[i + 1]
+                bp -= U[r0 + i] @ t[i + 1]
+            S[i], t[i] = (np.linalg.solve(cp, L[r0 + i - 1]),
+                          np.linalg.solve(cp, bp))
+        cm, bm = C[r0 + m].copy(), b[r0 + m].copy()
+        if m >= 1:
+            cm -= L[r0 + m - 1] @ S[m - 1]
+            bm -= L[r0 + m - 1] @ t[m - 1]
+        if m + 1 <= n - 1:
+            cm -= U[r0 + m] @ S[m + 1]
+            bm -= U[r0 + m] @ t[m + 1]
+        x[r0 + m] = xp = np.linalg.solve(cm, bm)
+        for i in range(m - 1, -1, -1):
+            x[r0 + i] = xp = t[i] - S[i] @ xp
+        xp = x[r0 + m]
+        for i in range(m + 1, n):
+            x[r0 + i] = xp = t[i] - S[i] @ xp
+        r0 += n
+    return x
+
+
+@pytest.mark.parametrize("nv", [1, 3, 10])
+def test_two_ended_recurrence_equals_top_down(nv):
+    """The elimination order of the segmented kernels (from both ends to
+    the middle row) reaches the reference's top-down solution
+    (linear_solver.py:6-103) on uneven systems of 1 to 40 rows."""
+    lengths, L, C, U, b = make_systems(60, nv, 1, 40, seed=70 + nv)
+    assert (lengths <= 3).any()
+    ref = solve_packed(lengths, L, C, U, b)
+    assert _rel(_two_ended(lengths, L, C, U, b), ref) < 1e-13
+
+
 def test_oracle_against_dense_solve():
     lengths, L, C, U, b = make_systems(1, 6, 5, 5, seed=3)
     n = int(lengths[0])
