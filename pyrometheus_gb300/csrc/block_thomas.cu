@@ -1325,14 +1325,15 @@ int launch_seg(const double* L, const double* C, const double* U,
                const int* order, int nsys, double* work, int* counter,
                int* status, int ctas, cudaStream_t stream) {
   // forward grid: by default two warps per SM partition (one's shuffle,
-  // redux and reciprocal latencies under the other's FP64 work) when every
-  // segment gets two sweeps or more (8,192 sweeps of 32..512 rows at nv =
-  // 10: 15.3 ms against 19.2 ms with one warp, 17.0 ms with three), else
-  // one
+  // redux and reciprocal latencies under the other's FP64 work) when the
+  // sweeps come to three per lane segment of one warp per partition or
+  // more, else one (forward sweeps at nv = 10, sweeps of 32..512 rows,
+  // one / two warps: 2,048 sweeps 7.7 / 9.9 ms, 4,096 10.4 / 11.5 ms,
+  // 6,000 14.5 / 11.5 ms, 8,192 19.2 / 15.3 ms, three warps 17.0 ms)
   const int units = 2 * nsys;
   if (ctas <= 0) {
     const int segs_per_warp_slot = pyro_sm_count() * 4 * SegCfg<NV>::P;
-    const int w = units >= 2 * 2 * segs_per_warp_slot ? 2 : 1;
+    const int w = units >= 3 * segs_per_warp_slot ? 2 : 1;
     ctas = pyro_sm_count() * w * 4 / kSegWarps;
   }
   const int fwd = seg_grid<NV>((const void*)k_block_thomas_seg<NV>, units,
