@@ -182,7 +182,7 @@ def _table(src, name):
             if v.strip()]
 
 
-@pytest.mark.parametrize("which", ["config1", "config2", "wide9"])
+@pytest.mark.parametrize("which", ["config1", "config2", "wide9", "mid18"])
 def test_jacobian_lane_tables(which):
     """The generated tables of the Jacobian kernel: every reaction runs on
     exactly one (round, lane); with whole-warp groups each warp's block of
@@ -195,7 +195,10 @@ def test_jacobian_lane_tables(which):
            "config2": synthetic.config2_mechanism,
            "wide9": lambda: synthetic.make_mechanism(
                synthetic.SPECIES_9, 60, 6, 4, 2, seed=5, name="wide9",
-               orient_temperature=1500.0)}[which]()
+               orient_temperature=1500.0),
+           "mid18": lambda: synthetic.make_mechanism(
+               list(synthetic.SPECIES_53[:17]) + ["N2"], 40, 5, 3, 1,
+               seed=7, name="mid18", orient_temperature=1500.0)}[which]()
     src = CudaCodeGenerator.generate("m", sol)
     jg = int(re.search(r"#define JGROUP (\d+)", src).group(1))
     nr = sol.n_reactions

@@ -117,15 +117,24 @@ def test_batch_tails_and_independence(name):
             assert np.array_equal(fm, ffull[:, sl], equal_nan=True)
 
 
-def test_wide_small_mechanism():
-    """9 species with 60 reactions (8-lane state groups, 44 states per CTA
-    after rounding to whole warps): central differences of the oracle
+@pytest.mark.parametrize("which", ["wide9", "mid18"])
+def test_small_and_mid_size_mechanisms(which):
+    """Mechanisms on the sub-warp state groups outside the golden sets: 9
+    species with 60 reactions (8-lane groups, 44 states per CTA after
+    rounding to whole warps) and 18 species with 40 reactions (16-lane
+    groups, two states per warp).  Central differences of the oracle
     source converge to the CUDA Jacobian at second order, and sub-batches
     give the same rows bit for bit."""
     from oracle.thermo_oracle import Thermochemistry as Oracle
     from pyrometheus_gb300 import synthetic
-    sol = synthetic.make_mechanism(synthetic.SPECIES_9, 60, 6, 4, 2, seed=5,
-                                   name="wide9", orient_temperature=1500.0)
+    if which == "wide9":
+        sol = synthetic.make_mechanism(synthetic.SPECIES_9, 60, 6, 4, 2,
+                                       seed=5, name="wide9",
+                                       orient_temperature=1500.0)
+    else:
+        sol = synthetic.make_mechanism(
+            list(synthetic.SPECIES_53[:17]) + ["N2"], 40, 5, 3, 1, seed=7,
+            name="mid18", orient_temperature=1500.0)
     th = _cls(sol)()
     orc = Oracle(sol)
     t, p, y = synthetic.sample_states(sol, 45, seed=9)
